@@ -1,0 +1,235 @@
+"""ORACLE ctypes binding — test infrastructure only.
+
+Loads the C restatement built by oracle/build.py and exposes numpy-level
+helpers to tests/, __graft_entry__.smoke() and bench.py.  Nothing in the
+product package imports this module.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_LIBS = {}
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("Om0", C.c_float), ("redshift", C.c_float), ("dc", C.c_float), ("rhoc", C.c_float),
+        ("Hz", C.c_float), ("Omz", C.c_float), ("rhomz", C.c_float), ("Dv", C.c_float),
+        ("Lc", C.c_float), ("Mcell", C.c_float), ("L", C.c_float * 3), ("Mtot", C.c_float),
+        ("kl", C.c_float * 3), ("Normx", C.c_float), ("Normk", C.c_float),
+        ("nd", C.c_int * 3), ("nz2", C.c_int), ("nmin", C.c_int),
+        ("ng", C.c_size_t),
+        ("Nmin", C.c_int), ("seed", C.c_int), ("DO_EB", C.c_int),
+        ("a", C.c_float), ("beta", C.c_float), ("alpha", C.c_float),
+        ("Lc_d", C.c_double), ("L_d", C.c_double * 3), ("kl_d", C.c_double * 3),
+        ("Normx_d", C.c_double), ("Normk_d", C.c_double), ("Omz_d", C.c_double),
+        ("Hz_d", C.c_double),
+    ]
+
+
+class Result(C.Structure):
+    _fields_ = [
+        ("nh", C.c_size_t), ("np", C.c_size_t),
+        ("Mh", C.c_void_p), ("posh", C.c_void_p), ("hx", C.c_void_p), ("hcount", C.c_void_p),
+        ("delta", C.c_void_p), ("flag", C.c_void_p), ("S", C.c_void_p),
+        ("t_field", C.c_double), ("t_halos", C.c_double), ("t_lpt", C.c_double),
+    ]
+
+
+def lib(prec="f64"):
+    if prec not in _LIBS:
+        paths = _build.build()
+        L = C.CDLL(paths[prec])
+        L.orc_spline_eval.restype = C.c_double
+        L.orc_taus_uniform.restype = C.c_double
+        L.orc_gaussian.restype = C.c_double
+        L.orc_taus_get.restype = C.c_uint32
+        L.orc_count_peaks.restype = C.c_size_t
+        L.orc_find_peaks.restype = C.c_size_t
+        L.orc_grow_halos.restype = C.c_size_t
+        L.orc_find_halos.restype = C.c_size_t
+        L.orc_barrier.restype = C.c_float
+        _LIBS[prec] = L
+    return _LIBS[prec]
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def real_dtype(prec):
+    return np.float32 if prec == "f32" else np.float64
+
+
+def set_threads(n, prec="f64"):
+    lib(prec).orc_set_threads(int(n))
+
+
+def make_params(nd, Lc, Om0=0.31, z=0.0, dc=-1.0, Nmin=1, a=1.0, beta=0.0, alpha=0.0, seed=12345,
+                prec="f64"):
+    L = lib(prec)
+    p = Params()
+    nd3 = nd if isinstance(nd, (tuple, list)) else (nd, nd, nd)
+    L.orc_set_cosmology(C.byref(p), C.c_float(Om0), C.c_float(z), C.c_float(dc))
+    if L.orc_set_box(C.byref(p), int(nd3[0]), int(nd3[1]), int(nd3[2]), C.c_float(Lc)):
+        raise ValueError("unsupported cell size")
+    L.orc_set_barrier(C.byref(p), int(Nmin), C.c_float(a), C.c_float(beta), C.c_float(alpha), int(seed))
+    return p
+
+
+def cells_in_spheres(lmax=10000):
+    out = np.zeros(9000, dtype=np.int32)
+    n = lib().orc_cells_in_spheres(int(lmax), _ptr(out), out.size)
+    return out[:n].copy()
+
+
+def fft_r2c_3d(x, prec="f64"):
+    x = np.ascontiguousarray(x, dtype=real_dtype(prec))
+    nx, ny, nz = x.shape
+    out = np.zeros((nx, ny, nz // 2 + 1, 2), dtype=real_dtype(prec))
+    lib(prec).orc_fft_r2c_3d(nx, ny, nz, _ptr(x), _ptr(out))
+    return out[..., 0] + 1j * out[..., 1]
+
+
+def fft_c2r_3d(xk, nz, prec="f64"):
+    nx, ny, nc = xk.shape
+    a = np.ascontiguousarray(np.stack([xk.real, xk.imag], axis=-1), dtype=real_dtype(prec))
+    out = np.zeros((nx, ny, nz), dtype=real_dtype(prec))
+    lib(prec).orc_fft_c2r_3d(nx, ny, nz, _ptr(a), _ptr(out))
+    return out
+
+
+def sigma_tables(p, k, P, prec64=0, prec="f64"):
+    L = lib(prec)
+    k = np.ascontiguousarray(k, dtype=np.float32)
+    P = np.ascontiguousarray(P, dtype=np.float32)
+    nc = L.orc_ncells(C.byref(p))
+    sig = np.zeros(nc, dtype=np.float32)
+    M = np.zeros(k.size, dtype=np.float64)
+    Int = np.zeros(k.size, dtype=np.float64)
+    r = L.orc_sigma_tables(C.byref(p), _ptr(k), _ptr(P), k.size, int(prec64), _ptr(sig), _ptr(M), _ptr(Int))
+    if r < 0:
+        raise RuntimeError("sigma tables failed")
+    btab = np.zeros(nc, dtype=np.float32)
+    L.orc_barrier_table(C.byref(p), _ptr(sig), nc, _ptr(btab))
+    return {"Sig_grid": sig, "M": M, "Int": Int, "Btab": btab, "Ncells": nc}
+
+
+def field_modes(p, k, P, stream=1, fixed=0, phase=0.0, prec="f64"):
+    L = lib(prec)
+    nd = tuple(p.nd)
+    k = np.ascontiguousarray(k, dtype=np.float32)
+    P = np.ascontiguousarray(P, dtype=np.float32)
+    out = np.zeros((nd[0], nd[1], nd[2] // 2 + 1, 2), dtype=real_dtype(prec))
+    r = L.orc_field_modes(C.byref(p), _ptr(k), _ptr(P), k.size, int(stream), int(fixed),
+                          C.c_float(phase), C.c_float(1e5), _ptr(out))
+    if r:
+        raise RuntimeError(f"field synthesis failed ({r})")
+    return out
+
+
+def field_real(p, modes, prec="f64"):
+    nd = tuple(p.nd)
+    out = np.zeros(nd, dtype=real_dtype(prec))
+    lib(prec).orc_field_real(C.byref(p), _ptr(np.ascontiguousarray(modes)), _ptr(out))
+    return out
+
+
+def find_halos(p, delta, tables, prec="f64"):
+    """Find_Halos on a given float32 grid with given tables."""
+    L = lib(prec)
+    delta = np.ascontiguousarray(delta, dtype=np.float32)
+    ng = delta.size
+    npk = L.orc_count_peaks(C.byref(p), _ptr(delta))
+    cap = max(int(npk), 1)
+    flag = np.zeros(ng, dtype=np.int64)
+    hx = np.zeros(3 * cap, dtype=np.int32)
+    hc = np.zeros(cap, dtype=np.int32)
+    Mh = np.zeros(cap, dtype=np.float32)
+    npo = C.c_size_t(0)
+    btab = np.ascontiguousarray(tables["Btab"], dtype=np.float32)
+    M = np.ascontiguousarray(tables["M"], dtype=np.float64)
+    Int = np.ascontiguousarray(tables["Int"], dtype=np.float64)
+    nh = L.orc_find_halos(C.byref(p), _ptr(delta), _ptr(btab), int(tables["Ncells"]), _ptr(M), _ptr(Int),
+                          M.size, _ptr(flag), _ptr(hx), _ptr(hc), _ptr(Mh), C.c_size_t(cap), C.byref(npo))
+    if nh >= (1 << 63):
+        raise RuntimeError("oracle halo finder reported a range error")
+    return {"nh": nh, "np": npo.value, "x": hx[:3 * nh].reshape(nh, 3), "count": hc[:nh],
+            "Mh": Mh[:nh], "flag": flag}
+
+
+def peaks_sorted(p, delta, prec="f64"):
+    """Peaks in the reference's quicksort order (ascending density)."""
+    L = lib(prec)
+    delta = np.ascontiguousarray(delta, dtype=np.float32)
+    npk = L.orc_count_peaks(C.byref(p), _ptr(delta))
+    pk = np.zeros(max(npk, 1), dtype=[("x", np.int32, 3), ("den", np.float32)])
+    L.orc_find_peaks(C.byref(p), _ptr(delta), _ptr(pk))
+    unsorted = pk[:npk].copy()
+    if npk > 0:
+        L.orc_quicksort_peaks(_ptr(pk), C.c_longlong(0), C.c_longlong(npk - 1))
+    return unsorted, pk[:npk]
+
+
+def quicksort_peaks(pk):
+    pk = np.ascontiguousarray(pk.copy())
+    if pk.size > 0:
+        lib().orc_quicksort_peaks(_ptr(pk), C.c_longlong(0), C.c_longlong(pk.size - 1))
+    return pk
+
+
+def cic(pos, nd, L, prec="f64"):
+    pos = np.ascontiguousarray(pos, dtype=real_dtype(prec)).reshape(-1, 3)
+    grid = np.zeros((nd, nd, nd), dtype=real_dtype(prec))
+    lib(prec).orc_cic(_ptr(pos), C.c_size_t(pos.shape[0]), int(nd), C.c_float(L), _ptr(grid))
+    return grid
+
+
+def power(grid, L, window=2, Nk=25, kmin=None, kmax=None, prec="f64"):
+    nd = grid.shape[-1]
+    if kmin is None:
+        kmin = 2.0 * np.pi / L
+    if kmax is None:
+        kmax = np.pi / L * nd
+    g = np.ascontiguousarray(grid, dtype=real_dtype(prec))
+    km = np.zeros(Nk)
+    Pk = np.zeros(Nk)
+    cnt = np.zeros(Nk, dtype=np.int64)
+    lib(prec).orc_power(_ptr(g), int(nd), C.c_float(L), int(window), int(Nk), C.c_float(np.float32(kmin)),
+                        C.c_float(np.float32(kmax)), _ptr(km), _ptr(Pk), _ptr(cnt))
+    return {"k": km, "Pk": Pk, "Nk": cnt}
+
+
+def halos_box_from_pk(k, P, nd=64, Lc=4.0, Om0=0.31, z=0.0, dc=-1.0, Nmin=1, a=1.0, beta=0.0,
+                      alpha=0.0, seed=12345, stream=0, fixed=0, phase=0.0, k_smooth=10000.0,
+                      do_2lpt=0, prec64=0, keep_S=0, prec="f32"):
+    L = lib(prec)
+    k = np.ascontiguousarray(k, dtype=np.float32)
+    P = np.ascontiguousarray(P, dtype=np.float32)
+    r = Result()
+    st = L.orc_halos_box_from_pk(_ptr(k), _ptr(P), k.size, int(nd), C.c_float(Lc), C.c_float(Om0),
+                                 C.c_float(z), C.c_float(dc), int(Nmin), C.c_float(a), C.c_float(beta),
+                                 C.c_float(alpha), int(seed), int(stream), int(fixed), C.c_float(phase),
+                                 C.c_float(k_smooth), int(do_2lpt), int(prec64), int(keep_S), C.byref(r))
+    if st:
+        raise RuntimeError(f"oracle pipeline failed ({st})")
+    nh, ng = r.nh, nd ** 3
+    rt = real_dtype(prec)
+
+    def arr(ptr, n, dt):
+        if not ptr or n == 0:
+            return np.zeros(0, dtype=dt)
+        return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(np.ctypeslib.as_ctypes_type(dt))), shape=(n,)).copy()
+
+    out = {"nh": nh, "np": r.np, "Mh": arr(r.Mh, nh, np.float32),
+           "posh": arr(r.posh, 3 * nh, rt).reshape(nh, 3), "x": arr(r.hx, 3 * nh, np.int32).reshape(nh, 3),
+           "count": arr(r.hcount, nh, np.int32), "delta": arr(r.delta, ng, np.float32).reshape(nd, nd, nd),
+           "flag": arr(r.flag, ng, np.int64),
+           "t_field": r.t_field, "t_halos": r.t_halos, "t_lpt": r.t_lpt}
+    if keep_S:
+        out["pos"] = arr(r.S, 3 * ng, rt).reshape(ng, 3)
+    L.orc_result_free(C.byref(r))
+    return out
