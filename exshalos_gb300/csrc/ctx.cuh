@@ -1,0 +1,91 @@
+// Library context: cached FFT plans, device work buffers and the results of
+// the last halo call.  One context per host thread.
+#pragma once
+#include <map>
+#include <tuple>
+#include <vector>
+#include <string>
+
+#include "exh_common.cuh"
+#include "fft.cuh"
+
+namespace exh {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  int ensure(size_t bytes) {
+    if (bytes <= cap) return EXH_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = bytes + bytes / 8 + 256;
+    if (cudaMalloc(&p, want) != cudaSuccess) {
+      cudaGetLastError();
+      exh_set_error_msg("device allocation failed", __FILE__, __LINE__);
+      return EXH_E_NOMEM;
+    }
+    cap = want;
+    return EXH_OK;
+  }
+  template <class T> T* as() const { return reinterpret_cast<T*>(p); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+struct HostTables {
+  int Ncells = 0, Nr = 0;
+  std::vector<float> Sig_grid, Btab;
+  std::vector<double> M, Int;
+};
+
+// halo-finder state of the last call (device)
+struct HaloState {
+  int64_t nh = 0, np = 0;
+  int nd[3] = {0, 0, 0};
+  size_t ng = 0;
+  bool have_field = false, have_S = false, have_vel = false;
+  HostTables tab;
+};
+
+enum BufId {
+  B_WORK = 0,     // complex work array of the FFTs
+  B_WORK2,        // second complex work array
+  B_DELTA,        // float field
+  B_GRID,         // float grid
+  B_PHI1,         // first-order potential (float)
+  B_PHI2,         // second-order potential (float)
+  B_S,            // displacements [3][ng]
+  B_V,            // velocities [3][ng]
+  B_FLAG,         // int32 halo flag per cell
+  B_PEAKS,        // peak keys/ids (sort ping-pong)
+  B_PEAKS2,
+  B_SORT,         // sort scratch
+  B_HALO,         // halo records
+  B_HALO2,
+  B_POSH,         // halo positions / velocities
+  B_MH,
+  B_TAB,          // device copies of tables
+  B_SCRATCH,      // per-block partials, counters
+  B_HOSTIO,       // staging for host pointers
+  B_HOSTIO2,
+  B_COUNT
+};
+
+struct Ctx {
+  int device = 0;
+  std::map<std::tuple<int, int, int>, FFTPlan3D> plans;
+  DevBuf buf[B_COUNT];
+  HaloState halos;
+  int64_t launches = 0;
+  int get_plan(int nx, int ny, int nz, FFTPlan3D** out);
+};
+
+}  // namespace exh
+
+struct exh_ctx {
+  exh::Ctx c;
+};

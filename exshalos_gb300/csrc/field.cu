@@ -1,0 +1,59 @@
+// Gaussian field: Philox modes generated inside the first pass of the
+// inverse FFT, scaled by Normx in the last pass (density_grid.c:71-217).
+#include <cmath>
+#include <vector>
+
+#include "ctx.cuh"
+#include "fft.cuh"
+#include "field.cuh"
+#include "pipeline.cuh"
+
+namespace exh {
+
+int upload_amplitudes(Ctx& c, const BoxParams& b, const float* K, const float* P, int Nk, float** A_dev,
+                      cudaStream_t st) {
+  std::vector<float> A;
+  int s = amplitude_table(b, K, P, Nk, A);
+  if (s == EXH_E_UNSUPPORTED) {
+    exh_set_error_msg("the field is built for cubic boxes (ndx == ndy == ndz)", __FILE__, __LINE__);
+    return s;
+  }
+  if (s != EXH_OK) {
+    exh_set_error_msg("P(k) table does not cover the box's wave numbers", __FILE__, __LINE__);
+    return s;
+  }
+  EXH_TRY(c.buf[B_TAB].ensure(sizeof(float) * A.size()));
+  EXH_CUDA_TRY(cudaMemcpyAsync(c.buf[B_TAB].p, A.data(), sizeof(float) * A.size(), cudaMemcpyHostToDevice, st));
+  // the host vector dies here: wait for the copy
+  EXH_CUDA_TRY(cudaStreamSynchronize(st));
+  *A_dev = c.buf[B_TAB].as<float>();
+  return EXH_OK;
+}
+
+FieldModes make_modes(const BoxParams& b, const float* A_dev, int fixed, float phase) {
+  FieldModes m;
+  m.n0 = b.nd[0]; m.n1 = b.nd[1]; m.n2 = b.nd[2]; m.nc = b.nz2;
+  m.seed = (uint32_t)b.seed;
+  m.fixed = fixed;
+  m.use_phase = phase != 0.0f;
+  m.cph = (float)std::cos((double)phase);
+  m.sph = (float)std::sin((double)phase);
+  m.A = A_dev;
+  return m;
+}
+
+int field_real(Ctx& c, const BoxParams& b, const float* K, const float* P, int Nk, int fixed, float phase,
+               float* delta_dev, cudaStream_t st) {
+  FFTPlan3D* p;
+  EXH_TRY(c.get_plan(b.nd[0], b.nd[1], b.nd[2], &p));
+  float* A_dev = nullptr;
+  EXH_TRY(upload_amplitudes(c, b, K, P, Nk, &A_dev, st));
+  const size_t nk = (size_t)b.nd[0] * b.nd[1] * p->nc;
+  EXH_TRY(c.buf[B_WORK].ensure(sizeof(float2) * nk));
+  float2* work = c.buf[B_WORK].as<float2>();
+  FieldGen gen{make_modes(b, A_dev, fixed, phase)};
+  EXH_CUDA_TRY(fft_c2r_3d(*p, gen, work, RealPairStore{delta_dev, b.nd[2], b.Normx}, st));
+  return EXH_OK;
+}
+
+}  // namespace exh

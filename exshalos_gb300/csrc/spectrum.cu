@@ -1,0 +1,213 @@
+// CIC density assignment and the shell-binned power spectrum.
+//
+// grid_compute   <- src/spectrum/spectrum.c:46-108, gridmodule.c:21-53,146-211
+// power_compute  <- src/spectrum/spectrum.c:111-197, powermodule.c:4-108,
+//                   spectrum_h.c:39-70,83-167
+//
+// The power spectrum never stores the transformed grid: the x pass of the
+// real-to-complex FFT deconvolves the window and bins |delta_k|^2 straight
+// from shared memory into per-block FP64 histograms.
+#include <cmath>
+
+#include "ctx.cuh"
+#include "fft.cuh"
+#include "spectrum.cuh"
+
+namespace exh {
+
+// ------------------------------------------------------------------ CIC
+// One thread per tracer: the periodic wrap of spectrum_h.c:17-27, the cell
+// index of spectrum_h.c:73-80 and the eight weights of gridmodule.c:29-50.
+__global__ void k_cic(const float* __restrict__ pos, int64_t np, int nd, float L, float Ld,
+                      float* __restrict__ grid) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  int xt[3], sg[3];
+  float dx[3], t[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    float x = pos[3 * p + a];
+    // at most a few turns for finite input; non-finite input is left alone
+    for (int it = 0; it < 64 && x >= L; it++) x = __fsub_rn(x, L);
+    for (int it = 0; it < 64 && x < 0.f; it++) x = __fadd_rn(x, L);
+    if (!(x >= 0.f && x < L)) return;
+    const float q = __fdiv_rn(x, Ld);
+    int c = (int)floorf(q);
+    if (c >= nd) c = nd - 1;
+    xt[a] = c;
+    float d = __fsub_rn(q, (float)c + 0.5f);
+    if (d >= 0.f) { sg[a] = 1; }
+    else { sg[a] = -1; d = -d; }
+    dx[a] = d;
+    t[a] = __fsub_rn(1.f, d);
+  }
+  const int x0 = xt[0], y0 = xt[1], z0 = xt[2];
+  const int x1 = exh_wrap(x0, sg[0], nd), y1 = exh_wrap(y0, sg[1], nd), z1 = exh_wrap(z0, sg[2], nd);
+  const size_t n2 = (size_t)nd * nd;
+  atomicAdd(&grid[x0 * n2 + (size_t)y0 * nd + z0], t[0] * t[1] * t[2]);
+  atomicAdd(&grid[x1 * n2 + (size_t)y0 * nd + z0], dx[0] * t[1] * t[2]);
+  atomicAdd(&grid[x0 * n2 + (size_t)y1 * nd + z0], t[0] * dx[1] * t[2]);
+  atomicAdd(&grid[x0 * n2 + (size_t)y0 * nd + z1], t[0] * t[1] * dx[2]);
+  atomicAdd(&grid[x1 * n2 + (size_t)y1 * nd + z0], dx[0] * dx[1] * t[2]);
+  atomicAdd(&grid[x1 * n2 + (size_t)y0 * nd + z1], dx[0] * t[1] * dx[2]);
+  atomicAdd(&grid[x0 * n2 + (size_t)y1 * nd + z1], t[0] * dx[1] * dx[2]);
+  atomicAdd(&grid[x1 * n2 + (size_t)y1 * nd + z1], dx[0] * dx[1] * dx[2]);
+}
+
+// delta = rho / (np / ng) - 1   (gridmodule.c:206-211)
+__global__ void k_cic_normalise(float* __restrict__ grid, size_t ng, float inv_mean) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (; i < ng; i += stride) grid[i] = grid[i] * inv_mean - 1.f;
+}
+
+int cic_assign(Ctx& c, const float* pos_dev, int64_t np, int nd, float L, float* grid_dev, cudaStream_t st) {
+  const size_t ng = (size_t)nd * nd * nd;
+  EXH_CUDA_TRY(cudaMemsetAsync(grid_dev, 0, sizeof(float) * ng, st));
+  const float Ld = L / (float)nd;
+  if (np > 0) {
+    k_cic<<<exh_div_up(np, 256), 256, 0, st>>>(pos_dev, np, nd, L, Ld, grid_dev);
+    count_launch(1);
+    EXH_CUDA_TRY(cudaGetLastError());
+  }
+  // np == 0 gives 0/0 in the reference; the grid is returned as -1 + nan there.
+  const float inv_mean = np > 0 ? (float)((double)ng / (double)np) : NAN;
+  k_cic_normalise<<<EXH_NUM_SMS * 8, 256, 0, st>>>(grid_dev, ng, inv_mean);
+  count_launch(1);
+  EXH_CUDA_TRY(cudaGetLastError());
+  return EXH_OK;
+}
+
+// ------------------------------------------------------------------ P(k)
+__device__ __forceinline__ float sinc_f(float x) { return x != 0.f ? sinf(x) / x : 1.f; }
+
+// x pass of the forward transform with the binning epilogue.
+// Tile: all nx modes of FFT_W adjacent (y, kz) columns.
+__global__ void __launch_bounds__(FFT_THREADS)
+k_fft_x_bin(const float2* __restrict__ work, RadixPlan pl, const float2* __restrict__ tw, int nd, int nc,
+            BinParams bp, double* __restrict__ partP, double* __restrict__ partK,
+            unsigned int* __restrict__ partN) {
+  extern __shared__ float2 smem[];
+  const int n = pl.n;
+  float2* b0 = smem;
+  float2* b1 = smem + n * FFT_W;
+  double* hP = reinterpret_cast<double*>(smem + 2 * n * FFT_W);
+  double* hK = hP + bp.Nk;
+  unsigned int* hN = reinterpret_cast<unsigned int*>(hK + bp.Nk);
+  const int inner = nd * nc;
+  const int i0 = blockIdx.x * FFT_W;
+  const int nb = min(FFT_W, inner - i0);
+  for (int b = threadIdx.x; b < bp.Nk; b += blockDim.x) { hP[b] = 0.0; hK[b] = 0.0; hN[b] = 0u; }
+  for (int t = threadIdx.x; t < n * FFT_W; t += blockDim.x) {
+    const int e = t / FFT_W, b = t % FFT_W;
+    b0[e * FFT_W + b] = (b < nb) ? work[(size_t)e * inner + i0 + b] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const float2* res = stockham_run(b0, b1, pl, FFT_W, FFT_W, tw, -1.f);
+  for (int t = threadIdx.x; t < n * FFT_W; t += blockDim.x) {
+    const int i = t / FFT_W, b = t % FFT_W;
+    if (b >= nb) continue;
+    const int col = i0 + b, j = col / nc, k = col % nc;
+    // mode-skip rule of powermodule.c:50-51 on the kz = 0 and kz = nd/2 planes
+    if ((k == 0 || k == nd / 2) &&
+        ((i > nd / 2 && j > nd / 2) || i == 0 || i == nd / 2 || j == 0 || j == nd / 2 || (i > nd / 2 && j < nd / 2)))
+      continue;
+    // wave numbers and bin index in the reference's float arithmetic
+    const float kx = (float)((2 * i < nd) ? i : i - nd) * bp.kn;
+    const float ky = (float)((2 * j < nd) ? j : j - nd) * bp.kn;
+    const float kz = (float)((2 * k < nd) ? k : k - nd) * bp.kn;
+    const float k2 = __fadd_rn(__fadd_rn(__fmul_rn(kx, kx), __fmul_rn(ky, ky)), __fmul_rn(kz, kz));
+    const float kmod = __fsqrt_rn(k2);
+    const int bin = (int)floorf(__fdiv_rn(__fsub_rn(kmod, bp.kmin), bp.dk));
+    if (bin < 0 || bin >= bp.Nk) continue;
+    float w = 1.f;
+    if (bp.window == 1 || bp.window == 2) {
+      w = sinc_f(kx * bp.Lb * 0.5f) * sinc_f(ky * bp.Lb * 0.5f) * sinc_f(kz * bp.Lb * 0.5f);
+      if (bp.window == 2) w = w * w;
+    }
+    const float2 v = res[i * FFT_W + b];
+    const double s = (double)bp.Normk / (double)w;
+    const double re = (double)v.x * s, im = (double)v.y * s;
+    atomicAdd(&hP[bin], re * re + im * im);
+    atomicAdd(&hK[bin], (double)kmod);
+    atomicAdd(&hN[bin], 1u);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < bp.Nk; b += blockDim.x) {
+    partP[(size_t)blockIdx.x * bp.Nk + b] = hP[b];
+    partK[(size_t)blockIdx.x * bp.Nk + b] = hK[b];
+    partN[(size_t)blockIdx.x * bp.Nk + b] = hN[b];
+  }
+}
+
+// per-bin sums over blocks, fixed order
+__global__ void k_bin_reduce(const double* __restrict__ partP, const double* __restrict__ partK,
+                             const unsigned int* __restrict__ partN, int nblk, int Nk, double* __restrict__ outP,
+                             double* __restrict__ outK, long long* __restrict__ outN) {
+  const int b = blockIdx.x;
+  double sP = 0.0, sK = 0.0;
+  unsigned long long sN = 0;
+  for (int q = threadIdx.x; q < nblk; q += blockDim.x) {
+    sP += partP[(size_t)q * Nk + b];
+    sK += partK[(size_t)q * Nk + b];
+    sN += partN[(size_t)q * Nk + b];
+  }
+  __shared__ double rP[256], rK[256];
+  __shared__ unsigned long long rN[256];
+  rP[threadIdx.x] = sP; rK[threadIdx.x] = sK; rN[threadIdx.x] = sN;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      rP[threadIdx.x] += rP[threadIdx.x + s];
+      rK[threadIdx.x] += rK[threadIdx.x + s];
+      rN[threadIdx.x] += rN[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const unsigned long long n = rN[0];
+    outN[b] = (long long)n;
+    outP[b] = n ? rP[0] / (double)n : 0.0;     // (4l+1) = 1 for l = 0
+    outK[b] = n ? rK[0] / (double)n : 0.0;
+  }
+}
+
+int power_spectrum(Ctx& c, const float* grid_dev, int nd, float L, int window, int Nk, float kmin, float kmax,
+                   double* outP_dev, double* outK_dev, long long* outN_dev, cudaStream_t st) {
+  FFTPlan3D* p;
+  EXH_TRY(c.get_plan(nd, nd, nd, &p));
+  const size_t nk = (size_t)nd * nd * p->nc;
+  EXH_TRY(c.buf[B_WORK].ensure(sizeof(float2) * nk));
+  float2* work = c.buf[B_WORK].as<float2>();
+  // z and y passes of the forward transform
+  const size_t rows = (size_t)nd * nd;
+  EXH_CUDA_TRY(launch_r2c_rows(RealPairLoad{grid_dev, nd}, HalfStore{work, p->nc}, *p, rows, st));
+  EXH_CUDA_TRY(launch_strided(CplxLoad{work, nd, p->nc}, CplxStore{work, nd, p->nc}, p->py, p->twy, -1.f, nd,
+                              p->nc, st));
+  // x pass + binning
+  BinParams bp;
+  bp.Nk = Nk;
+  bp.kn = (float)(2 * M_PI / L);                      // powermodule.c:7
+  bp.kmin = kmin;
+  bp.dk = (kmax - kmin) / (float)Nk;                  // powermodule.c:11
+  bp.Lb = L / (float)nd;
+  bp.Normk = (float)pow((double)(L / (float)(nd * nd)), 1.5);   // spectrum_h.c:90
+  bp.window = window;
+  const int inner = nd * p->nc;
+  const int nblk = (int)exh_div_up(inner, FFT_W);
+  EXH_TRY(c.buf[B_SCRATCH].ensure((sizeof(double) * 2 + sizeof(unsigned)) * (size_t)nblk * Nk));
+  double* partP = c.buf[B_SCRATCH].as<double>();
+  double* partK = partP + (size_t)nblk * Nk;
+  unsigned* partN = reinterpret_cast<unsigned*>(partK + (size_t)nblk * Nk);
+  const size_t sm = smem_strided(nd) + (size_t)Nk * (2 * sizeof(double) + sizeof(unsigned)) + 16;
+  EXH_CUDA_TRY(set_smem(k_fft_x_bin, sm));
+  k_fft_x_bin<<<nblk, FFT_THREADS, sm, st>>>(work, p->px, p->twx, nd, p->nc, bp, partP, partK, partN);
+  count_launch(1);
+  EXH_CUDA_TRY(cudaGetLastError());
+  k_bin_reduce<<<Nk, 256, 0, st>>>(partP, partK, partN, nblk, Nk, outP_dev, outK_dev, outN_dev);
+  count_launch(1);
+  EXH_CUDA_TRY(cudaGetLastError());
+  return EXH_OK;
+}
+
+}  // namespace exh

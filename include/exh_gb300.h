@@ -1,0 +1,148 @@
+/*
+ * exh_gb300 — C ABI of the GB300 (sm_103a) implementation of the ExSHalos
+ * mock-generation path: Gaussian field from a tabulated P(k), halo finding by
+ * sphere growth with exclusion, (2)LPT displacement, CIC assignment and the
+ * shell-binned power spectrum.
+ *
+ * Plain C types only.  Every function returns an int status (EXH_OK = 0);
+ * exh_last_error() gives the text of the most recent failure on the calling
+ * thread.  Buffers belong to the caller; `mem` says whether the pointers are
+ * host (EXH_MEM_HOST) or device (EXH_MEM_DEVICE) memory.  `stream` is a
+ * cudaStream_t (NULL = legacy default stream).  A context is not reentrant:
+ * use one per host thread.
+ *
+ * Each entry point names the reference interface it replaces
+ * (paths relative to the Voivodic/ExSHalos tree).
+ */
+#ifndef EXH_GB300_H
+#define EXH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes.  The reference reports failures with printf + exit(0)
+ * (include/exshalos/exshalos_h.h:40-44) or a GSL abort; here they come back
+ * as codes that the Python layer raises as exceptions. */
+#define EXH_OK 0
+#define EXH_E_INVALID 1      /* argument outside what the path accepts   -> ValueError   */
+#define EXH_E_NOMEM 2        /* device or host allocation failed         -> MemoryError  */
+#define EXH_E_CUDA 3         /* CUDA runtime error                       -> RuntimeError */
+#define EXH_E_RANGE 4        /* halo beyond the sigma table / spline domain -> RuntimeError */
+#define EXH_E_TIMEOUT 5      /* a bounded device-side wait expired       -> RuntimeError */
+#define EXH_E_UNSUPPORTED 6  /* reference option not built here          -> NotImplementedError */
+#define EXH_E_NO_DEVICE 7    /* no CUDA device / driver                  -> RuntimeError */
+
+#define EXH_MEM_HOST 0
+#define EXH_MEM_DEVICE 1
+
+/* Gaussian-field random streams */
+#define EXH_FIELD_PHILOX 1   /* counter-based Philox4x32-10 per Fourier mode (default) */
+
+typedef struct exh_ctx exh_ctx;
+
+int exh_ctx_create(int device, exh_ctx **out);
+int exh_ctx_destroy(exh_ctx *ctx);
+const char *exh_strerror(int code);
+const char *exh_last_error(void);
+int exh_version(void);
+
+/* check_precision (src/exshalos/exshalos.c:41-43, src/spectrum/spectrum.c:41-43):
+ * size of the grid scalar, 4 (float32). */
+int exh_check_precision(void);
+
+/* ------------------------------------------------------------------------
+ * grid_compute (src/spectrum/spectrum.c:46-108 -> Tracer_Grid,
+ * src/spectrum/gridmodule.c:146-211): density contrast of np tracers on an
+ * nd^3 grid.  Supported: window 2 (CIC), one tracer type, unit mass, no
+ * interlacing, no redshift-space shift, folds >= 1.
+ * pos[3*np], grid[nd^3] (x-major, z fastest).  */
+int exh_grid_compute(exh_ctx *ctx, const float *pos, int64_t np, int nd, float L, int window,
+                     int folds, float *grid, int mem, void *stream);
+
+/* ------------------------------------------------------------------------
+ * power_compute (src/spectrum/spectrum.c:111-197 -> Power_Spectrum,
+ * src/spectrum/powermodule.c:4-108): shell-binned auto power spectrum of
+ * one grid, l_max = 0, no interlacing, window 0 (none), 1 (NGP), 2 (CIC)
+ * deconvolved.  grid is in `mem`; k_out[Nk], P_out[Nk], count_out[Nk] are
+ * host memory. Bin sums run in FP64. */
+int exh_power_compute(exh_ctx *ctx, const float *grid, int nd, float L, int window, int Nk,
+                      float k_min, float k_max, float *k_out, float *P_out, int64_t *count_out,
+                      int mem, void *stream);
+
+/* ------------------------------------------------------------------------
+ * halos_box_from_pk (src/exshalos/exshalos.c:710-940 ->
+ * Generate_Halos_Box_from_Pk, src/exshalos/box.c:4-68).  Field arguments
+ * mirror the reference keyword list (exshalos.c:718).  Results stay in the
+ * context until fetched with exh_halos_fetch(). */
+typedef struct {
+  float R_max;                 /* only the default 1e5 (no FFTLog truncation) is built   */
+  int ndx, ndy, ndz;
+  float Lc;                    /* cell size, Mpc/h                                       */
+  int seed;
+  float k_smooth;
+  float Om0, redshift, dc;     /* dc <= 0: 1.686 Omega_m(z)^0.0055                       */
+  int Nmin;
+  float a, beta, alpha;        /* barrier; DO_EB unless (1, 0, 0)                        */
+  int fixed;
+  float phase;
+  int OUT_DEN, OUT_LPT, OUT_VEL, DO_2LPT, OUT_FLAG, OUT_PROF;
+  int verbose, nthreads;       /* nthreads is accepted and ignored (one GPU)             */
+  int field_stream;            /* EXH_FIELD_PHILOX                                       */
+  int setup_fp64;              /* 1: sigma(M) and mass-function tables in FP64;
+                                  0: the reference's float arithmetic                    */
+} exh_halo_params;
+
+void exh_halo_params_default(exh_halo_params *p);
+
+int exh_halos_box_from_pk(exh_ctx *ctx, const float *k, const float *P, int Nk,
+                          const exh_halo_params *prm, int64_t *nh_out, void *stream);
+
+/* find_halos (src/exshalos/exshalos.c:509-610 -> Find_Halos,
+ * src/exshalos/find_halos.c:479-563) on a caller-given float grid (in `mem`).
+ * Halos stay in the context (exh_halos_fetch; posh = Lagrangian centre). */
+int exh_find_halos(exh_ctx *ctx, const float *delta, int ndx, int ndy, int ndz, const float *k,
+                   const float *P, int Nk, const exh_halo_params *prm, int mem, int64_t *nh_out,
+                   void *stream);
+
+/* Copy results of the last halos call into caller buffers (host or device
+ * per `mem`; NULL skips an output).  posh/velh [3*nh], Mh[nh], Lagrangian
+ * centre cells xc[3*nh], member counts count[nh]; grid[ng] the Gaussian
+ * field; pos/vel [3*ng] particle positions; flag[ng] the host-halo flag
+ * (ng = unclaimed, -h at a centre, ng+1 for halos below Nmin). */
+int exh_halos_fetch(exh_ctx *ctx, float *posh, float *velh, float *Mh, int32_t *xc,
+                    int32_t *count, float *grid, float *pos, float *vel, int64_t *flag, int mem,
+                    void *stream);
+
+/* Halo-finder tables of the last call (host memory): Sig_grid[Ncells],
+ * barrier B(Sig_grid)[Ncells], mass-function knots M[Nr], Int[Nr]. */
+int exh_halo_tables(exh_ctx *ctx, int *Ncells, int *Nr, float *Sig_grid, float *Btab, double *M,
+                    double *Int);
+
+/* ------------------------------------------------------------------------
+ * Stage hooks used by the parity tests (device buffers owned by the
+ * context; results copied to caller memory).
+ * Gaussian field only (density_grid_compute, src/exshalos/exshalos.c:46-121
+ * -> Compute_Den, src/exshalos/density_grid.c:71-217): delta[ng]. */
+int exh_density_grid_compute(exh_ctx *ctx, const float *k, const float *P, int Nk,
+                             const exh_halo_params *prm, float *delta, int mem, void *stream);
+
+/* 3-D FFTs with FFTW conventions (unnormalised, half-complex last axis,
+ * interleaved float2) — the transforms fftwf_plan_dft_r2c_3d /
+ * fftwf_plan_dft_c2r_3d perform at src/spectrum/spectrum_h.c:103-107 and
+ * src/exshalos/density_grid.c:208,225.  Device pointers only. c2r may
+ * overwrite its input. */
+int exh_fft_r2c_3d(exh_ctx *ctx, int nx, int ny, int nz, const float *in, float *out, void *stream);
+int exh_fft_c2r_3d(exh_ctx *ctx, int nx, int ny, int nz, float *in, float *out, void *stream);
+
+/* Number of kernels launched by this context since creation (counted on the
+ * host at each launch). */
+int64_t exh_launch_count(exh_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
