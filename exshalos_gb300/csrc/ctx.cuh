@@ -42,12 +42,15 @@ struct HostTables {
   std::vector<double> M, Int;
 };
 
-// halo-finder state of the last call (device)
+// results of the last halo call (device pointers into the context buffers)
 struct HaloState {
-  int64_t nh = 0, np = 0;
+  int64_t nh = 0, np = 0, nproc = 0;
   int nd[3] = {0, 0, 0};
   size_t ng = 0;
-  bool have_field = false, have_S = false, have_vel = false;
+  float *posh = nullptr, *velh = nullptr, *Mh = nullptr;
+  int *count = nullptr, *xc = nullptr;
+  float *delta = nullptr, *pos = nullptr, *vel = nullptr;
+  int *flag = nullptr, *hid = nullptr;
   HostTables tab;
 };
 

@@ -1,0 +1,990 @@
+// Halo finder (src/exshalos/find_halos.c:108-563) on sm_103a.
+//
+//  find_peaks   Count_Peaks/Find_Peaks (:108-156): strict 6-neighbour maxima,
+//               compacted in row-major order.
+//  sort_peaks   quickSort_peaks (:175-197) reproduced exactly, tie order
+//               included.  Each Lomuto partition is computed in parallel:
+//               elements <= pivot keep their order at their L-rank; an
+//               element > pivot at relative position a moves along
+//               a <- a + g(a) (g = number of > elements before the L with
+//               rank a) until a >= nL; the one landing on nL swaps with the
+//               pivot into the last slot.  Runs of equal g are crossed in one
+//               step, so each element costs O(distinct g values crossed).
+//               Large segments use all SMs per level; segments of at most
+//               SORT_SMALL elements finish inside one block, one warp per
+//               pending segment.
+//  grow_halos   Grow_Halos (:215-379) with deterministic reservations: every
+//               pending peak reserves the cells its exclusion-free growth
+//               could read; peaks holding all their cells are grown exactly
+//               (double running means in the reference's operation order,
+//               no contraction) in the same round.  Halo numbers are assigned
+//               afterwards in processing order.
+//  halo_masses  Compute_Mass (:455-476): the taus stream is advanced to each
+//               halo's draw by GF(2) jump matrices.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "halos.cuh"
+#include "scan.cuh"
+
+namespace exh {
+
+// ------------------------------------------------------------------ shells
+int build_shell_tables(Ctx& c, const BoxParams& b, int Ncells, ShellTable* t, cudaStream_t st) {
+  const int T = b.nmin / 2;
+  const std::vector<int>& cis = cells_in_spheres();
+  // last shell needed: the first r^2 whose cumulative count reaches Ncells
+  long cum = 0;
+  int gmax = -1;
+  std::vector<long> hist;
+  const int tmax = 64;
+  hist.assign((size_t)3 * tmax * tmax + 1, 0);
+  for (int i = -tmax; i <= tmax; i++)
+    for (int j = -tmax; j <= tmax; j++)
+      for (int k = -tmax; k <= tmax; k++) {
+        const int d = i * i + j * j + k * k;
+        if (d < (int)hist.size()) hist[d]++;
+      }
+  for (int g = 0; g < tmax * tmax; g++) {
+    cum += hist[g];
+    if (cum >= Ncells) { gmax = g; break; }
+  }
+  (void)cis;
+  if (gmax < 0) {
+    exh_set_error_msg("Ncells beyond the shell table", __FILE__, __LINE__);
+    return EXH_E_RANGE;
+  }
+  t->gmax = gmax;
+  const int r = (int)std::floor(std::sqrt((double)gmax)) + 1;
+  std::vector<int> oc, oa, sc(gmax + 2, 0), sa(gmax + 2, 0);
+  for (int g = 0; g <= gmax; g++) {
+    sc[g] = (int)oc.size();
+    sa[g] = (int)oa.size();
+    const int tg = (int)std::floor(std::sqrt((double)g));
+    for (int i = -tg; i <= tg; i++)
+      for (int j = -tg; j <= tg; j++)
+        for (int k = -tg; k <= tg; k++) {
+          if (i * i + j * j + k * k != g) continue;
+          const int packed = (i + 128) | ((j + 128) << 8) | ((k + 128) << 16);
+          oa.push_back(packed);
+          if (std::abs(i) <= T && std::abs(j) <= T && std::abs(k) <= T) oc.push_back(packed);
+        }
+  }
+  sc[gmax + 1] = (int)oc.size();
+  sa[gmax + 1] = (int)oa.size();
+  (void)r;
+  const size_t bytes = sizeof(int) * (oc.size() + oa.size() + 2 * (size_t)(gmax + 2));
+  EXH_TRY(c.buf[B_HALO2].ensure(bytes));
+  int* base = c.buf[B_HALO2].as<int>();
+  t->off_cap = base;
+  t->off_all = base + oc.size();
+  t->start_cap = t->off_all + oa.size();
+  t->start_all = t->start_cap + (gmax + 2);
+  std::vector<int> host;
+  host.reserve(bytes / 4);
+  host.insert(host.end(), oc.begin(), oc.end());
+  host.insert(host.end(), oa.begin(), oa.end());
+  host.insert(host.end(), sc.begin(), sc.end());
+  host.insert(host.end(), sa.begin(), sa.end());
+  EXH_CUDA_TRY(cudaMemcpyAsync(base, host.data(), bytes, cudaMemcpyHostToDevice, st));
+  EXH_CUDA_TRY(cudaStreamSynchronize(st));
+  return EXH_OK;
+}
+
+__device__ __forceinline__ void unpack_off(int p, int& i, int& j, int& k) {
+  i = (p & 0xff) - 128;
+  j = ((p >> 8) & 0xff) - 128;
+  k = ((p >> 16) & 0xff) - 128;
+}
+
+// ------------------------------------------------------------------ peaks
+__device__ __forceinline__ bool is_peak(const float* __restrict__ d, int i, int j, int k, int n0, int n1, int n2,
+                                        float den) {
+  const size_t s1 = n2, s0 = (size_t)n1 * n2;
+  const size_t c = (size_t)i * s0 + (size_t)j * s1;
+  return den > d[(size_t)exh_wrap(i, 1, n0) * s0 + (size_t)j * s1 + k] &&
+         den > d[(size_t)exh_wrap(i, -1, n0) * s0 + (size_t)j * s1 + k] &&
+         den > d[(size_t)i * s0 + (size_t)exh_wrap(j, 1, n1) * s1 + k] &&
+         den > d[(size_t)i * s0 + (size_t)exh_wrap(j, -1, n1) * s1 + k] &&
+         den > d[c + exh_wrap(k, 1, n2)] && den > d[c + exh_wrap(k, -1, n2)];
+}
+
+constexpr int PK_T = 256;
+
+__global__ void k_peak_mask(const float* __restrict__ d, int n0, int n1, int n2, size_t ng,
+                            unsigned* __restrict__ mask, unsigned* __restrict__ cnt) {
+  const size_t cell = (size_t)blockIdx.x * PK_T + threadIdx.x;
+  bool pk = false;
+  if (cell < ng) {
+    const int k = (int)(cell % n2);
+    const size_t r = cell / n2;
+    const int j = (int)(r % n1), i = (int)(r / n1);
+    pk = is_peak(d, i, j, k, n0, n1, n2, d[cell]);
+  }
+  const unsigned m = __ballot_sync(0xffffffffu, pk);
+  __shared__ unsigned wc[PK_T / 32];
+  if ((threadIdx.x & 31) == 0) {
+    mask[cell >> 5] = m;
+    wc[threadIdx.x >> 5] = __popc(m);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned s = 0;
+    for (int w = 0; w < PK_T / 32; w++) s += wc[w];
+    cnt[blockIdx.x] = s;
+  }
+}
+
+__global__ void k_peak_write(const float* __restrict__ d, size_t ng, const unsigned* __restrict__ mask,
+                             const unsigned* __restrict__ off, float* __restrict__ key, unsigned* __restrict__ id) {
+  const size_t cell = (size_t)blockIdx.x * PK_T + threadIdx.x;
+  __shared__ unsigned wo[PK_T / 32];
+  const unsigned m = mask[cell >> 5];
+  if (threadIdx.x == 0) {
+    unsigned s = 0;
+    for (int w = 0; w < PK_T / 32; w++) {
+      wo[w] = s;
+      s += __popc(mask[((size_t)blockIdx.x * PK_T >> 5) + w]);
+    }
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  if (cell < ng && ((m >> lane) & 1u)) {
+    const unsigned pos = off[blockIdx.x] + wo[threadIdx.x >> 5] + __popc(m & ((1u << lane) - 1u));
+    key[pos] = d[cell];
+    id[pos] = (unsigned)cell;
+  }
+}
+
+int find_peaks(Ctx& c, const float* delta, const BoxParams& b, HaloDev* h, cudaStream_t st) {
+  const size_t ng = b.ng;
+  const unsigned nb = exh_div_up(ng, PK_T);
+  const size_t words = (size_t)nb * (PK_T / 32);
+  // scratch: mask words, block counts, block offsets, scan sums, total
+  EXH_TRY(c.buf[B_SORT].ensure(sizeof(unsigned) * (words + 3 * (size_t)nb + 64)));
+  unsigned* mask = c.buf[B_SORT].as<unsigned>();
+  unsigned* cnt = mask + words;
+  unsigned* off = cnt + nb;
+  unsigned* sums = off + nb;
+  unsigned* total = sums + nb + 32;
+  k_peak_mask<<<nb, PK_T, 0, st>>>(delta, b.nd[0], b.nd[1], b.nd[2], ng, mask, cnt);
+  count_launch(1);
+  EXH_CUDA_TRY(cudaGetLastError());
+  EXH_CUDA_TRY(exclusive_scan<unsigned>(cnt, off, nb, sums, total, st));
+  unsigned np = 0;
+  EXH_CUDA_TRY(cudaMemcpyAsync(&np, total, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  EXH_CUDA_TRY(cudaStreamSynchronize(st));
+  h->np = np;
+  const size_t cap = std::max<size_t>(np, 1);
+  EXH_TRY(c.buf[B_PEAKS].ensure((sizeof(float) + sizeof(unsigned)) * cap * 3));
+  h->key = c.buf[B_PEAKS].as<float>();
+  h->id = reinterpret_cast<unsigned*>(h->key + cap);
+  k_peak_write<<<nb, PK_T, 0, st>>>(delta, ng, mask, off, h->key, h->id);
+  count_launch(1);
+  EXH_CUDA_TRY(cudaGetLastError());
+  return EXH_OK;
+}
+
+// ------------------------------------------------------------------ sort
+constexpr int SORT_SMALL = 4096;     // segment size finished inside one block
+constexpr int SORT_T = 512;
+constexpr int CH_T = 256, CH_ITEMS = 8, CH = CH_T * CH_ITEMS;
+
+struct Seg {
+  int lo, hi;   // inclusive
+  int buf;      // ping-pong buffer holding the segment
+  int pad;
+};
+
+// Final position (relative) of the > element at relative position a.
+// lam: nondecreasing L-counts before each > element (m of them).
+template <typename LamT>
+__device__ __forceinline__ int lomuto_g_dest(int a, int nL, int m, LamT lam) {
+  while (a < nL) {
+    int lo = 0, hi = m;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (lam(mid) <= a) lo = mid + 1;
+      else hi = mid;
+    }
+    const int c = lo;                              // >= 1
+    const int bnd = c < m ? min(lam(c), nL) : nL;
+    const int steps = (bnd - a + c - 1) / c;
+    a += c * steps;
+  }
+  return a;
+}
+
+// per-chunk L counts
+__global__ void k_qs_count(const float* __restrict__ key, const Seg* __restrict__ segs, const int* __restrict__ cseg,
+                           const int* __restrict__ coff, int nchunks, int* __restrict__ cL) {
+  const int ch = blockIdx.x;
+  if (ch >= nchunks) return;
+  const Seg s = segs[cseg[ch]];
+  const float pv = key[s.hi];
+  const int start = s.lo + coff[ch], end = min(start + CH, s.hi);
+  int n = 0;
+  for (int p = start + threadIdx.x; p < end; p += CH_T) n += key[p] <= pv;
+  __shared__ int ws[32];
+  int tot;
+  block_exclusive_scan<int>(n, ws, tot);
+  if (threadIdx.x == 0) cL[ch] = tot;
+}
+
+__global__ void k_qs_seg_scan(const int* __restrict__ cfirst, int nseg, int* __restrict__ cL,
+                              int* __restrict__ segNL) {
+  const int sidx = blockIdx.x;
+  if (sidx >= nseg) return;
+  const int c0 = cfirst[sidx], c1 = cfirst[sidx + 1];
+  __shared__ int ws[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = c0; base < c1; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    const int v = i < c1 ? cL[i] : 0;
+    int tot;
+    const int ex = block_exclusive_scan<int>(v, ws, tot);
+    if (i < c1) cL[i] = carry + ex;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) segNL[sidx] = carry;
+}
+
+// L placement, lam, pivot (phase 1) and > placement (phase 2)
+template <int PHASE>
+__global__ void k_qs_place(const float* __restrict__ key, const unsigned* __restrict__ id, const Seg* __restrict__ segs,
+                           const int* __restrict__ cseg, const int* __restrict__ coff, int nchunks,
+                           const int* __restrict__ cLoff, const int* __restrict__ segNL, int* __restrict__ lam,
+                           float* __restrict__ okey, unsigned* __restrict__ oid, float* __restrict__ fkey,
+                           unsigned* __restrict__ fid) {
+  const int ch = blockIdx.x;
+  if (ch >= nchunks) return;
+  const int sidx = cseg[ch];
+  const Seg s = segs[sidx];
+  const float pv = key[s.hi];
+  const int nL = segNL[sidx];
+  const int start = s.lo + coff[ch], end = min(start + CH, s.hi);
+  const int base = start + threadIdx.x * CH_ITEMS;
+  bool isL[CH_ITEMS];
+  int n = 0;
+#pragma unroll
+  for (int q = 0; q < CH_ITEMS; q++) {
+    const int p = base + q;
+    isL[q] = p < end && key[p] <= pv;
+    n += isL[q];
+  }
+  __shared__ int ws[32];
+  int tot;
+  int rank = block_exclusive_scan<int>(n, ws, tot) + cLoff[ch];
+  const int m = (s.hi - s.lo) - nL;
+#pragma unroll
+  for (int q = 0; q < CH_ITEMS; q++) {
+    const int p = base + q;
+    if (p >= end) break;
+    if (isL[q]) {
+      if (PHASE == 1) {
+        okey[s.lo + rank] = key[p];
+        oid[s.lo + rank] = id[p];
+      }
+      rank++;
+    } else {
+      const int rel = p - s.lo;
+      if (PHASE == 1) {
+        lam[s.lo + (rel - rank)] = rank;
+      } else {
+        const int* lseg = lam + s.lo;
+        int a = lomuto_g_dest(rel, nL, m, [lseg](int i) { return __ldg(&lseg[i]); });
+        const int dest = (a == nL) ? (s.hi - s.lo) : a;
+        okey[s.lo + dest] = key[p];
+        oid[s.lo + dest] = id[p];
+      }
+    }
+  }
+  if (PHASE == 1 && coff[ch] == 0 && threadIdx.x == 0) {
+    okey[s.lo + nL] = key[s.hi];
+    oid[s.lo + nL] = id[s.hi];
+    fkey[s.lo + nL] = key[s.hi];
+    fid[s.lo + nL] = id[s.hi];
+  }
+}
+
+// copy finished single elements into the final arrays
+__global__ void k_qs_copy_single(const int* __restrict__ pos, const int* __restrict__ bufi, int n,
+                                 float* const* __restrict__ kb, unsigned* const* __restrict__ ib,
+                                 float* __restrict__ fkey, unsigned* __restrict__ fid) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int p = pos[t];
+  fkey[p] = kb[bufi[t]][p];
+  fid[p] = ib[bufi[t]][p];
+}
+
+struct SmallSortBuffers {
+  float* kb[2];
+  unsigned* ib[2];
+};
+
+// One block sorts one segment of at most SORT_SMALL elements; one warp per
+// pending sub-segment (work stack in shared memory).
+__global__ void __launch_bounds__(SORT_T)
+k_qs_small(const Seg* __restrict__ segs, int nseg, SmallSortBuffers bufs, float* __restrict__ fkey,
+           unsigned* __restrict__ fid, int* __restrict__ err) {
+  extern __shared__ unsigned char sm_raw[];
+  float* ka = reinterpret_cast<float*>(sm_raw);
+  unsigned* ia = reinterpret_cast<unsigned*>(ka + SORT_SMALL);
+  float* kb = reinterpret_cast<float*>(ia + SORT_SMALL);
+  unsigned* ib = reinterpret_cast<unsigned*>(kb + SORT_SMALL);
+  int* lam = reinterpret_cast<int*>(ib + SORT_SMALL);
+  int* stk = lam + SORT_SMALL;                       // pairs (lo, hi)
+  __shared__ int sp, pending, lock, bad;
+  if (blockIdx.x >= nseg) return;
+  const Seg sg = segs[blockIdx.x];
+  const int n = sg.hi - sg.lo + 1;
+  const float* sk = bufs.kb[sg.buf] + sg.lo;
+  const unsigned* si = bufs.ib[sg.buf] + sg.lo;
+  for (int t = threadIdx.x; t < n; t += blockDim.x) { ka[t] = sk[t]; ia[t] = si[t]; }
+  if (threadIdx.x == 0) {
+    sp = 0; lock = 0; bad = 0;
+    pending = n >= 2 ? 1 : 0;
+    if (n >= 2) { stk[0] = 0; stk[1] = n - 1; sp = 1; }
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  long long spins = 0;
+  while (true) {
+    int lo = -1, hi = -1;
+    if (lane == 0) {
+      while (atomicCAS(&lock, 0, 1) != 0) {
+        if (++spins > (1ll << 24)) { bad = 1; break; }
+      }
+      if (!bad) {
+        if (sp > 0) { sp--; lo = stk[2 * sp]; hi = stk[2 * sp + 1]; }
+        __threadfence_block();
+        atomicExch(&lock, 0);
+      }
+    }
+    lo = __shfl_sync(0xffffffffu, lo, 0);
+    hi = __shfl_sync(0xffffffffu, hi, 0);
+    if (lo < 0) {
+      const int pend = *(volatile int*)&pending;
+      const int bd = *(volatile int*)&bad;
+      if (pend == 0 || bd) break;
+      if (++spins > (1ll << 24)) { if (lane == 0) bad = 1; break; }
+      __nanosleep(64);
+      continue;
+    }
+    // partition [lo, hi] (block-local positions)
+    const float pv = ka[hi];
+    const int s = hi - lo + 1;
+    int run = 0;
+    for (int b0 = lo; b0 < hi; b0 += 32) {
+      const int p = b0 + lane;
+      const bool L = p < hi && ka[p] <= pv;
+      const unsigned msk = __ballot_sync(0xffffffffu, L);
+      const int r = run + __popc(msk & ((1u << lane) - 1u));
+      if (p < hi) {
+        if (L) { kb[lo + r] = ka[p]; ib[lo + r] = ia[p]; }
+        else lam[lo + (p - lo - r)] = r;
+      }
+      run += __popc(msk);
+    }
+    const int nL = run, m = s - 1 - nL;
+    __syncwarp();
+    for (int b0 = lo; b0 < hi; b0 += 32) {
+      const int p = b0 + lane;
+      if (p < hi && !(ka[p] <= pv)) {
+        const int* ls = lam + lo;
+        const int a = lomuto_g_dest(p - lo, nL, m, [ls](int i) { return ls[i]; });
+        const int dest = (a == nL) ? (s - 1) : a;
+        kb[lo + dest] = ka[p];
+        ib[lo + dest] = ia[p];
+      }
+    }
+    if (lane == 0) { kb[lo + nL] = ka[hi]; ib[lo + nL] = ia[hi]; }
+    __syncwarp();
+    for (int p = lo + lane; p <= hi; p += 32) { ka[p] = kb[p]; ia[p] = ib[p]; }
+    __syncwarp();
+    if (lane == 0) {
+      int nc = 0;
+      int cl[2][2];
+      if (nL >= 2) { cl[nc][0] = lo; cl[nc][1] = lo + nL - 1; nc++; }
+      if (m >= 2) { cl[nc][0] = lo + nL + 1; cl[nc][1] = hi; nc++; }
+      while (atomicCAS(&lock, 0, 1) != 0) {
+        if (++spins > (1ll << 24)) { bad = 1; break; }
+      }
+      if (!bad) {
+        for (int q = 0; q < nc; q++) { stk[2 * sp] = cl[q][0]; stk[2 * sp + 1] = cl[q][1]; sp++; }
+        atomicAdd(&pending, nc - 1);
+        __threadfence_block();
+        atomicExch(&lock, 0);
+      }
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  if (bad) {
+    if (threadIdx.x == 0) atomicExch(err, 1);
+    return;
+  }
+  for (int t = threadIdx.x; t < n; t += blockDim.x) { fkey[sg.lo + t] = ka[t]; fid[sg.lo + t] = ia[t]; }
+}
+
+int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
+  const int np = (int)h->np;
+  const size_t cap = std::max<size_t>(np, 1);
+  float* k0 = h->key;
+  unsigned* i0 = h->id;
+  float* k1 = reinterpret_cast<float*>(i0 + cap);
+  unsigned* i1 = reinterpret_cast<unsigned*>(k1 + cap);
+  float* fk = reinterpret_cast<float*>(i1 + cap);
+  // final arrays live in B_PEAKS2
+  EXH_TRY(c.buf[B_PEAKS2].ensure((sizeof(float) + sizeof(unsigned)) * cap + sizeof(int) * cap));
+  fk = c.buf[B_PEAKS2].as<float>();
+  unsigned* fi = reinterpret_cast<unsigned*>(fk + cap);
+  int* lam = reinterpret_cast<int*>(fi + cap);
+  if (np <= 1) {
+    if (np == 1) {
+      EXH_CUDA_TRY(cudaMemcpyAsync(fk, k0, sizeof(float), cudaMemcpyDeviceToDevice, st));
+      EXH_CUDA_TRY(cudaMemcpyAsync(fi, i0, sizeof(unsigned), cudaMemcpyDeviceToDevice, st));
+    }
+    h->key = fk;
+    h->id = fi;
+    return EXH_OK;
+  }
+  float* kb[2] = {k0, k1};
+  unsigned* ib[2] = {i0, i1};
+  std::vector<Seg> large, small;
+  std::vector<int> single_pos, single_buf;
+  if (np > SORT_SMALL) large.push_back({0, np - 1, 0, 0});
+  else small.push_back({0, np - 1, 0, 0});
+  // scratch: segments, chunk tables, counts
+  const int max_chunks = np / CH + 2 * (np / SORT_SMALL + 2) + 8;
+  const int max_segs = np / SORT_SMALL + 8;
+  const size_t scratch = sizeof(Seg) * (size_t)max_segs + sizeof(int) * ((size_t)max_chunks * 3 + 2 * (size_t)max_segs + 8);
+  EXH_TRY(c.buf[B_SCRATCH].ensure(std::max<size_t>(scratch, sizeof(Seg) * (size_t)(np / 2 + 8))));
+  Seg* d_segs = c.buf[B_SCRATCH].as<Seg>();
+  int* d_cseg = reinterpret_cast<int*>(d_segs + max_segs);
+  int* d_coff = d_cseg + max_chunks;
+  int* d_cL = d_coff + max_chunks;
+  int* d_cfirst = d_cL + max_chunks;
+  int* d_nl = d_cfirst + max_segs + 1;
+  std::vector<int> hcseg, hcoff, hcfirst, hnl;
+  while (!large.empty()) {
+    const int buf = large[0].buf;   // every large segment of a level sits in the same buffer
+    hcseg.clear(); hcoff.clear(); hcfirst.clear();
+    for (size_t sidx = 0; sidx < large.size(); sidx++) {
+      hcfirst.push_back((int)hcseg.size());
+      const int len = large[sidx].hi - large[sidx].lo;   // elements before the pivot
+      for (int o = 0; o < len; o += CH) { hcseg.push_back((int)sidx); hcoff.push_back(o); }
+    }
+    hcfirst.push_back((int)hcseg.size());
+    const int nseg = (int)large.size(), nch = (int)hcseg.size();
+    EXH_CUDA_TRY(cudaMemcpyAsync(d_segs, large.data(), sizeof(Seg) * nseg, cudaMemcpyHostToDevice, st));
+    EXH_CUDA_TRY(cudaMemcpyAsync(d_cseg, hcseg.data(), sizeof(int) * nch, cudaMemcpyHostToDevice, st));
+    EXH_CUDA_TRY(cudaMemcpyAsync(d_coff, hcoff.data(), sizeof(int) * nch, cudaMemcpyHostToDevice, st));
+    EXH_CUDA_TRY(cudaMemcpyAsync(d_cfirst, hcfirst.data(), sizeof(int) * (nseg + 1), cudaMemcpyHostToDevice, st));
+    k_qs_count<<<nch, CH_T, 0, st>>>(kb[buf], d_segs, d_cseg, d_coff, nch, d_cL);
+    k_qs_seg_scan<<<nseg, 256, 0, st>>>(d_cfirst, nseg, d_cL, d_nl);
+    k_qs_place<1><<<nch, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, nch, d_cL, d_nl, lam,
+                                        kb[buf ^ 1], ib[buf ^ 1], fk, fi);
+    k_qs_place<2><<<nch, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, nch, d_cL, d_nl, lam,
+                                        kb[buf ^ 1], ib[buf ^ 1], fk, fi);
+    count_launch(4);
+    EXH_CUDA_TRY(cudaGetLastError());
+    hnl.resize(nseg);
+    EXH_CUDA_TRY(cudaMemcpyAsync(hnl.data(), d_nl, sizeof(int) * nseg, cudaMemcpyDeviceToHost, st));
+    EXH_CUDA_TRY(cudaStreamSynchronize(st));
+    std::vector<Seg> next;
+    for (int sidx = 0; sidx < nseg; sidx++) {
+      const Seg s = large[sidx];
+      const int nL = hnl[sidx];
+      const Seg ch[2] = {{s.lo, s.lo + nL - 1, buf ^ 1, 0}, {s.lo + nL + 1, s.hi, buf ^ 1, 0}};
+      for (const Seg& cs : ch) {
+        const int len = cs.hi - cs.lo + 1;
+        if (len == 1) { single_pos.push_back(cs.lo); single_buf.push_back(buf ^ 1); }
+        else if (len > SORT_SMALL) next.push_back(cs);
+        else if (len >= 2) small.push_back(cs);
+      }
+    }
+    // a level holds segments from one buffer only: children all live in buf^1
+    large.swap(next);
+  }
+  if (!single_pos.empty()) {
+    const int ns = (int)single_pos.size();
+    DevBuf& tmp = c.buf[B_HOSTIO2];
+    EXH_TRY(tmp.ensure(sizeof(int) * 2 * ns + sizeof(void*) * 4 + 64));
+    int* dpos = tmp.as<int>();
+    int* dbuf = dpos + ns;
+    void** dptr = reinterpret_cast<void**>(reinterpret_cast<char*>(tmp.p) + ((sizeof(int) * 2 * ns + 15) & ~size_t(15)));
+    void* hp[4] = {kb[0], kb[1], ib[0], ib[1]};
+    EXH_CUDA_TRY(cudaMemcpyAsync(dpos, single_pos.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
+    EXH_CUDA_TRY(cudaMemcpyAsync(dbuf, single_buf.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
+    EXH_CUDA_TRY(cudaMemcpyAsync(dptr, hp, sizeof(hp), cudaMemcpyHostToDevice, st));
+    k_qs_copy_single<<<exh_div_up(ns, 256), 256, 0, st>>>(dpos, dbuf, ns, reinterpret_cast<float* const*>(dptr),
+                                                          reinterpret_cast<unsigned* const*>(dptr + 2), fk, fi);
+    count_launch(1);
+    EXH_CUDA_TRY(cudaGetLastError());
+    EXH_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  if (!small.empty()) {
+    const int ns = (int)small.size();
+    EXH_CUDA_TRY(cudaMemcpyAsync(d_segs, small.data(), sizeof(Seg) * ns, cudaMemcpyHostToDevice, st));
+    EXH_TRY(c.buf[B_HOSTIO2].ensure(64));
+    int* d_err = c.buf[B_HOSTIO2].as<int>();
+    EXH_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+    const size_t sm = (size_t)SORT_SMALL * (4 * 4 + 4) + sizeof(int) * 2 * (SORT_SMALL + 2);
+    EXH_CUDA_TRY(set_smem(k_qs_small, sm));
+    SmallSortBuffers sb{{kb[0], kb[1]}, {ib[0], ib[1]}};
+    k_qs_small<<<ns, SORT_T, sm, st>>>(d_segs, ns, sb, fk, fi, d_err);
+    count_launch(1);
+    EXH_CUDA_TRY(cudaGetLastError());
+    int herr = 0;
+    EXH_CUDA_TRY(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    EXH_CUDA_TRY(cudaStreamSynchronize(st));
+    if (herr) {
+      exh_set_error_msg("peak sort: work-stack wait exceeded its bound", __FILE__, __LINE__);
+      return EXH_E_TIMEOUT;
+    }
+  }
+  h->key = fk;
+  h->id = fi;
+  return EXH_OK;
+}
+
+// ------------------------------------------------------------------ growth
+struct GrowArgs {
+  const float* delta;
+  const float* key;        // sorted peaks (ascending)
+  const unsigned* id;
+  int64_t np;
+  int nproc;
+  HaloScalars hs;
+  const float* Btab;
+  ShellTable t;
+};
+
+__device__ __forceinline__ size_t cell_at(int x0, int y0, int z0, int off, const HaloScalars& hs) {
+  int i, j, k;
+  unpack_off(off, i, j, k);
+  return ((size_t)exh_wrap(x0, i, hs.n0) * hs.n1 + exh_wrap(y0, j, hs.n1)) * hs.n2 + exh_wrap(z0, k, hs.n2);
+}
+__device__ __forceinline__ void peak_coords(unsigned cell, const HaloScalars& hs, int& x, int& y, int& z) {
+  z = (int)(cell % hs.n2);
+  const unsigned r = cell / hs.n2;
+  y = (int)(r % hs.n1);
+  x = (int)(r / hs.n1);
+}
+
+// growth + shrink of find_halos.c:274-337.  flag == nullptr: exclusion-free.
+// Returns 0 ok, 1 count beyond the sigma table, 2 shell beyond the tables.
+__device__ int grow_one(const GrowArgs& A, const int* __restrict__ flag, int x0, int y0, int z0, float pden,
+                        int& count_out, int& gtmp_out) {
+  const HaloScalars& hs = A.hs;
+  double den = (double)pden, den_tmp = (double)pden;
+  int count = 0, count_tmp = 1, grows_tmp = 0, grows = 0;
+  const double bmin = (double)hs.Bmin, mneg = -(double)hs.Mtot;
+  while (den_tmp >= bmin) {
+    if (count < count_tmp) grows = grows_tmp;
+    grows_tmp++;
+    den = den_tmp;
+    count = count_tmp;
+    if (count >= hs.Ncells) { count_out = count; gtmp_out = grows_tmp; return 1; }
+    if (grows_tmp > A.t.gmax) { count_out = count; gtmp_out = grows_tmp; return 2; }
+    den_tmp = __dmul_rn(den, (double)count);
+    const int s0 = A.t.start_cap[grows_tmp], s1 = A.t.start_cap[grows_tmp + 1];
+    for (int q = s0; q < s1; q++) {
+      const size_t cell = cell_at(x0, y0, z0, A.t.off_cap[q], hs);
+      const double v = (flag && flag[cell] != FLAG_FREE) ? mneg : (double)A.delta[cell];
+      den_tmp = __dadd_rn(den_tmp, v);
+      count_tmp++;
+    }
+    den_tmp = __ddiv_rn(den_tmp, (double)count_tmp);
+  }
+  while (count > 0 && den < (double)A.Btab[count]) {
+    den_tmp = den;
+    count_tmp = count;
+    den = __dmul_rn(den, (double)count);
+    const int s0 = A.t.start_cap[grows], s1 = A.t.start_cap[grows + 1];
+    for (int q = s0; q < s1; q++) {
+      den = __dsub_rn(den, (double)A.delta[cell_at(x0, y0, z0, A.t.off_cap[q], hs)]);
+      count--;
+    }
+    if (count > 0) den = __ddiv_rn(den, (double)count);
+    if (count < count_tmp) grows_tmp = grows;
+    grows--;
+  }
+  count_out = count;
+  gtmp_out = grows_tmp;
+  return 0;
+}
+
+__global__ void k_gfree(GrowArgs A, int* __restrict__ gfree) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= A.nproc) return;
+  const int64_t l = A.np - 1 - r;
+  int x, y, z;
+  peak_coords(A.id[l], A.hs, x, y, z);
+  int cnt, gt;
+  const int st = grow_one(A, nullptr, x, y, z, A.key[l], cnt, gt);
+  // growth with exclusion reads at most the shells this one reads
+  gfree[r] = st ? A.t.gmax : min(gt, A.t.gmax);
+}
+
+__device__ __forceinline__ unsigned resv_key(int tag, int r) { return ((unsigned)tag << 24) | (0xFFFFFFu - (unsigned)r); }
+
+__global__ void k_reserve(GrowArgs A, const int* __restrict__ gfree, unsigned char* __restrict__ state,
+                          const int* __restrict__ flag, unsigned* __restrict__ resv, int tag, int* __restrict__ cnt,
+                          int* __restrict__ npend) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= A.nproc || state[r]) return;
+  const int64_t l = A.np - 1 - r;
+  const unsigned cell0 = A.id[l];
+  if (flag[cell0] != FLAG_FREE) {        // find_halos.c:233: the peak is already inside a halo
+    state[r] = 1;
+    cnt[r] = 0;
+    return;
+  }
+  atomicAdd(npend, 1);
+  int x, y, z;
+  peak_coords(cell0, A.hs, x, y, z);
+  const unsigned key = resv_key(tag, r);
+  const int e = A.t.start_all[gfree[r] + 1];
+  for (int q = 0; q < e; q++) atomicMax(&resv[cell_at(x, y, z, A.t.off_all[q], A.hs)], key);
+}
+
+__global__ void k_commit(GrowArgs A, const int* __restrict__ gfree, unsigned char* __restrict__ state,
+                         int* __restrict__ flag, const unsigned* __restrict__ resv, int tag, int* __restrict__ cnt,
+                         int* __restrict__ gfin, int* __restrict__ err) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= A.nproc || state[r]) return;
+  const int64_t l = A.np - 1 - r;
+  const unsigned cell0 = A.id[l];
+  int x, y, z;
+  peak_coords(cell0, A.hs, x, y, z);
+  const unsigned key = resv_key(tag, r);
+  const int e = A.t.start_all[gfree[r] + 1];
+  for (int q = 0; q < e; q++)
+    if (resv[cell_at(x, y, z, A.t.off_all[q], A.hs)] != key) return;
+  int count, gt;
+  const int st = grow_one(A, flag, x, y, z, A.key[l], count, gt);
+  if (st) { atomicMax(err, st); state[r] = 1; cnt[r] = 0; return; }
+  state[r] = 1;
+  cnt[r] = count;
+  gfin[r] = gt;
+  if (count == 0) return;                 // find_halos.c:339-340
+  const int we = A.t.start_all[gt];       // cells with r^2 < grows_tmp
+  for (int q = 0; q < we; q++) flag[cell_at(x, y, z, A.t.off_all[q], A.hs)] = r;
+  flag[cell0] = -(r + 2);
+}
+
+__global__ void k_kept(const int* __restrict__ cnt, const unsigned char* __restrict__ state, int nproc, int Nmin,
+                       int* __restrict__ kept) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nproc) return;
+  kept[r] = (cnt[r] > 0 && cnt[r] >= Nmin) ? 1 : 0;
+}
+
+__global__ void k_halo_index(const int* __restrict__ kept, const int* __restrict__ hid_ex, int nproc,
+                             int* __restrict__ hid, int* __restrict__ hpeak) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nproc) return;
+  if (kept[r]) {
+    hid[r] = hid_ex[r];
+    hpeak[hid_ex[r]] = r;
+  } else {
+    hid[r] = -1;
+  }
+}
+
+int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars& hs, const float* Btab_dev,
+               const ShellTable& t, HaloDev* h, cudaStream_t st) {
+  const int64_t np = h->np;
+  // the reference loop visits sorted indices np-1 .. 1 while den >= Bmin
+  int64_t nproc = 0;
+  if (np >= 2) {
+    // lower bound of Bmin in the ascending keys, on the host
+    std::vector<float> keys(np);
+    EXH_CUDA_TRY(cudaMemcpyAsync(keys.data(), h->key, sizeof(float) * np, cudaMemcpyDeviceToHost, st));
+    EXH_CUDA_TRY(cudaStreamSynchronize(st));
+    int64_t lo = 0, hi = np;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) / 2;
+      if (keys[mid] < hs.Bmin) lo = mid + 1;
+      else hi = mid;
+    }
+    const int64_t L0 = std::max<int64_t>(lo, 1);
+    nproc = np - L0;
+  }
+  h->nproc = nproc;
+  if (nproc >= (1 << 24) - 1) {
+    exh_set_error_msg("more than 2^24 peaks above the barrier", __FILE__, __LINE__);
+    return EXH_E_UNSUPPORTED;
+  }
+  const size_t ng = b.ng;
+  const size_t npr = std::max<int64_t>(nproc, 1);
+  EXH_TRY(c.buf[B_FLAG].ensure(sizeof(int) * ng * 2));
+  h->flag = c.buf[B_FLAG].as<int>();
+  h->resv = reinterpret_cast<unsigned*>(h->flag + ng);
+  EXH_TRY(c.buf[B_HALO].ensure(npr * (sizeof(int) * 7 + 1) + 64));
+  h->gfree = c.buf[B_HALO].as<int>();
+  h->gfin = h->gfree + npr;
+  h->cnt = h->gfin + npr;
+  h->hid = h->cnt + npr;
+  h->hpeak = h->hid + npr;
+  int* kept = h->hpeak + npr;
+  int* misc = kept + npr;             // npr ints: scan scratch / counters
+  h->state = reinterpret_cast<unsigned char*>(misc + npr);
+  EXH_CUDA_TRY(cudaMemsetAsync(h->flag, 0xff, sizeof(int) * ng, st));      // FLAG_FREE
+  EXH_CUDA_TRY(cudaMemsetAsync(h->resv, 0, sizeof(unsigned) * ng, st));
+  EXH_CUDA_TRY(cudaMemsetAsync(h->state, 0, npr, st));
+  EXH_CUDA_TRY(cudaMemsetAsync(h->cnt, 0, sizeof(int) * npr, st));
+  h->nh = 0;
+  if (nproc == 0) return EXH_OK;
+  GrowArgs A{delta, h->key, h->id, np, (int)nproc, hs, Btab_dev, t};
+  const unsigned nb = exh_div_up(nproc, 128);
+  k_gfree<<<nb, 128, 0, st>>>(A, h->gfree);
+  count_launch(1);
+  EXH_CUDA_TRY(cudaGetLastError());
+  // device counters: [0] pending this round, [1] error
+  EXH_TRY(c.buf[B_HOSTIO2].ensure(64));
+  int* dcnt = c.buf[B_HOSTIO2].as<int>();
+  int round = 0;
+  while (true) {
+    const int tag = (round % 255) + 1;
+    if (round > 0 && tag == 1) EXH_CUDA_TRY(cudaMemsetAsync(h->resv, 0, sizeof(unsigned) * ng, st));
+    EXH_CUDA_TRY(cudaMemsetAsync(dcnt, 0, sizeof(int) * 2, st));
+    k_reserve<<<nb, 128, 0, st>>>(A, h->gfree, h->state, h->flag, h->resv, tag, h->cnt, dcnt);
+    k_commit<<<nb, 128, 0, st>>>(A, h->gfree, h->state, h->flag, h->resv, tag, h->cnt, h->gfin, dcnt + 1);
+    count_launch(2);
+    EXH_CUDA_TRY(cudaGetLastError());
+    int hc[2];
+    EXH_CUDA_TRY(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
+    EXH_CUDA_TRY(cudaStreamSynchronize(st));
+    if (hc[1]) {
+      exh_set_error_msg(hc[1] == 1 ? "a halo grew past the sigma(M) table (find_halos.c:316 would read past Sig_Grid)"
+                                   : "a halo grew past every shell of the box",
+                        __FILE__, __LINE__);
+      return EXH_E_RANGE;
+    }
+    if (hc[0] == 0) break;
+    round++;
+    if (round > nproc + 2) {
+      exh_set_error_msg("halo growth made no progress", __FILE__, __LINE__);
+      return EXH_E_TIMEOUT;
+    }
+  }
+  k_kept<<<nb, 128, 0, st>>>(h->cnt, h->state, (int)nproc, hs.Nmin, kept);
+  count_launch(1);
+  int* total = dcnt + 2;
+  // gfree is dead after the rounds: it serves as the scan's block sums
+  EXH_CUDA_TRY(exclusive_scan<int>(kept, misc, nproc, h->gfree, total, st));
+  int nh = 0;
+  EXH_CUDA_TRY(cudaMemcpyAsync(&nh, total, sizeof(int), cudaMemcpyDeviceToHost, st));
+  EXH_CUDA_TRY(cudaStreamSynchronize(st));
+  k_halo_index<<<nb, 128, 0, st>>>(kept, misc, (int)nproc, h->hid, h->hpeak);
+  count_launch(1);
+  EXH_CUDA_TRY(cudaGetLastError());
+  h->nh = nh;
+  return EXH_OK;
+}
+
+// ------------------------------------------------------------------ flags
+__global__ void k_flags_ref(const int* __restrict__ flag, const int* __restrict__ hid, size_t ng,
+                            long long* __restrict__ out) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (; i < ng; i += stride) {
+    const int v = flag[i];
+    long long o;
+    if (v == FLAG_FREE) o = (long long)ng;
+    else if (v >= 0) o = hid[v] >= 0 ? (long long)hid[v] : (long long)ng + 1;
+    else o = hid[-v - 2] >= 0 ? -(long long)hid[-v - 2] : (long long)ng + 1;
+    out[i] = o;
+  }
+}
+
+int flags_to_reference(const HaloDev& h, size_t ng, int64_t* out_dev, cudaStream_t st) {
+  k_flags_ref<<<EXH_NUM_SMS * 8, 256, 0, st>>>(h.flag, h.hid, ng, reinterpret_cast<long long*>(out_dev));
+  count_launch(1);
+  EXH_CUDA_TRY(cudaGetLastError());
+  return EXH_OK;
+}
+
+// ------------------------------------------------------------------ masses
+// taus jump matrices: for component c and power 2^e, 32 column words
+struct TausJump {
+  unsigned col[3][32][32];   // [component][bit e][column]
+  unsigned s0[3];            // state after seeding
+};
+
+static unsigned taus_step1(unsigned s, int c) {
+  if (c == 0) return ((s & 0xFFFFFFFEu) << 12) ^ (((s << 13) ^ s) >> 19);
+  if (c == 1) return ((s & 0xFFFFFFF8u) << 4) ^ (((s << 2) ^ s) >> 25);
+  return ((s & 0xFFFFFFF0u) << 17) ^ (((s << 3) ^ s) >> 11);
+}
+
+static void taus_jump_tables(unsigned long seed, TausJump* J) {
+  // the seeding documented for gsl_rng_taus: LCG(69069) chain, minimum
+  // values 2, 8, 16, six warm-up steps
+  unsigned s = (unsigned)(seed & 0xFFFFFFFFul);
+  if (s == 0) s = 1;
+  unsigned s1 = 69069u * s;
+  if (s1 < 2u) s1 += 2u;
+  unsigned s2 = 69069u * s1;
+  if (s2 < 8u) s2 += 8u;
+  unsigned s3 = 69069u * s2;
+  if (s3 < 16u) s3 += 16u;
+  for (int w = 0; w < 6; w++) { s1 = taus_step1(s1, 0); s2 = taus_step1(s2, 1); s3 = taus_step1(s3, 2); }
+  J->s0[0] = s1; J->s0[1] = s2; J->s0[2] = s3;
+  for (int c = 0; c < 3; c++) {
+    unsigned cur[32];
+    for (int b = 0; b < 32; b++) cur[b] = taus_step1(1u << b, c);     // one step
+    for (int e = 0; e < 32; e++) {
+      std::memcpy(J->col[c][e], cur, sizeof(cur));
+      unsigned nx[32];
+      for (int b = 0; b < 32; b++) {                                   // square
+        unsigned v = cur[b], acc = 0;
+        for (int q = 0; q < 32; q++)
+          if ((v >> q) & 1u) acc ^= cur[q];
+        nx[b] = acc;
+      }
+      std::memcpy(cur, nx, sizeof(nx));
+    }
+  }
+}
+
+__device__ __forceinline__ unsigned gf2_apply(const unsigned* __restrict__ col, unsigned s) {
+  unsigned acc = 0;
+#pragma unroll 8
+  for (int q = 0; q < 32; q++)
+    if ((s >> q) & 1u) acc ^= col[q];
+  return acc;
+}
+
+struct DevSpline {
+  const double* x;
+  const double* y;
+  const double* c;
+  int n;
+  // natural cubic spline, the same operations and order as the host set-up
+  __device__ double eval(double q, int* bad) const {
+    if (!(q >= x[0] && q <= x[n - 1])) { *bad = 1; return 0.0; }
+    int lo = 0, hi = n - 1;
+    while (hi > lo + 1) {
+      const int mid = (hi + lo) >> 1;
+      if (x[mid] > q) hi = mid; else lo = mid;
+    }
+    const double xl = x[lo], dx = __dsub_rn(x[lo + 1], xl), dy = __dsub_rn(y[lo + 1], y[lo]);
+    const double c0 = c[lo], c1 = c[lo + 1];
+    const double bb = __dsub_rn(__ddiv_rn(dy, dx), __ddiv_rn(__dmul_rn(dx, __dadd_rn(c1, __dmul_rn(2.0, c0))), 3.0));
+    const double dd = __ddiv_rn(__dsub_rn(c1, c0), __dmul_rn(3.0, dx));
+    const double t = __dsub_rn(q, xl);
+    return __dadd_rn(y[lo], __dmul_rn(t, __dadd_rn(bb, __dmul_rn(t, __dadd_rn(c0, __dmul_rn(t, dd))))));
+  }
+};
+
+constexpr int MASS_CHUNK = 32;
+
+__global__ void k_masses(const TausJump* __restrict__ J, DevSpline sI, DevSpline sInv, const int* __restrict__ hpeak,
+                         const int* __restrict__ cnt, const unsigned* __restrict__ pid, int64_t np,
+                         const int* __restrict__ spheres, int nsph, int Ncells, float Mcell, int64_t nh,
+                         HaloScalars hs, float* __restrict__ Mh, int* __restrict__ count_out, int* __restrict__ xc,
+                         int* __restrict__ err) {
+  const int64_t h0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * MASS_CHUNK;
+  if (h0 >= nh) return;
+  // state after h0 draws
+  unsigned s[3] = {J->s0[0], J->s0[1], J->s0[2]};
+  for (int e = 0; e < 32; e++)
+    if ((h0 >> e) & 1)
+      for (int c = 0; c < 3; c++) s[c] = gf2_apply(J->col[c][e], s[c]);
+  const int64_t h1 = min(nh, h0 + MASS_CHUNK);
+  int bad = 0;
+  for (int64_t h = h0; h < h1; h++) {
+    s[0] = ((s[0] & 0xFFFFFFFEu) << 12) ^ (((s[0] << 13) ^ s[0]) >> 19);
+    s[1] = ((s[1] & 0xFFFFFFF8u) << 4) ^ (((s[1] << 2) ^ s[1]) >> 25);
+    s[2] = ((s[2] & 0xFFFFFFF0u) << 17) ^ (((s[2] << 3) ^ s[2]) >> 11);
+    const double u = (double)(s[0] ^ s[1] ^ s[2]) / 4294967296.0;
+    const int r = hpeak[h];
+    const int count = cnt[r];
+    // Next_Count (find_halos.c:442-452): first table entry equal to count
+    int lo = 0, hi = min(nsph, Ncells);
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (spheres[mid] < count) lo = mid + 1; else hi = mid;
+    }
+    const int nx = lo + 1;
+    float m;
+    if (lo >= min(nsph, Ncells) || spheres[lo] != count || nx >= nsph) {
+      bad = 1;
+      m = __int_as_float(0x7fc00000);
+    } else {
+      const float m0 = __fmul_rn((float)count, Mcell), m1 = __fmul_rn((float)spheres[nx], Mcell);
+      const double i0 = sI.eval((double)m0, &bad), i1 = sI.eval((double)m1, &bad);
+      const float dt = (float)__dadd_rn(i0, __dmul_rn(__dsub_rn(i1, i0), u));
+      m = (float)sInv.eval((double)dt, &bad);
+    }
+    Mh[h] = m;
+    count_out[h] = count;
+    int x, y, z;
+    peak_coords(pid[np - 1 - r], hs, x, y, z);
+    xc[3 * h] = x; xc[3 * h + 1] = y; xc[3 * h + 2] = z;
+  }
+  if (bad) atomicExch(err, 1);
+}
+
+int halo_masses(Ctx& c, const BoxParams& b, const HaloDev& h, const HostTables& tab, float* Mh_dev, int* count_dev,
+                int* xc_dev, cudaStream_t st) {
+  if (h.nh == 0) return EXH_OK;
+  TausJump J;
+  taus_jump_tables((unsigned long)b.seed, &J);
+  const std::vector<int>& sph = cells_in_spheres();
+  const int Nr = tab.Nr;
+  // spline coefficients for I(M) and its inverse
+  Spline sI, sInv;
+  if (sI.init(tab.M.data(), tab.Int.data(), Nr) != EXH_OK || sInv.init(tab.Int.data(), tab.M.data(), Nr) != EXH_OK) {
+    exh_set_error_msg("mass-function integral is not increasing", __FILE__, __LINE__);
+    return EXH_E_RANGE;
+  }
+  const size_t bytes = sizeof(TausJump) + sizeof(double) * 6 * Nr + sizeof(int) * sph.size() + 64;
+  EXH_TRY(c.buf[B_WORK2].ensure(bytes));
+  char* base = c.buf[B_WORK2].as<char>();
+  TausJump* dJ = reinterpret_cast<TausJump*>(base);
+  double* dd = reinterpret_cast<double*>(base + ((sizeof(TausJump) + 15) & ~size_t(15)));
+  int* dsph = reinterpret_cast<int*>(dd + 6 * Nr);
+  std::vector<double> hd(6 * Nr);
+  std::memcpy(&hd[0], sI.x.data(), sizeof(double) * Nr);
+  std::memcpy(&hd[Nr], sI.y.data(), sizeof(double) * Nr);
+  std::memcpy(&hd[2 * Nr], sI.c.data(), sizeof(double) * Nr);
+  std::memcpy(&hd[3 * Nr], sInv.x.data(), sizeof(double) * Nr);
+  std::memcpy(&hd[4 * Nr], sInv.y.data(), sizeof(double) * Nr);
+  std::memcpy(&hd[5 * Nr], sInv.c.data(), sizeof(double) * Nr);
+  EXH_CUDA_TRY(cudaMemcpyAsync(dJ, &J, sizeof(J), cudaMemcpyHostToDevice, st));
+  EXH_CUDA_TRY(cudaMemcpyAsync(dd, hd.data(), sizeof(double) * hd.size(), cudaMemcpyHostToDevice, st));
+  EXH_CUDA_TRY(cudaMemcpyAsync(dsph, sph.data(), sizeof(int) * sph.size(), cudaMemcpyHostToDevice, st));
+  DevSpline dI{dd, dd + Nr, dd + 2 * Nr, Nr}, dInv{dd + 3 * Nr, dd + 4 * Nr, dd + 5 * Nr, Nr};
+  EXH_TRY(c.buf[B_HOSTIO2].ensure(64));
+  int* derr = c.buf[B_HOSTIO2].as<int>();
+  EXH_CUDA_TRY(cudaMemsetAsync(derr, 0, sizeof(int), st));
+  HaloScalars hs{};
+  hs.n0 = b.nd[0]; hs.n1 = b.nd[1]; hs.n2 = b.nd[2];
+  const int64_t nchunk = (h.nh + MASS_CHUNK - 1) / MASS_CHUNK;
+  k_masses<<<exh_div_up(nchunk, 128), 128, 0, st>>>(dJ, dI, dInv, h.hpeak, h.cnt, h.id, h.np, dsph, (int)sph.size(),
+                                                   tab.Ncells, b.Mcell, h.nh, hs, Mh_dev, count_dev, xc_dev, derr);
+  count_launch(1);
+  EXH_CUDA_TRY(cudaGetLastError());
+  int herr = 0;
+  EXH_CUDA_TRY(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, st));
+  EXH_CUDA_TRY(cudaStreamSynchronize(st));   // host tables above must outlive the copies
+  if (herr) {
+    exh_set_error_msg("halo mass outside the mass-function tables", __FILE__, __LINE__);
+    return EXH_E_RANGE;
+  }
+  return EXH_OK;
+}
+
+}  // namespace exh

@@ -1,9 +1,13 @@
 // Halo-box pipeline entry points: Generate_Halos_Box_from_Pk
-// (src/exshalos/box.c:4-68) and its sub-stage hooks.
+// (src/exshalos/box.c:4-68, binding exshalos.c:710-940), Find_Halos on a
+// given grid (exshalos.c:509-610), the Gaussian field alone
+// (exshalos.c:46-121) and the result fetch.
 #include <cstring>
 #include <vector>
 
 #include "ctx.cuh"
+#include "halos.cuh"
+#include "lpt.cuh"
 #include "pipeline.cuh"
 
 using namespace exh;
@@ -29,8 +33,56 @@ static int check_common(const exh_halo_params* p, const float* k, const float* P
   REQUIRE(p->Lc > 0.f && p->Lc < 100.f, EXH_E_INVALID, "cell size Lc must be in (0, 100) Mpc/h");
   REQUIRE(p->R_max >= 100000.f, EXH_E_UNSUPPORTED, "R_max < 1e5 (FFTLog truncation) is not built");
   REQUIRE(p->field_stream == EXH_FIELD_PHILOX, EXH_E_UNSUPPORTED, "unknown field stream");
+  REQUIRE(p->OUT_PROF == 0, EXH_E_UNSUPPORTED, "Lagrangian profiles (OUT_PROF) are not built");
+  for (int i = 0; i < Nk; i++) REQUIRE(k[i] > 0.f && P[i] >= 0.f, EXH_E_INVALID, "k must be > 0 and P >= 0");
   return EXH_OK;
 }
+
+namespace {
+
+// Find_Halos (find_halos.c:479-563) on the device field `delta`
+int run_halo_finder(Ctx& c, const BoxParams& b, const float* k, const float* P, int Nk, int setup_fp64,
+                    const float* delta, HaloDev* h, ShellTable* t, cudaStream_t st) {
+  HostTables& tab = c.halos.tab;
+  EXH_TRY(halo_tables(b, k, P, Nk, setup_fp64, tab.Sig_grid, tab.Btab, tab.M, tab.Int));
+  tab.Ncells = (int)tab.Sig_grid.size();
+  tab.Nr = Nk;
+  EXH_TRY(build_shell_tables(c, b, tab.Ncells, t, st));
+  EXH_TRY(c.buf[B_HOSTIO].ensure(sizeof(float) * tab.Ncells));
+  float* Btab_dev = c.buf[B_HOSTIO].as<float>();
+  EXH_CUDA_TRY(cudaMemcpyAsync(Btab_dev, tab.Btab.data(), sizeof(float) * tab.Ncells, cudaMemcpyHostToDevice, st));
+  EXH_TRY(find_peaks(c, delta, b, h, st));
+  EXH_TRY(sort_peaks(c, h, st));
+  HaloScalars hs;
+  hs.Bmin = tab.Btab[tab.Ncells - 1];
+  hs.Mtot = b.Mtot;
+  hs.Ncells = tab.Ncells;
+  hs.Nmin = b.Nmin;
+  hs.nmin_half = b.nmin / 2;
+  hs.n0 = b.nd[0]; hs.n1 = b.nd[1]; hs.n2 = b.nd[2];
+  EXH_TRY(grow_halos(c, delta, b, hs, Btab_dev, *t, h, st));
+  const size_t nh = std::max<int64_t>(h->nh, 1);
+  EXH_TRY(c.buf[B_MH].ensure((sizeof(float) + 4 * sizeof(int)) * nh));
+  float* Mh = c.buf[B_MH].as<float>();
+  int* cnt = reinterpret_cast<int*>(Mh + nh);
+  int* xc = cnt + nh;
+  EXH_TRY(halo_masses(c, b, *h, tab, Mh, cnt, xc, st));
+  HaloState& s = c.halos;
+  s.nh = h->nh; s.np = h->np; s.nproc = h->nproc;
+  s.nd[0] = b.nd[0]; s.nd[1] = b.nd[1]; s.nd[2] = b.nd[2];
+  s.ng = b.ng;
+  s.Mh = Mh; s.count = cnt; s.xc = xc;
+  s.flag = h->flag; s.hid = h->hid;
+  return EXH_OK;
+}
+
+__global__ void k_lagrangian_posh(const int* __restrict__ xc, int64_t nh, float Lc, float* __restrict__ posh) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= 3 * nh) return;
+  posh[i] = (float)((double)Lc * ((double)xc[i] + 0.5));     // exshalos.c:591
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -62,6 +114,7 @@ int exh_density_grid_compute(exh_ctx* ctx, const float* k, const float* P, int N
   EXH_CUDA_TRY(cudaSetDevice(c.device));
   cudaStream_t st = (cudaStream_t)stream;
   BoxParams b;
+  // density_grid_compute sets a fixed cosmology (exshalos.c:71-73); only the box matters
   EXH_TRY(setup_box(&b, prm->ndx, prm->ndy, prm->ndz, prm->Lc, 0.31f, 0.f, 1.686f, 1, 1.f, 0.f, 0.f, prm->seed));
   float* d = delta;
   if (mem == EXH_MEM_HOST) {
@@ -78,24 +131,142 @@ int exh_density_grid_compute(exh_ctx* ctx, const float* k, const float* P, int N
 
 int exh_halos_box_from_pk(exh_ctx* ctx, const float* k, const float* P, int Nk, const exh_halo_params* prm,
                           int64_t* nh_out, void* stream) {
-  (void)ctx; (void)k; (void)P; (void)Nk; (void)prm; (void)nh_out; (void)stream;
-  exh_set_error_msg("halo pipeline not built yet", __FILE__, __LINE__);
-  return EXH_E_UNSUPPORTED;
+  REQUIRE(ctx && nh_out, EXH_E_INVALID, "null argument");
+  EXH_TRY(check_common(prm, k, P, Nk));
+  Ctx& c = ctx->c;
+  EXH_CUDA_TRY(cudaSetDevice(c.device));
+  cudaStream_t st = (cudaStream_t)stream;
+  halo_state_release(c);
+  BoxParams b;
+  EXH_TRY(setup_box(&b, prm->ndx, prm->ndy, prm->ndz, prm->Lc, prm->Om0, prm->redshift, prm->dc, prm->Nmin, prm->a,
+                    prm->beta, prm->alpha, prm->seed));
+  const size_t ng = b.ng;
+  // field (box.c:18, k_smooth fixed at 1e5 there)
+  float* A_dev = nullptr;
+  EXH_TRY(upload_amplitudes(c, b, k, P, Nk, &A_dev, st));
+  EXH_TRY(c.buf[B_DELTA].ensure(sizeof(float) * ng));
+  float* delta = c.buf[B_DELTA].as<float>();
+  {
+    FFTPlan3D* p;
+    EXH_TRY(c.get_plan(b.nd[0], b.nd[1], b.nd[2], &p));
+    EXH_TRY(c.buf[B_WORK].ensure(sizeof(float2) * (size_t)b.nd[0] * b.nd[1] * p->nc));
+    FieldGen gen{make_modes(b, A_dev, prm->fixed, prm->phase)};
+    EXH_CUDA_TRY(fft_c2r_3d(*p, gen, c.buf[B_WORK].as<float2>(), RealPairStore{delta, b.nd[2], b.Normx}, st));
+  }
+  // halos (box.c:21)
+  HaloDev h;
+  ShellTable t;
+  EXH_TRY(run_halo_finder(c, b, k, P, Nk, prm->setup_fp64, delta, &h, &t, st));
+  // LPT (box.c:38-58): the amplitude table is re-uploaded (the mass step reused the buffer)
+  EXH_TRY(upload_amplitudes(c, b, k, P, Nk, &A_dev, st));
+  FieldModes modes = make_modes(b, A_dev, prm->fixed, prm->phase);
+  EXH_TRY(c.buf[B_S].ensure(sizeof(float) * 3 * ng));
+  EXH_TRY(c.buf[B_PHI1].ensure(sizeof(float) * ng));
+  float* S = c.buf[B_S].as<float>();
+  float* phi1 = c.buf[B_PHI1].as<float>();
+  float* phi2 = nullptr;
+  if (prm->DO_2LPT) {
+    EXH_TRY(c.buf[B_PHI2].ensure(sizeof(float) * ng));
+    phi2 = c.buf[B_PHI2].as<float>();
+  }
+  EXH_TRY(lpt_run(c, b, modes, prm->k_smooth, prm->DO_2LPT != 0, S, phi1, phi2, st));
+  const size_t nh = std::max<int64_t>(h.nh, 1);
+  EXH_TRY(c.buf[B_POSH].ensure(sizeof(float) * 6 * nh));
+  float* posh = c.buf[B_POSH].as<float>();
+  float* velh = prm->OUT_VEL ? posh + 3 * nh : nullptr;
+  const HaloOut o = make_halo_out(b, posh, velh);
+  EXH_TRY(halo_displacements(c, b, h, t, S, phi2, o, st));
+  HaloState& s = c.halos;
+  s.posh = posh;
+  s.velh = velh;
+  s.delta = prm->OUT_DEN ? delta : nullptr;
+  if (prm->OUT_LPT) {
+    EXH_TRY(c.buf[B_V].ensure(sizeof(float) * 6 * ng));
+    float* pos = c.buf[B_V].as<float>();
+    float* vel = prm->OUT_VEL ? pos + 3 * ng : nullptr;
+    EXH_TRY(particles(b, S, phi2, o, pos, vel, st));
+    s.pos = pos;
+    s.vel = vel;
+  }
+  *nh_out = s.nh;
+  return EXH_OK;
 }
 
 int exh_find_halos(exh_ctx* ctx, const float* delta, int ndx, int ndy, int ndz, const float* k, const float* P,
                    int Nk, const exh_halo_params* prm, int mem, int64_t* nh_out, void* stream) {
-  (void)ctx; (void)delta; (void)ndx; (void)ndy; (void)ndz; (void)k; (void)P; (void)Nk; (void)prm; (void)mem;
-  (void)nh_out; (void)stream;
-  exh_set_error_msg("halo finder not built yet", __FILE__, __LINE__);
-  return EXH_E_UNSUPPORTED;
+  REQUIRE(ctx && delta && nh_out && prm, EXH_E_INVALID, "null argument");
+  exh_halo_params q = *prm;
+  q.ndx = ndx; q.ndy = ndy; q.ndz = ndz;
+  q.ndz += (ndz & 1);   // evenness only matters for the FFTs, not used here
+  EXH_TRY(check_common(&q, k, P, Nk));
+  Ctx& c = ctx->c;
+  EXH_CUDA_TRY(cudaSetDevice(c.device));
+  cudaStream_t st = (cudaStream_t)stream;
+  halo_state_release(c);
+  BoxParams b;
+  // find_halos binds the mass draws to seed 12345 (exshalos.c:552)
+  EXH_TRY(setup_box(&b, ndx, ndy, ndz, prm->Lc, prm->Om0, prm->redshift, prm->dc, prm->Nmin, prm->a, prm->beta,
+                    prm->alpha, 12345));
+  const float* d = delta;
+  if (mem == EXH_MEM_HOST) {
+    EXH_TRY(c.buf[B_DELTA].ensure(sizeof(float) * b.ng));
+    EXH_CUDA_TRY(cudaMemcpyAsync(c.buf[B_DELTA].p, delta, sizeof(float) * b.ng, cudaMemcpyHostToDevice, st));
+    d = c.buf[B_DELTA].as<float>();
+  }
+  HaloDev h;
+  ShellTable t;
+  EXH_TRY(run_halo_finder(c, b, k, P, Nk, prm->setup_fp64, d, &h, &t, st));
+  const size_t nh = std::max<int64_t>(h.nh, 1);
+  EXH_TRY(c.buf[B_POSH].ensure(sizeof(float) * 6 * nh));
+  float* posh = c.buf[B_POSH].as<float>();
+  if (h.nh > 0) {
+    k_lagrangian_posh<<<exh_div_up(3 * h.nh, 256), 256, 0, st>>>(c.halos.xc, h.nh, b.Lc, posh);
+    count_launch(1);
+    EXH_CUDA_TRY(cudaGetLastError());
+  }
+  c.halos.posh = posh;
+  *nh_out = h.nh;
+  return EXH_OK;
 }
 
 int exh_halos_fetch(exh_ctx* ctx, float* posh, float* velh, float* Mh, int32_t* xc, int32_t* count, float* grid,
                     float* pos, float* vel, int64_t* flag, int mem, void* stream) {
-  (void)ctx; (void)posh; (void)velh; (void)Mh; (void)xc; (void)count; (void)grid; (void)pos; (void)vel; (void)flag;
-  (void)mem; (void)stream;
-  return EXH_E_UNSUPPORTED;
+  REQUIRE(ctx, EXH_E_INVALID, "null context");
+  Ctx& c = ctx->c;
+  EXH_CUDA_TRY(cudaSetDevice(c.device));
+  cudaStream_t st = (cudaStream_t)stream;
+  const HaloState& s = c.halos;
+  const cudaMemcpyKind kind = mem == EXH_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  const size_t nh = (size_t)s.nh, ng = s.ng;
+  REQUIRE(!velh || s.velh || nh == 0, EXH_E_INVALID, "velocities were not requested (OUT_VEL)");
+  REQUIRE(!grid || s.delta, EXH_E_INVALID, "the field was not requested (OUT_DEN)");
+  REQUIRE(!pos || s.pos, EXH_E_INVALID, "particles were not requested (OUT_LPT)");
+  REQUIRE(!vel || s.vel, EXH_E_INVALID, "particle velocities were not requested (OUT_LPT and OUT_VEL)");
+  if (nh) {
+    if (posh) EXH_CUDA_TRY(cudaMemcpyAsync(posh, s.posh, sizeof(float) * 3 * nh, kind, st));
+    if (velh) EXH_CUDA_TRY(cudaMemcpyAsync(velh, s.velh, sizeof(float) * 3 * nh, kind, st));
+    if (Mh) EXH_CUDA_TRY(cudaMemcpyAsync(Mh, s.Mh, sizeof(float) * nh, kind, st));
+    if (xc) EXH_CUDA_TRY(cudaMemcpyAsync(xc, s.xc, sizeof(int) * 3 * nh, kind, st));
+    if (count) EXH_CUDA_TRY(cudaMemcpyAsync(count, s.count, sizeof(int) * nh, kind, st));
+  }
+  if (grid) EXH_CUDA_TRY(cudaMemcpyAsync(grid, s.delta, sizeof(float) * ng, kind, st));
+  if (pos) EXH_CUDA_TRY(cudaMemcpyAsync(pos, s.pos, sizeof(float) * 3 * ng, kind, st));
+  if (vel) EXH_CUDA_TRY(cudaMemcpyAsync(vel, s.vel, sizeof(float) * 3 * ng, kind, st));
+  if (flag) {
+    REQUIRE(s.flag, EXH_E_INVALID, "no halo flags available");
+    int64_t* fdev = flag;
+    if (mem == EXH_MEM_HOST) {
+      EXH_TRY(c.buf[B_HOSTIO].ensure(sizeof(int64_t) * ng));
+      fdev = c.buf[B_HOSTIO].as<int64_t>();
+    }
+    HaloDev hd;
+    hd.flag = s.flag;
+    hd.hid = s.hid;
+    EXH_TRY(flags_to_reference(hd, ng, fdev, st));
+    if (mem == EXH_MEM_HOST) EXH_CUDA_TRY(cudaMemcpyAsync(flag, fdev, sizeof(int64_t) * ng, kind, st));
+  }
+  EXH_CUDA_TRY(cudaStreamSynchronize(st));
+  return EXH_OK;
 }
 
 int exh_halo_tables(exh_ctx* ctx, int* Ncells, int* Nr, float* Sig_grid, float* Btab, double* M, double* Int) {

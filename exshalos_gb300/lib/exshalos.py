@@ -1,0 +1,144 @@
+"""Mirror of the reference extension pyexshalos.lib.exshalos
+(src/exshalos/exshalos.c) for the functions on the mock path.
+
+Arguments keep the reference's positional order and meaning
+(exshalos.c:52, 518, 718).  Failures raise exceptions where the reference
+prints and exits: ValueError for invalid sizes, MemoryError, RuntimeError for
+CUDA errors and for halos that outgrow the sigma(M) table, and
+NotImplementedError for options the GPU path does not build (R_max < 1e5,
+OUT_PROF).
+"""
+import numpy as np
+
+from .. import _capi
+
+
+def check_precision():
+    """sizeof(fft_real): 4, the grids are float32 (exshalos.c:41-43)."""
+    return int(_capi.load().exh_check_precision())
+
+
+def _params(**kw):
+    return _capi.default_params(**kw)
+
+
+def _fetch_catalogue(nh, ng, want_vel=False, want_grid=False, want_pos=False, want_flag=False, nd=None):
+    L = _capi.load()
+    out = {
+        "posh": np.zeros((nh, 3), dtype=np.float32),
+        "Mh": np.zeros(nh, dtype=np.float32),
+        "x": np.zeros((nh, 3), dtype=np.int32),
+        "count": np.zeros(nh, dtype=np.int32),
+    }
+    velh = np.zeros((nh, 3), dtype=np.float32) if want_vel else None
+    grid = np.zeros(nd, dtype=np.float32) if want_grid else None
+    pos = np.zeros((ng, 3), dtype=np.float32) if want_pos else None
+    vel = np.zeros((ng, 3), dtype=np.float32) if (want_pos and want_vel) else None
+    flag = np.zeros(nd, dtype=np.int64) if want_flag else None
+    _capi.check(L.exh_halos_fetch(_capi.context(), _capi.ptr(out["posh"]), _capi.ptr(velh), _capi.ptr(out["Mh"]),
+                                  _capi.ptr(out["x"]), _capi.ptr(out["count"]), _capi.ptr(grid), _capi.ptr(pos),
+                                  _capi.ptr(vel), _capi.ptr(flag), _capi.EXH_MEM_HOST, None))
+    if velh is not None:
+        out["velh"] = velh
+    if grid is not None:
+        out["grid"] = grid
+    if pos is not None:
+        out["pos"] = pos
+    if vel is not None:
+        out["vel"] = vel
+    if flag is not None:
+        out["flag"] = flag
+    return out
+
+
+def halos_box_from_pk(k, P, R_max, Ndx, Ndy, Ndz, Lc, seed, k_smooth, Om0, redshift, dc, Nmin, a, beta, alpha,
+                      fixed, phase, OUT_DEN, OUT_LPT, OUT_VEL, DO_2LPT, OUT_FLAG, OUT_PROF, verbose, nthreads,
+                      _catalogue=False):
+    """Halo catalogue from a linear P(k) (exshalos.c:710-940 / box.c:4-68).
+
+    Returns the reference's dictionary: "posh", "Mh" always; "velh" with
+    OUT_VEL; "pos" (and "vel" with OUT_VEL) with OUT_LPT; "flag" with OUT_FLAG;
+    "grid" with OUT_DEN.  The reference returns an empty dict for a few flag
+    combinations it does not list (e.g. OUT_DEN alone); here every requested
+    output is returned.  With _catalogue=True the Lagrangian centre cells "x"
+    and member counts "count" are added.
+    """
+    k = np.ascontiguousarray(k, dtype=np.float32)
+    P = np.ascontiguousarray(P, dtype=np.float32)
+    if k.shape != P.shape or k.ndim != 1:
+        raise ValueError("k and P must be 1-D arrays of the same length")
+    prm = _params(R_max=float(R_max), ndx=int(Ndx), ndy=int(Ndy), ndz=int(Ndz), Lc=float(Lc), seed=int(seed),
+                  k_smooth=float(k_smooth), Om0=float(Om0), redshift=float(redshift), dc=float(dc), Nmin=int(Nmin),
+                  a=float(a), beta=float(beta), alpha=float(alpha), fixed=int(fixed), phase=float(phase),
+                  OUT_DEN=int(OUT_DEN), OUT_LPT=int(OUT_LPT), OUT_VEL=int(OUT_VEL), DO_2LPT=int(DO_2LPT),
+                  OUT_FLAG=int(OUT_FLAG), OUT_PROF=int(OUT_PROF), verbose=int(verbose), nthreads=int(nthreads))
+    L = _capi.load()
+    import ctypes as C
+    nh = C.c_int64(0)
+    _capi.check(L.exh_halos_box_from_pk(_capi.context(), _capi.ptr(k), _capi.ptr(P), k.size, prm, C.byref(nh), None))
+    nd = (int(Ndx), int(Ndy), int(Ndz))
+    ng = nd[0] * nd[1] * nd[2]
+    out = _fetch_catalogue(nh.value, ng, want_vel=bool(OUT_VEL), want_grid=bool(OUT_DEN), want_pos=bool(OUT_LPT),
+                           want_flag=bool(OUT_FLAG), nd=nd)
+    if not _catalogue:
+        out.pop("x")
+        out.pop("count")
+    return out
+
+
+def find_halos(delta, k, P, Lc, Om0, redshift, dc, Nmin, a, beta, alpha, OUT_FLAG, OUT_PROF, verbose,
+               _catalogue=False, setup_fp64=0):
+    """Halos of a given density grid (exshalos.c:509-610): "posh" are the
+    Lagrangian centres Lc (x + 1/2), "Mh" the masses, "flag" with OUT_FLAG."""
+    if int(OUT_PROF):
+        raise NotImplementedError("Lagrangian profiles (OUT_PROF) are not built")
+    d = np.ascontiguousarray(delta, dtype=np.float32)
+    if d.ndim != 3:
+        raise ValueError("delta must be a 3-D grid")
+    k = np.ascontiguousarray(k, dtype=np.float32)
+    P = np.ascontiguousarray(P, dtype=np.float32)
+    prm = _params(Lc=float(Lc), Om0=float(Om0), redshift=float(redshift), dc=float(dc), Nmin=int(Nmin),
+                  a=float(a), beta=float(beta), alpha=float(alpha), verbose=int(verbose), setup_fp64=int(setup_fp64))
+    L = _capi.load()
+    import ctypes as C
+    nh = C.c_int64(0)
+    nd = d.shape
+    _capi.check(L.exh_find_halos(_capi.context(), _capi.ptr(d), nd[0], nd[1], nd[2], _capi.ptr(k), _capi.ptr(P),
+                                 k.size, prm, _capi.EXH_MEM_HOST, C.byref(nh), None))
+    out = _fetch_catalogue(nh.value, d.size, want_flag=bool(OUT_FLAG), nd=nd)
+    if not _catalogue:
+        out.pop("x")
+        out.pop("count")
+    return out
+
+
+def density_grid_compute(k, P, R_max, Ndx, Ndy, Ndz, Lc, outk, seed, fixed, phase, k_smooth, verbose, nthreads):
+    """Gaussian density grid (exshalos.c:46-121): {"grid"}.  The Fourier
+    modes are regenerated where they are needed and are not returned
+    (outk raises NotImplementedError)."""
+    if int(outk):
+        raise NotImplementedError("returning the Fourier-space grid (outk) is not built")
+    k = np.ascontiguousarray(k, dtype=np.float32)
+    P = np.ascontiguousarray(P, dtype=np.float32)
+    prm = _params(R_max=float(R_max), ndx=int(Ndx), ndy=int(Ndy), ndz=int(Ndz), Lc=float(Lc), seed=int(seed),
+                  fixed=int(fixed), phase=float(phase), k_smooth=float(k_smooth))
+    grid = np.empty((int(Ndx), int(Ndy), int(Ndz)), dtype=np.float32)
+    _capi.check(_capi.load().exh_density_grid_compute(_capi.context(), _capi.ptr(k), _capi.ptr(P), k.size, prm,
+                                                      _capi.ptr(grid), _capi.EXH_MEM_HOST, None))
+    return {"grid": grid}
+
+
+def halo_tables():
+    """Sigma(M), barrier and mass-function tables of the last halo call."""
+    import ctypes as C
+    L = _capi.load()
+    nc, nr = C.c_int(0), C.c_int(0)
+    ctx = _capi.context()
+    _capi.check(L.exh_halo_tables(ctx, C.byref(nc), C.byref(nr), None, None, None, None))
+    sig = np.zeros(nc.value, dtype=np.float32)
+    btab = np.zeros(nc.value, dtype=np.float32)
+    M = np.zeros(nr.value)
+    Int = np.zeros(nr.value)
+    _capi.check(L.exh_halo_tables(ctx, C.byref(nc), C.byref(nr), _capi.ptr(sig), _capi.ptr(btab), _capi.ptr(M),
+                                  _capi.ptr(Int)))
+    return {"Sig_grid": sig, "Btab": btab, "M": M, "Int": Int, "Ncells": nc.value}

@@ -233,3 +233,27 @@ def halos_box_from_pk(k, P, nd=64, Lc=4.0, Om0=0.31, z=0.0, dc=-1.0, Nmin=1, a=1
         out["pos"] = arr(r.S, 3 * ng, rt).reshape(ng, 3)
     L.orc_result_free(C.byref(r))
     return out
+
+
+def lpt_posh(p, k, P, flag, hx, hcount, do_2lpt=1, k_smooth=10000.0, stream=1, keep_pos=False, prec="f64"):
+    """Compute_1LPT/Compute_2LPT/Compute_Posh (lpt.c) for a given halo
+    labelling, on the field modes of the given stream."""
+    L = lib(prec)
+    rt = real_dtype(prec)
+    modes = field_modes(p, k, P, stream=stream, prec=prec)
+    nh = int(hcount.size)
+    ng = int(p.ng)
+    flag = np.ascontiguousarray(flag, dtype=np.int64).reshape(-1)
+    posh = np.zeros((max(nh, 1), 3), dtype=rt)
+    S = np.zeros((ng, 3), dtype=rt)
+    L.orc_lpt1(C.byref(p), _ptr(modes), _ptr(flag), C.c_size_t(nh), C.c_float(k_smooth), _ptr(S), _ptr(posh))
+    if do_2lpt:
+        L.orc_lpt2(C.byref(p), _ptr(S), _ptr(flag), C.c_size_t(nh), C.c_float(k_smooth), int(keep_pos), _ptr(posh))
+    hx = np.ascontiguousarray(hx, dtype=np.int32).reshape(-1)
+    hc = np.ascontiguousarray(hcount, dtype=np.int32)
+    L.orc_posh(C.byref(p), C.c_size_t(nh), _ptr(hx), _ptr(hc), _ptr(posh))
+    out = {"posh": posh[:nh]}
+    if keep_pos:
+        L.orc_pos(C.byref(p), _ptr(S))
+        out["pos"] = S
+    return out
