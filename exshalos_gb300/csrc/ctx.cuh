@@ -84,6 +84,7 @@ struct Ctx {
   DevBuf buf[B_COUNT];
   HaloState halos;
   int64_t launches = 0;
+  int verbose = 0;     // progress lines on stdout, as the reference's verbose flag
   int get_plan(int nx, int ny, int nz, FFTPlan3D** out);
 };
 

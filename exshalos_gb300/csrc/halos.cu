@@ -23,6 +23,7 @@
 //               halo's draw by GF(2) jump matrices.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -209,7 +210,8 @@ __device__ __forceinline__ int lomuto_g_dest(int a, int nL, int m, LamT lam) {
       if (lam(mid) <= a) lo = mid + 1;
       else hi = mid;
     }
-    const int c = lo;                              // >= 1
+    const int c = lo;                              // >= 1 for consistent input
+    if (c <= 0) return nL;                         // never loop on inconsistent input
     const int bnd = c < m ? min(lam(c), nL) : nL;
     const int steps = (bnd - a + c - 1) / c;
     a += c * steps;
@@ -329,8 +331,46 @@ struct SmallSortBuffers {
   unsigned* ib[2];
 };
 
-// One block sorts one segment of at most SORT_SMALL elements; one warp per
-// pending sub-segment (work stack in shared memory).
+// One block sorts one segment of at most SORT_SMALL elements, level by
+// level: in each level every warp partitions its share of the pending
+// sub-segments (Lomuto, computed as in k_qs_place), then the block
+// collects the children for the next level.  No locks and no waits other
+// than block barriers; at most n levels.
+__device__ __forceinline__ void warp_partition(float* ka, unsigned* ia, float* kb, unsigned* ib, int* lam, int lo,
+                                               int hi, int lane, int& nL_out) {
+  const float pv = ka[hi];
+  const int s = hi - lo + 1;
+  int run = 0;
+  for (int b0 = lo; b0 < hi; b0 += 32) {
+    const int p = b0 + lane;
+    const bool L = p < hi && ka[p] <= pv;
+    const unsigned msk = __ballot_sync(0xffffffffu, L);
+    const int r = run + __popc(msk & ((1u << lane) - 1u));
+    if (p < hi) {
+      if (L) { kb[lo + r] = ka[p]; ib[lo + r] = ia[p]; }
+      else lam[lo + (p - lo - r)] = r;
+    }
+    run += __popc(msk);
+  }
+  const int nL = run, m = s - 1 - nL;
+  __syncwarp();
+  for (int b0 = lo; b0 < hi; b0 += 32) {
+    const int p = b0 + lane;
+    if (p < hi && !(ka[p] <= pv)) {
+      const int* ls = lam + lo;
+      const int a = lomuto_g_dest(p - lo, nL, m, [ls](int i) { return ls[i]; });
+      const int dest = (a == nL) ? (s - 1) : a;
+      kb[lo + dest] = ka[p];
+      ib[lo + dest] = ia[p];
+    }
+  }
+  if (lane == 0) { kb[lo + nL] = ka[hi]; ib[lo + nL] = ia[hi]; }
+  __syncwarp();
+  for (int p = lo + lane; p <= hi; p += 32) { ka[p] = kb[p]; ia[p] = ib[p]; }
+  __syncwarp();
+  nL_out = nL;
+}
+
 __global__ void __launch_bounds__(SORT_T)
 k_qs_small(const Seg* __restrict__ segs, int nseg, SmallSortBuffers bufs, float* __restrict__ fkey,
            unsigned* __restrict__ fid, int* __restrict__ err) {
@@ -340,8 +380,9 @@ k_qs_small(const Seg* __restrict__ segs, int nseg, SmallSortBuffers bufs, float*
   float* kb = reinterpret_cast<float*>(ia + SORT_SMALL);
   unsigned* ib = reinterpret_cast<unsigned*>(kb + SORT_SMALL);
   int* lam = reinterpret_cast<int*>(ib + SORT_SMALL);
-  int* stk = lam + SORT_SMALL;                       // pairs (lo, hi)
-  __shared__ int sp, pending, lock, bad;
+  int* cur = lam + SORT_SMALL;              // pending (lo, hi) pairs of this level
+  int* nxt = cur + SORT_SMALL;              // two child slots per pending segment
+  __shared__ int ncur;
   if (blockIdx.x >= nseg) return;
   const Seg sg = segs[blockIdx.x];
   const int n = sg.hi - sg.lo + 1;
@@ -349,91 +390,37 @@ k_qs_small(const Seg* __restrict__ segs, int nseg, SmallSortBuffers bufs, float*
   const unsigned* si = bufs.ib[sg.buf] + sg.lo;
   for (int t = threadIdx.x; t < n; t += blockDim.x) { ka[t] = sk[t]; ia[t] = si[t]; }
   if (threadIdx.x == 0) {
-    sp = 0; lock = 0; bad = 0;
-    pending = n >= 2 ? 1 : 0;
-    if (n >= 2) { stk[0] = 0; stk[1] = n - 1; sp = 1; }
+    ncur = 0;
+    if (n >= 2) { cur[0] = 0; cur[1] = n - 1; ncur = 1; }
   }
   __syncthreads();
-  const int lane = threadIdx.x & 31;
-  long long spins = 0;
-  while (true) {
-    int lo = -1, hi = -1;
-    if (lane == 0) {
-      while (atomicCAS(&lock, 0, 1) != 0) {
-        if (++spins > (1ll << 24)) { bad = 1; break; }
-      }
-      if (!bad) {
-        if (sp > 0) { sp--; lo = stk[2 * sp]; hi = stk[2 * sp + 1]; }
-        __threadfence_block();
-        atomicExch(&lock, 0);
-      }
-    }
-    lo = __shfl_sync(0xffffffffu, lo, 0);
-    hi = __shfl_sync(0xffffffffu, hi, 0);
-    if (lo < 0) {
-      const int pend = *(volatile int*)&pending;
-      const int bd = *(volatile int*)&bad;
-      if (pend == 0 || bd) break;
-      if (++spins > (1ll << 24)) { if (lane == 0) bad = 1; break; }
-      __nanosleep(64);
-      continue;
-    }
-    // partition [lo, hi] (block-local positions)
-    const float pv = ka[hi];
-    const int s = hi - lo + 1;
-    int run = 0;
-    for (int b0 = lo; b0 < hi; b0 += 32) {
-      const int p = b0 + lane;
-      const bool L = p < hi && ka[p] <= pv;
-      const unsigned msk = __ballot_sync(0xffffffffu, L);
-      const int r = run + __popc(msk & ((1u << lane) - 1u));
-      if (p < hi) {
-        if (L) { kb[lo + r] = ka[p]; ib[lo + r] = ia[p]; }
-        else lam[lo + (p - lo - r)] = r;
-      }
-      run += __popc(msk);
-    }
-    const int nL = run, m = s - 1 - nL;
-    __syncwarp();
-    for (int b0 = lo; b0 < hi; b0 += 32) {
-      const int p = b0 + lane;
-      if (p < hi && !(ka[p] <= pv)) {
-        const int* ls = lam + lo;
-        const int a = lomuto_g_dest(p - lo, nL, m, [ls](int i) { return ls[i]; });
-        const int dest = (a == nL) ? (s - 1) : a;
-        kb[lo + dest] = ka[p];
-        ib[lo + dest] = ia[p];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int level = 0; level <= n && ncur > 0; level++) {
+    const int nc = ncur;
+    for (int q = w; q < nc; q += nw) {
+      const int lo = cur[2 * q], hi = cur[2 * q + 1];
+      int nL;
+      warp_partition(ka, ia, kb, ib, lam, lo, hi, lane, nL);
+      if (lane == 0) {
+        const int m = hi - lo - nL;
+        nxt[4 * q + 0] = nL >= 2 ? lo : -1;
+        nxt[4 * q + 1] = lo + nL - 1;
+        nxt[4 * q + 2] = m >= 2 ? lo + nL + 1 : -1;
+        nxt[4 * q + 3] = hi;
       }
     }
-    if (lane == 0) { kb[lo + nL] = ka[hi]; ib[lo + nL] = ia[hi]; }
-    __syncwarp();
-    for (int p = lo + lane; p <= hi; p += 32) { ka[p] = kb[p]; ia[p] = ib[p]; }
-    __syncwarp();
-    if (lane == 0) {
-      int nc = 0;
-      int cl[2][2];
-      if (nL >= 2) { cl[nc][0] = lo; cl[nc][1] = lo + nL - 1; nc++; }
-      if (m >= 2) { cl[nc][0] = lo + nL + 1; cl[nc][1] = hi; nc++; }
-      while (atomicCAS(&lock, 0, 1) != 0) {
-        if (++spins > (1ll << 24)) { bad = 1; break; }
-      }
-      if (!bad) {
-        for (int q = 0; q < nc; q++) { stk[2 * sp] = cl[q][0]; stk[2 * sp + 1] = cl[q][1]; sp++; }
-        atomicAdd(&pending, nc - 1);
-        __threadfence_block();
-        atomicExch(&lock, 0);
-      }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int k = 0;
+      for (int q = 0; q < 2 * nc; q++)
+        if (nxt[2 * q] >= 0) { cur[2 * k] = nxt[2 * q]; cur[2 * k + 1] = nxt[2 * q + 1]; k++; }
+      ncur = k;
     }
-    __syncwarp();
+    __syncthreads();
   }
-  __syncthreads();
-  if (bad) {
-    if (threadIdx.x == 0) atomicExch(err, 1);
-    return;
-  }
+  if (ncur > 0 && threadIdx.x == 0) atomicExch(err, 1);
   for (int t = threadIdx.x; t < n; t += blockDim.x) { fkey[sg.lo + t] = ka[t]; fid[sg.lo + t] = ia[t]; }
 }
-
 int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
   const int np = (int)h->np;
   const size_t cap = std::max<size_t>(np, 1);
@@ -513,6 +500,7 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
     }
     // a level holds segments from one buffer only: children all live in buf^1
     large.swap(next);
+    if (c.verbose) { printf("  sort level: %zu large, %zu small, %zu single\n", large.size(), small.size(), single_pos.size()); fflush(stdout); }
   }
   if (!single_pos.empty()) {
     const int ns = (int)single_pos.size();
@@ -537,7 +525,7 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
     EXH_TRY(c.buf[B_HOSTIO2].ensure(64));
     int* d_err = c.buf[B_HOSTIO2].as<int>();
     EXH_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
-    const size_t sm = (size_t)SORT_SMALL * (4 * 4 + 4) + sizeof(int) * 2 * (SORT_SMALL + 2);
+    const size_t sm = (size_t)SORT_SMALL * (4 * 4 + 4) + sizeof(int) * 3 * (size_t)SORT_SMALL;
     EXH_CUDA_TRY(set_smem(k_qs_small, sm));
     SmallSortBuffers sb{{kb[0], kb[1]}, {ib[0], ib[1]}};
     k_qs_small<<<ns, SORT_T, sm, st>>>(d_segs, ns, sb, fk, fi, d_err);
@@ -547,8 +535,8 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
     EXH_CUDA_TRY(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
     EXH_CUDA_TRY(cudaStreamSynchronize(st));
     if (herr) {
-      exh_set_error_msg("peak sort: work-stack wait exceeded its bound", __FILE__, __LINE__);
-      return EXH_E_TIMEOUT;
+      exh_set_error_msg("peak sort: a block segment did not finish", __FILE__, __LINE__);
+      return EXH_E_RANGE;
     }
   }
   h->key = fk;
@@ -747,6 +735,7 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   if (nproc == 0) return EXH_OK;
   GrowArgs A{delta, h->key, h->id, np, (int)nproc, hs, Btab_dev, t};
   const unsigned nb = exh_div_up(nproc, 128);
+  if (c.verbose) { printf("  %lld peaks above the barrier\n", (long long)nproc); fflush(stdout); }
   k_gfree<<<nb, 128, 0, st>>>(A, h->gfree);
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
@@ -771,6 +760,7 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
                         __FILE__, __LINE__);
       return EXH_E_RANGE;
     }
+    if (c.verbose > 1) { printf("  growth round %d: %d pending\n", round, hc[0]); fflush(stdout); }
     if (hc[0] == 0) break;
     round++;
     if (round > nproc + 2) {

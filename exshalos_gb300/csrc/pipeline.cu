@@ -2,6 +2,7 @@
 // (src/exshalos/box.c:4-68, binding exshalos.c:710-940), Find_Halos on a
 // given grid (exshalos.c:509-610), the Gaussian field alone
 // (exshalos.c:46-121) and the result fetch.
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -52,7 +53,9 @@ int run_halo_finder(Ctx& c, const BoxParams& b, const float* k, const float* P, 
   float* Btab_dev = c.buf[B_HOSTIO].as<float>();
   EXH_CUDA_TRY(cudaMemcpyAsync(Btab_dev, tab.Btab.data(), sizeof(float) * tab.Ncells, cudaMemcpyHostToDevice, st));
   EXH_TRY(find_peaks(c, delta, b, h, st));
+  if (c.verbose) { printf("There are %lld peaks\n", (long long)h->np); fflush(stdout); }
   EXH_TRY(sort_peaks(c, h, st));
+  if (c.verbose) { printf("peaks sorted\n"); fflush(stdout); }
   HaloScalars hs;
   hs.Bmin = tab.Btab[tab.Ncells - 1];
   hs.Mtot = b.Mtot;
@@ -61,6 +64,7 @@ int run_halo_finder(Ctx& c, const BoxParams& b, const float* k, const float* P, 
   hs.nmin_half = b.nmin / 2;
   hs.n0 = b.nd[0]; hs.n1 = b.nd[1]; hs.n2 = b.nd[2];
   EXH_TRY(grow_halos(c, delta, b, hs, Btab_dev, *t, h, st));
+  if (c.verbose) { printf("There are %lld halos\n", (long long)h->nh); fflush(stdout); }
   const size_t nh = std::max<int64_t>(h->nh, 1);
   EXH_TRY(c.buf[B_MH].ensure((sizeof(float) + 4 * sizeof(int)) * nh));
   float* Mh = c.buf[B_MH].as<float>();
@@ -137,6 +141,7 @@ int exh_halos_box_from_pk(exh_ctx* ctx, const float* k, const float* P, int Nk, 
   EXH_CUDA_TRY(cudaSetDevice(c.device));
   cudaStream_t st = (cudaStream_t)stream;
   halo_state_release(c);
+  c.verbose = prm->verbose;
   BoxParams b;
   EXH_TRY(setup_box(&b, prm->ndx, prm->ndy, prm->ndz, prm->Lc, prm->Om0, prm->redshift, prm->dc, prm->Nmin, prm->a,
                     prm->beta, prm->alpha, prm->seed));
@@ -203,6 +208,7 @@ int exh_find_halos(exh_ctx* ctx, const float* delta, int ndx, int ndy, int ndz, 
   EXH_CUDA_TRY(cudaSetDevice(c.device));
   cudaStream_t st = (cudaStream_t)stream;
   halo_state_release(c);
+  c.verbose = prm->verbose;
   BoxParams b;
   // find_halos binds the mass draws to seed 12345 (exshalos.c:552)
   EXH_TRY(setup_box(&b, ndx, ndy, ndz, prm->Lc, prm->Om0, prm->redshift, prm->dc, prm->Nmin, prm->a, prm->beta,

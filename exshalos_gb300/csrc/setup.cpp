@@ -18,31 +18,42 @@ namespace exh {
 
 static const double kMmax = 1e+16;  // exshalos_h.h:47
 
+// The reference calls the C <math.h> functions, which take and return double
+// even for float arguments; these wrappers keep that promotion (the C++
+// overloads would otherwise pick the float versions).
+static inline double c_sqrt(double x) { return std::sqrt(x); }
+static inline double c_pow(double x, double y) { return std::pow(x, y); }
+static inline double c_sin(double x) { return std::sin(x); }
+static inline double c_cos(double x) { return std::cos(x); }
+static inline double c_exp(double x) { return std::exp(x); }
+static inline double c_log10(double x) { return std::log10(x); }
+static inline double c_log(double x) { return std::log(x); }
+
 int setup_box(BoxParams* b, int ndx, int ndy, int ndz, float Lc, float Om0, float z, float dc, int Nmin,
               float a, float beta, float alpha, int seed) {
   std::memset(b, 0, sizeof(*b));
   b->Om0 = Om0;
   b->redshift = z;
   b->rhoc = 2.775e+11f;
-  const double zp3 = std::pow(1.0 + (double)b->redshift, 3.0);
-  b->Hz = (float)(100.0 * std::sqrt(b->Om0 * zp3 + (1.0 - b->Om0)));
+  const double zp3 = c_pow(1.0 + (double)b->redshift, 3.0);
+  b->Hz = (float)(100.0 * c_sqrt(b->Om0 * zp3 + (1.0 - b->Om0)));
   b->Omz = (float)(b->Om0 * zp3 / (b->Om0 * zp3 + (1.0 - b->Om0)));
   b->rhomz = b->Om0 * b->rhoc;
-  b->dc = dc <= 0.0f ? (float)(1.686 * std::pow((double)b->Omz, 0.0055)) : dc;
+  b->dc = dc <= 0.0f ? (float)(1.686 * c_pow((double)b->Omz, 0.0055)) : dc;
   b->Omz_d = (double)Om0 * zp3 / ((double)Om0 * zp3 + (1.0 - (double)Om0));
-  b->Hz_d = 100.0 * std::sqrt((double)Om0 * zp3 + (1.0 - (double)Om0));
+  b->Hz_d = 100.0 * c_sqrt((double)Om0 * zp3 + (1.0 - (double)Om0));
   if (!(Lc > 0.0f && Lc < 100.0f)) return EXH_E_INVALID;    // Lc_MAX, exshalos_h.h:45
   b->nd[0] = ndx; b->nd[1] = ndy; b->nd[2] = ndz;
   b->ng = (size_t)ndx * (size_t)ndy * (size_t)ndz;
   b->nz2 = ndz / 2 + 1;
   b->Lc = Lc;
-  b->Mcell = (float)(b->rhomz * std::pow((double)Lc, 3.0));
+  b->Mcell = (float)(b->rhomz * c_pow((double)Lc, 3.0));
   for (int i = 0; i < 3; i++) b->L[i] = b->Lc * b->nd[i];
   b->Mtot = b->rhomz * b->L[0] * b->L[1] * b->L[2];
   for (int i = 0; i < 3; i++) b->kl[i] = (float)(2.0 * M_PI / b->L[i]);
   const float vol = b->L[0] * b->L[1] * b->L[2];
-  b->Normx = (float)(1.0 / std::sqrt((double)vol));
-  b->Normk = (float)(std::sqrt((double)vol) / (double)(ndx * ndy * ndz));
+  b->Normx = (float)(1.0 / c_sqrt((double)vol));
+  b->Normk = (float)(c_sqrt((double)vol) / (double)(ndx * ndy * ndz));
   b->nmin = std::min(ndx, std::min(ndy, ndz));
   b->Nmin = Nmin; b->seed = seed;
   b->a = a; b->beta = beta; b->alpha = alpha;
@@ -97,18 +108,18 @@ double Spline::eval(double q, int* status) const {
 int ncells(const BoxParams& b) { return (int)std::floor(kMmax / b.Mcell); }
 
 static float tophat_f(float k, float R) {
-  return (float)(3.0 / (std::pow(k * R, 2)) * (std::sin(k * R) / (k * R) - std::cos(k * R)));
+  return (float)(3.0 / (c_pow(k * R, 2)) * (c_sin(k * R) / (k * R) - c_cos(k * R)));
 }
 static double tophat_d(double k, double R) {
   const double x = k * R;
-  return 3.0 / (x * x) * (std::sin(x) / x - std::cos(x));
+  return 3.0 / (x * x) * (c_sin(x) / x - c_cos(x));
 }
 
 static float sigma2_f(const float* k, const float* P, int Nk, float R) {
   float acc = 0.0f;
   for (int i = 0; i < Nk - 1; i++)
     acc += (k[i + 1] - k[i]) / 2.0 *
-           (P[i] * std::pow(k[i] * tophat_f(k[i], R), 2) + P[i + 1] * std::pow(k[i + 1] * tophat_f(k[i + 1], R), 2));
+           (P[i] * c_pow(k[i] * tophat_f(k[i], R), 2) + P[i + 1] * c_pow(k[i + 1] * tophat_f(k[i + 1], R), 2));
   return (float)(acc / (2.0 * M_PI * M_PI));
 }
 static double sigma2_d(const float* k, const float* P, int Nk, double R) {
@@ -124,16 +135,16 @@ static double sigma2_d(const float* k, const float* P, int Nk, double R) {
 // Tinker et al. (2008) multiplicity function at Delta = 300
 static float tinker_f(float s) {
   const float B = 0.466f, d = 2.06f, e = 0.99f, f = 0.48f, g = 1.310f;
-  return (float)(B * (std::pow(s / e, -d) + std::pow(s, -f)) * std::exp(-g / (s * s)));
+  return (float)(B * (c_pow(s / e, -d) + c_pow(s, -f)) * c_exp(-g / (s * s)));
 }
 static double tinker_d(double s) {
   const double B = 0.466, d = 2.06, e = 0.99, f = 0.48, g = 1.310;
-  return B * (std::pow(s / e, -d) + std::pow(s, -f)) * std::exp(-g / (s * s));
+  return B * (c_pow(s / e, -d) + c_pow(s, -f)) * c_exp(-g / (s * s));
 }
 
 float barrier(const BoxParams& b, float S) {
   if (b.DO_EB == 0) return b.dc;
-  return (float)(std::sqrt(b.a) * b.dc * (1.0 + b.beta * std::pow(S / (b.a * b.dc * b.dc), b.alpha)));
+  return (float)(c_sqrt(b.a) * b.dc * (1.0 + b.beta * c_pow(S / (b.a * b.dc * b.dc), b.alpha)));
 }
 
 int halo_tables(const BoxParams& b, const float* K, const float* P, int Nk, int prec64, std::vector<float>& Sig_grid,
@@ -144,38 +155,38 @@ int halo_tables(const BoxParams& b, const float* K, const float* P, int Nk, int 
   Int.assign(Nr, 0.0);
   std::vector<double> sig(Nr), R(Nr);
   if (!prec64) {
-    const float Rmin = (float)std::pow(b.Mcell * 0.9 * 3.0 / (4.0 * M_PI * b.rhomz), 1.0 / 3.0);
-    const float Rmax = (float)std::pow(kMmax * 3.0 / (4.0 * M_PI * b.rhomz), 1.0 / 3.0);
+    const float Rmin = (float)c_pow(b.Mcell * 0.9 * 3.0 / (4.0 * M_PI * b.rhomz), 1.0 / 3.0);
+    const float Rmax = (float)c_pow(kMmax * 3.0 / (4.0 * M_PI * b.rhomz), 1.0 / 3.0);
     for (int i = 0; i < Nr; i++) {
-      const float r = (float)std::pow(10, std::log10(Rmin) + i * (std::log10(Rmax) - std::log10(Rmin)) / (Nr - 1));
+      const float r = (float)c_pow(10, c_log10(Rmin) + i * (c_log10(Rmax) - c_log10(Rmin)) / (Nr - 1));
       R[i] = r;
-      M[i] = (double)4.0 / 3.0 * M_PI * ((float)b.rhomz * std::pow(r, 3));
+      M[i] = (double)4.0 / 3.0 * M_PI * ((float)b.rhomz * c_pow(r, 3));
     }
-    for (int i = 0; i < Nr; i++) sig[i] = (double)std::sqrt(sigma2_f(K, P, Nk, (float)R[i]));
+    for (int i = 0; i < Nr; i++) sig[i] = (double)c_sqrt(sigma2_f(K, P, Nk, (float)R[i]));
   } else {
-    const double Rmin = std::pow((double)b.Mcell * 0.9 * 3.0 / (4.0 * M_PI * (double)b.rhomz), 1.0 / 3.0);
-    const double Rmax = std::pow(kMmax * 3.0 / (4.0 * M_PI * (double)b.rhomz), 1.0 / 3.0);
+    const double Rmin = c_pow((double)b.Mcell * 0.9 * 3.0 / (4.0 * M_PI * (double)b.rhomz), 1.0 / 3.0);
+    const double Rmax = c_pow(kMmax * 3.0 / (4.0 * M_PI * (double)b.rhomz), 1.0 / 3.0);
     for (int i = 0; i < Nr; i++) {
-      R[i] = std::pow(10.0, std::log10(Rmin) + i * (std::log10(Rmax) - std::log10(Rmin)) / (Nr - 1));
-      M[i] = 4.0 / 3.0 * M_PI * (double)b.rhomz * std::pow(R[i], 3);
+      R[i] = c_pow(10.0, c_log10(Rmin) + i * (c_log10(Rmax) - c_log10(Rmin)) / (Nr - 1));
+      M[i] = 4.0 / 3.0 * M_PI * (double)b.rhomz * c_pow(R[i], 3);
     }
-    for (int i = 0; i < Nr; i++) sig[i] = std::sqrt(sigma2_d(K, P, Nk, R[i]));
+    for (int i = 0; i < Nr; i++) sig[i] = c_sqrt(sigma2_d(K, P, Nk, R[i]));
   }
   Spline s;
   if (s.init(M.data(), sig.data(), Nr) != EXH_OK) return EXH_E_INVALID;
   Sig_grid.assign(Nc, 0.f);
   Sig_grid[0] = 1e+30f;
   int st = 0;
-  for (int i = 1; i < Nc; i++) Sig_grid[i] = (float)std::pow(s.eval((double)i * b.Mcell, &st), 2.0);
+  for (int i = 1; i < Nc; i++) Sig_grid[i] = (float)c_pow(s.eval((double)i * b.Mcell, &st), 2.0);
   if (st) return EXH_E_RANGE;
   for (int i = 1; i < Nr; i++) {
     if (!prec64) {
       const float r1 = (float)R[i], r0 = (float)R[i - 1];
-      Int[i] = Int[i - 1] - (double)(std::log(sig[i]) - std::log(sig[i - 1])) / 2.0 *
-                                (tinker_f((float)sig[i]) / std::pow(r1, 3.0) + tinker_f((float)sig[i - 1]) / std::pow(r0, 3.0));
+      Int[i] = Int[i - 1] - (double)(c_log(sig[i]) - c_log(sig[i - 1])) / 2.0 *
+                                (tinker_f((float)sig[i]) / c_pow(r1, 3.0) + tinker_f((float)sig[i - 1]) / c_pow(r0, 3.0));
     } else {
-      Int[i] = Int[i - 1] - (std::log(sig[i]) - std::log(sig[i - 1])) / 2.0 *
-                                (tinker_d(sig[i]) / std::pow(R[i], 3.0) + tinker_d(sig[i - 1]) / std::pow(R[i - 1], 3.0));
+      Int[i] = Int[i - 1] - (c_log(sig[i]) - c_log(sig[i - 1])) / 2.0 *
+                                (tinker_d(sig[i]) / c_pow(R[i], 3.0) + tinker_d(sig[i - 1]) / c_pow(R[i - 1], 3.0));
     }
     if (Int[i] == Int[i - 1]) Int[i] = Int[i - 1] * 1.000001;
   }
@@ -196,8 +207,8 @@ int amplitude_table(const BoxParams& b, const float* K, const float* P, int Nk, 
   A.assign(nmax + 1, 0.f);
   int st = 0;
   for (int n2 = 1; n2 <= nmax; n2++) {
-    const double k = kf * std::sqrt((double)n2);
-    A[n2] = (float)std::sqrt(s.eval(k, &st) / 2.0);
+    const double k = kf * c_sqrt((double)n2);
+    A[n2] = (float)c_sqrt(s.eval(k, &st) / 2.0);
   }
   return st ? EXH_E_RANGE : EXH_OK;
 }
