@@ -1,0 +1,329 @@
+#!/usr/bin/env python
+"""Benchmark of the mock-generation path: 256^3 realisations per second.
+
+One step = one realisation of the single-box workload: Gaussian field
+(nd = 256, Lc = 2 Mpc/h, L = 512 Mpc/h, synthetic BBKS P(k)), halo finding
+with the ellipsoidal barrier (a = 1, beta = 0.12, alpha = 0), 2LPT
+displacement of the halos, CIC of the halo positions on a 256^3 grid and the
+power spectrum in 128 bins.  Every step draws a new Philox seed.
+
+  value   device-resident: C ABI calls with device buffers (k, P are the only
+          inputs, 8 KB), halo positions and the grid stay in HBM
+  e2e     the public Python API (mock.Generate_Halos_Box_from_Pk ->
+          simulation.Compute_Density_Grid -> simulation.Compute_Power_Spectrum)
+          with host numpy arrays, copies in both directions inside the timing
+  --impl reference
+          the reference's CPU algorithm (the oracle's C restatement in the
+          reference's float precision, GSL-taus field stream) on all host
+          cores, one full 256^3 realisation per step
+
+Multi-GPU: one process per GPU (torchrun); realisations are independent, so
+every rank runs its own seeds (weak scaling) and value sums all ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ND, LC, NK_PK = 256, 2.0, 128
+BARRIER = dict(a=1.0, beta=0.12, alpha=0.0)
+METRIC = "256^3 realisations/s (halos+P(k))"
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[2:6]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        v = d.get("hbm_gbs") or d.get("hbm_GBs") or d.get("hbm")
+        if isinstance(v, dict):
+            v = v.get("value") or v.get("burst")
+        return float(v), "measured"
+    except (OSError, ValueError, TypeError):
+        return 6800.0, "fallback"
+
+
+def committed_traffic():
+    """DRAM bytes per launch of the dominant kernel class from the committed
+    ncu summary (profiles/*.txt lines 'traffic_per_launch <class> <bytes>')."""
+    out = {}
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return out
+    for fn in sorted(os.listdir(pdir)):
+        if not fn.endswith(".txt"):
+            continue
+        with open(os.path.join(pdir, fn)) as f:
+            for line in f:
+                p = line.split()
+                if len(p) == 3 and p[0] == "traffic_per_launch":
+                    try:
+                        out[p[1]] = float(p[2])
+                    except ValueError:
+                        pass
+    return out
+
+
+def cpu_baseline_sample(k, P, seed=1):
+    """The reference algorithm on the host: one full 256^3 realisation (Lc = 2)
+    with the GSL-taus field stream in float precision, all host threads."""
+    from oracle import orc
+    nthr = os.cpu_count() or 1
+    orc.set_threads(nthr, prec="f32")
+    nd = ND
+    t0 = time.perf_counter()
+    r = orc.halos_box_from_pk(k, P, nd=nd, Lc=LC, seed=seed, stream=0, do_2lpt=1, prec="f32", **BARRIER)
+    g = orc.cic(r["posh"], nd, nd * LC, prec="f32")
+    orc.power(g, nd * LC, window=2, Nk=NK_PK, prec="f32")
+    dt = time.perf_counter() - t0
+    equiv = (nd / ND) ** 3
+    return dt, equiv, nthr
+
+
+def run_reference(args, ws, rank):
+    from exshalos_gb300.workloads import synthetic_pk
+    if rank != 0:
+        return
+    k, P = synthetic_pk()
+    k, P = k.astype(np.float32), P.astype(np.float32)
+    for w in range(args.warmup):
+        cpu_baseline_sample(k, P, seed=100 + w)
+    tot, eq = 0.0, 0.0
+    nthr = 1
+    for s in range(args.steps):
+        dt, e, nthr = cpu_baseline_sample(k, P, seed=s + 1)
+        tot += dt
+        eq += e
+    v = eq / tot
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "realisations/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tot / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "box_256 (nd=256, Lc=2, L=512, 2LPT, barrier a=1 beta=0.12 alpha=0, CIC 256^3, "
+                                   "P(k) 128 bins)", "sample": "one full 256^3 realisation per step"},
+            "cpu_baseline": {"value": v, "unit": "realisations/s", "cores": nthr, "kind": "port",
+                             "sample": "one 256^3 realisation (field, halos, 2LPT, CIC, P(k)) per step"},
+            "e2e": {"value": v, "unit": "realisations/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, ws, rank, local):
+    os.environ["EXH_DEVICE"] = str(local)
+    import ctypes as C
+
+    import torch
+    torch.cuda.set_device(local)
+    from exshalos_gb300 import _capi
+    from exshalos_gb300 import mock, simulation
+    from exshalos_gb300.workloads import synthetic_pk
+    k, P = synthetic_pk()
+    k, P = k.astype(np.float32), P.astype(np.float32)
+    L_ = _capi.load()
+    ctx = _capi.context()
+    ng = ND ** 3
+    Lbox = np.float32(ND * LC)
+    kmin, kmax = np.float32(2 * np.pi / Lbox), np.float32(np.pi / Lbox * ND)
+    posh_dev = torch.empty(3 * ng // 2, dtype=torch.float32, device="cuda")
+    grid_dev = torch.empty(ng, dtype=torch.float32, device="cuda")
+    k_out = np.zeros(NK_PK, dtype=np.float32)
+    P_out = np.zeros(NK_PK, dtype=np.float32)
+    c_out = np.zeros(NK_PK, dtype=np.int64)
+    nh = C.c_int64(0)
+    nh_seen = []
+
+    def step(seed):
+        prm = _capi.default_params(ndx=ND, ndy=ND, ndz=ND, Lc=LC, seed=seed, DO_2LPT=1, **BARRIER)
+        _capi.check(L_.exh_halos_box_from_pk(ctx, _capi.ptr(k), _capi.ptr(P), k.size, prm, C.byref(nh), None))
+        _capi.check(L_.exh_halos_fetch(ctx, _capi.ptr(posh_dev), None, None, None, None, None, None, None, None,
+                                       _capi.EXH_MEM_DEVICE, None))
+        _capi.check(L_.exh_grid_compute(ctx, _capi.ptr(posh_dev), nh.value, ND, float(Lbox), 2, 1,
+                                        _capi.ptr(grid_dev), _capi.EXH_MEM_DEVICE, None))
+        _capi.check(L_.exh_power_compute(ctx, _capi.ptr(grid_dev), ND, float(Lbox), 2, NK_PK, float(kmin),
+                                         float(kmax), _capi.ptr(k_out), _capi.ptr(P_out), _capi.ptr(c_out),
+                                         _capi.EXH_MEM_DEVICE, None))
+        nh_seen.append(nh.value)
+
+    seed0 = 1000 * rank + 1
+    for w in range(args.warmup):
+        step(seed0 + 500 + w)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    _capi.timing_enable(True)
+    l0 = _capi.launch_count()
+    barrier(ws)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for s in range(args.steps):
+        step(seed0 + s)
+    ev1.record()
+    torch.cuda.synchronize()
+    barrier(ws)
+    launches = _capi.launch_count() - l0
+    rep = _capi.timing_report()
+    _capi.timing_enable(False)
+    clk = clocks.stop()
+    t_dev = ev0.elapsed_time(ev1) / 1000.0
+    t_max = max_over_ranks(t_dev, ws)
+    value = ws * args.steps / t_max
+
+    # end to end through the public API with host arrays
+    e2e_steps = max(1, min(args.steps, 5))
+    h2d = d2h = 0
+    barrier(ws)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in range(e2e_steps):
+        r = mock.Generate_Halos_Box_from_Pk(k, P, nd=ND, Lc=LC, seed=seed0 + 200 + s, DO_2LPT=True, **BARRIER)
+        grid = simulation.Compute_Density_Grid(r["posh"], nd=ND, L=float(Lbox), window="CIC")
+        pk = simulation.Compute_Power_Spectrum(grid, L=float(Lbox), window="CIC", Nk=NK_PK)
+        n = r["posh"].shape[0]
+        h2d += k.nbytes + P.nbytes + 12 * n + 4 * ng
+        d2h += 16 * n + 4 * ng + pk["k"].nbytes + pk["Pk"].nbytes + pk["Nk"].nbytes
+    torch.cuda.synchronize()
+    t_e2e = max_over_ranks(time.perf_counter() - t0, ws)
+    e2e = ws * e2e_steps / t_e2e
+
+    # roofline of the dominant kernel class (live CUDA-event timing)
+    dom = max(rep.items(), key=lambda kv: kv[1][0])
+    name, (ms, nl, by) = dom
+    peak, peak_kind = measured_peak()
+    achieved = (by / nl) / ((ms / nl) / 1000.0) / 1e9 if nl and ms > 0 else None
+    traffic = committed_traffic().get(name)
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        dt, eq, nthr = cpu_baseline_sample(k, P)
+        cpu = {"value": eq / dt, "unit": "realisations/s", "cores": nthr, "kind": "port",
+               "sample": "one 256^3 realisation (field, halos, 2LPT, CIC, P(k)) in the reference's float "
+                         "arithmetic and GSL-taus field stream"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "realisations/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "box_256: nd=256, Lc=2 Mpc/h (L=512), synthetic BBKS P(k) sigma8=0.81, 2LPT, barrier "
+                               "a=1 beta=0.12 alpha=0, CIC 256^3 of the halos, P(k) 128 bins; new seed per step",
+                   "l2": "inputs and intermediates (>1 GB per realisation) exceed L2",
+                   "smoothing_ladder": "not in the step",
+                   "mean_halos": float(np.mean(nh_seen[-args.steps:])) if nh_seen else None},
+        "e2e": {"value": e2e, "unit": "realisations/s", "h2d_bytes_per_step": int(h2d / e2e_steps),
+                "d2h_bytes_per_step": int(d2h / e2e_steps)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
+                     "traffic": traffic, "launches": nl, "ms_total": ms},
+        "stage_ms_per_step": {kk: round(v[0] / args.steps, 4) for kk, v in rep.items() if v[1]},
+        "clocks": clk,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_ours(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -61,7 +61,26 @@ SIGNATURES = {
     "exh_fft_r2c_3d": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P]),
     "exh_fft_c2r_3d": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P]),
     "exh_launch_count": (C.c_int64, [_P]),
+    "exh_timing_enable": (C.c_int, [C.c_int]),
+    "exh_timing_report": (C.c_int, [C.c_int, _P, _P, _P]),
 }
+
+TIMING_CLASSES = ["fft_strided", "fft_rows", "peaks", "sort", "grow", "mass", "lpt_stencil", "halo_disp", "cic",
+                  "pk_bin", "other"]
+
+
+def timing_enable(on=True):
+    load().exh_timing_enable(1 if on else 0)
+
+
+def timing_report():
+    """{class: (ms, launches, bytes)} since timing_enable(True)."""
+    n = len(TIMING_CLASSES)
+    ms = np.zeros(n)
+    la = np.zeros(n, dtype=np.int64)
+    by = np.zeros(n)
+    load().exh_timing_report(n, ptr(ms), ptr(la), ptr(by))
+    return {TIMING_CLASSES[i]: (float(ms[i]), int(la[i]), float(by[i])) for i in range(n)}
 
 
 def lib_path():

@@ -12,6 +12,7 @@
 // instead of as separate sweeps over HBM.
 #pragma once
 #include "exh_common.cuh"
+#include "timing.cuh"
 
 namespace exh {
 
@@ -116,6 +117,7 @@ __device__ __forceinline__ float2* stockham_run(float2* a, float2* b, const Radi
 // ---------------------------------------------------------------- functors
 // complex array [outer][n][inner]
 struct CplxLoad {
+  static constexpr int io_bytes = 8;
   const float2* __restrict__ p;
   int n, inner;
   __device__ __forceinline__ float2 operator()(int o, int e, int i) const {
@@ -123,6 +125,7 @@ struct CplxLoad {
   }
 };
 struct CplxStore {
+  static constexpr int io_bytes = 8;
   float2* __restrict__ p;
   int n, inner;
   __device__ __forceinline__ void operator()(int o, int e, int i, float2 v) const {
@@ -131,6 +134,7 @@ struct CplxStore {
 };
 // real rows: element (row, m) of the packed pair view (x[2m], x[2m+1])
 struct RealPairLoad {
+  static constexpr int io_bytes = 8;
   const float* __restrict__ p;
   int N;
   __device__ __forceinline__ float2 operator()(size_t row, int m) const {
@@ -138,6 +142,7 @@ struct RealPairLoad {
   }
 };
 struct RealPairStore {
+  static constexpr int io_bytes = 8;
   float* __restrict__ p;
   int N;
   float scale;
@@ -147,11 +152,13 @@ struct RealPairStore {
 };
 // half-complex rows [row][nc]
 struct HalfLoad {
+  static constexpr int io_bytes = 8;
   const float2* __restrict__ p;
   int nc;
   __device__ __forceinline__ float2 operator()(size_t row, int k) const { return p[row * nc + k]; }
 };
 struct HalfStore {
+  static constexpr int io_bytes = 8;
   float2* __restrict__ p;
   int nc;
   __device__ __forceinline__ void operator()(size_t row, int k, float2 v) const { p[row * nc + k] = v; }
@@ -269,6 +276,9 @@ inline cudaError_t set_smem(K kernel, size_t bytes) {
 }
 
 // Strided pass launcher: data [outer][n][inner].
+// bytes each functor moves per complex element (0 for generators)
+template <class F> constexpr int io_bytes() { return F::io_bytes; }
+
 template <class Src, class Dst>
 inline cudaError_t launch_strided(Src src, Dst dst, const RadixPlan& pl, const float2* tw, float sgn,
                                   int outer, int inner, cudaStream_t st) {
@@ -277,6 +287,7 @@ inline cudaError_t launch_strided(Src src, Dst dst, const RadixPlan& pl, const f
   cudaError_t e = set_smem(kern, sm);
   if (e != cudaSuccess) return e;
   dim3 grid(exh_div_up(inner, FFT_W), outer);
+  KTimer kt(KC_FFT_STRIDED, st, (double)pl.n * inner * outer * (io_bytes<Src>() + io_bytes<Dst>()));
   kern<<<grid, FFT_THREADS, sm, st>>>(src, dst, pl, tw, sgn, inner);
   count_launch(1);
   return cudaGetLastError();
@@ -288,6 +299,7 @@ inline cudaError_t launch_r2c_rows(Src src, Dst dst, const FFTPlan3D& p, size_t 
   size_t sm = smem_r2c(p.M);
   cudaError_t e = set_smem(kern, sm);
   if (e != cudaSuccess) return e;
+  KTimer kt(KC_FFT_ROWS, st, (double)rows * (p.M * io_bytes<Src>() + (p.M + 1) * io_bytes<Dst>()));
   kern<<<exh_div_up(rows, FFT_ROWS), FFT_THREADS, sm, st>>>(src, dst, p.pm, p.twm, p.twn, rows);
   count_launch(1);
   return cudaGetLastError();
@@ -299,6 +311,7 @@ inline cudaError_t launch_c2r_rows(Src src, Dst dst, const FFTPlan3D& p, size_t 
   size_t sm = smem_c2r(p.M);
   cudaError_t e = set_smem(kern, sm);
   if (e != cudaSuccess) return e;
+  KTimer kt(KC_FFT_ROWS, st, (double)rows * ((p.M + 1) * io_bytes<Src>() + p.M * io_bytes<Dst>()));
   kern<<<exh_div_up(rows, FFT_ROWS), FFT_THREADS, sm, st>>>(src, dst, p.pm, p.twm, p.twn, rows);
   count_launch(1);
   return cudaGetLastError();

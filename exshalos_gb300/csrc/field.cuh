@@ -82,6 +82,7 @@ struct FieldModes {
 
 // Source functor of the x pass: (o = 0, e = i, inner = j * nc + k)
 struct FieldGen {
+  static constexpr int io_bytes = 0;
   FieldModes m;
   __device__ __forceinline__ float2 operator()(int, int e, int inner) const {
     return m.mode(e, inner / m.nc, inner % m.nc);

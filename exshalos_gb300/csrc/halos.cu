@@ -170,7 +170,8 @@ int find_peaks(Ctx& c, const float* delta, const BoxParams& b, HaloDev* h, cudaS
   unsigned* off = cnt + nb;
   unsigned* sums = off + nb;
   unsigned* total = sums + nb + 32;
-  k_peak_mask<<<nb, PK_T, 0, st>>>(delta, b.nd[0], b.nd[1], b.nd[2], ng, mask, cnt);
+  { KTimer kt(KC_PEAKS, st, 4.0 * ng + ng / 8.0);
+  k_peak_mask<<<nb, PK_T, 0, st>>>(delta, b.nd[0], b.nd[1], b.nd[2], ng, mask, cnt); }
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   EXH_CUDA_TRY(exclusive_scan<unsigned>(cnt, off, nb, sums, total, st));
@@ -182,7 +183,8 @@ int find_peaks(Ctx& c, const float* delta, const BoxParams& b, HaloDev* h, cudaS
   EXH_TRY(c.buf[B_PEAKS].ensure((sizeof(float) + sizeof(unsigned)) * cap * 3));
   h->key = c.buf[B_PEAKS].as<float>();
   h->id = reinterpret_cast<unsigned*>(h->key + cap);
-  k_peak_write<<<nb, PK_T, 0, st>>>(delta, ng, mask, off, h->key, h->id);
+  { KTimer kt(KC_PEAKS, st, ng / 8.0 + 12.0 * np);
+  k_peak_write<<<nb, PK_T, 0, st>>>(delta, ng, mask, off, h->key, h->id); }
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   return EXH_OK;
@@ -475,6 +477,7 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
     EXH_CUDA_TRY(cudaMemcpyAsync(d_cseg, hcseg.data(), sizeof(int) * nch, cudaMemcpyHostToDevice, st));
     EXH_CUDA_TRY(cudaMemcpyAsync(d_coff, hcoff.data(), sizeof(int) * nch, cudaMemcpyHostToDevice, st));
     EXH_CUDA_TRY(cudaMemcpyAsync(d_cfirst, hcfirst.data(), sizeof(int) * (nseg + 1), cudaMemcpyHostToDevice, st));
+    KTimer kt(KC_SORT, st, 0.0);
     k_qs_count<<<nch, CH_T, 0, st>>>(kb[buf], d_segs, d_cseg, d_coff, nch, d_cL);
     k_qs_seg_scan<<<nseg, 256, 0, st>>>(d_cfirst, nseg, d_cL, d_nl);
     k_qs_place<1><<<nch, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, nch, d_cL, d_nl, lam,
@@ -528,7 +531,8 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
     const size_t sm = (size_t)SORT_SMALL * (4 * 4 + 4) + sizeof(int) * 3 * (size_t)SORT_SMALL;
     EXH_CUDA_TRY(set_smem(k_qs_small, sm));
     SmallSortBuffers sb{{kb[0], kb[1]}, {ib[0], ib[1]}};
-    k_qs_small<<<ns, SORT_T, sm, st>>>(d_segs, ns, sb, fk, fi, d_err);
+    { KTimer kt(KC_SORT, st, 16.0 * np);
+    k_qs_small<<<ns, SORT_T, sm, st>>>(d_segs, ns, sb, fk, fi, d_err); }
     count_launch(1);
     EXH_CUDA_TRY(cudaGetLastError());
     int herr = 0;
@@ -736,7 +740,8 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   GrowArgs A{delta, h->key, h->id, np, (int)nproc, hs, Btab_dev, t};
   const unsigned nb = exh_div_up(nproc, 128);
   if (c.verbose) { printf("  %lld peaks above the barrier\n", (long long)nproc); fflush(stdout); }
-  k_gfree<<<nb, 128, 0, st>>>(A, h->gfree);
+  { KTimer kt(KC_GROW, st, 0.0);
+  k_gfree<<<nb, 128, 0, st>>>(A, h->gfree); }
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   // device counters: [0] pending this round, [1] error
@@ -747,6 +752,7 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
     const int tag = (round % 255) + 1;
     if (round > 0 && tag == 1) EXH_CUDA_TRY(cudaMemsetAsync(h->resv, 0, sizeof(unsigned) * ng, st));
     EXH_CUDA_TRY(cudaMemsetAsync(dcnt, 0, sizeof(int) * 2, st));
+    KTimer kt(KC_GROW, st, 0.0);
     k_reserve<<<nb, 128, 0, st>>>(A, h->gfree, h->state, h->flag, h->resv, tag, h->cnt, dcnt);
     k_commit<<<nb, 128, 0, st>>>(A, h->gfree, h->state, h->flag, h->resv, tag, h->cnt, h->gfin, dcnt + 1);
     count_launch(2);
@@ -963,8 +969,9 @@ int halo_masses(Ctx& c, const BoxParams& b, const HaloDev& h, const HostTables& 
   HaloScalars hs{};
   hs.n0 = b.nd[0]; hs.n1 = b.nd[1]; hs.n2 = b.nd[2];
   const int64_t nchunk = (h.nh + MASS_CHUNK - 1) / MASS_CHUNK;
+  { KTimer kt(KC_MASS, st, 0.0);
   k_masses<<<exh_div_up(nchunk, 128), 128, 0, st>>>(dJ, dI, dInv, h.hpeak, h.cnt, h.id, h.np, dsph, (int)sph.size(),
-                                                   tab.Ncells, b.Mcell, h.nh, hs, Mh_dev, count_dev, xc_dev, derr);
+                                                   tab.Ncells, b.Mcell, h.nh, hs, Mh_dev, count_dev, xc_dev, derr); }
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   int herr = 0;

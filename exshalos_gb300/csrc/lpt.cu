@@ -38,6 +38,7 @@ struct KGrid {
 
 // x-pass source of the first-order potential
 struct Lpt1Gen {
+  static constexpr int io_bytes = 0;
   FieldModes m;
   KGrid g;
   __device__ __forceinline__ float2 operator()(int, int e, int inner) const {
@@ -251,12 +252,14 @@ int lpt_run(Ctx& c, const BoxParams& b, const FieldModes& modes, float k_smooth,
   KGrid g{b.nd[0], b.nd[1], b.nd[2], b.kl[0], b.kl[1], b.kl[2], k_smooth};
   EXH_CUDA_TRY(fft_c2r_3d(*p, Lpt1Gen{modes, g}, work, RealPairStore{phi1, b.nd[2], 1.f}, st));
   const unsigned grid = EXH_NUM_SMS * 16;
-  k_lpt1_disp<<<grid, 256, 0, st>>>(phi1, b.nd[0], b.nd[1], b.nd[2], (float)(b.Normx / (60.0 * b.Lc)), S);
+  { KTimer kt(KC_LPT_STENCIL, st, 16.0 * b.ng);
+  k_lpt1_disp<<<grid, 256, 0, st>>>(phi1, b.nd[0], b.nd[1], b.nd[2], (float)(b.Normx / (60.0 * b.Lc)), S); }
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   if (!do2) return EXH_OK;
   float* src = phi2;   // the source is transformed, then phi2 overwrites it
-  k_lpt2_source<<<grid, 256, 0, st>>>(S, b.nd[0], b.nd[1], b.nd[2], (float)(1.0 / (60.0 * b.Lc)), src);
+  { KTimer kt(KC_LPT_STENCIL, st, 16.0 * b.ng);
+  k_lpt2_source<<<grid, 256, 0, st>>>(S, b.nd[0], b.nd[1], b.nd[2], (float)(1.0 / (60.0 * b.Lc)), src); }
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   const size_t rows = (size_t)b.nd[0] * b.nd[1];
@@ -266,7 +269,8 @@ int lpt_run(Ctx& c, const BoxParams& b, const FieldModes& modes, float k_smooth,
   const int inner = b.nd[1] * p->nc;
   const size_t sm = smem_strided(b.nd[0]);
   EXH_CUDA_TRY(set_smem(k_fft_x_poisson, sm));
-  k_fft_x_poisson<<<exh_div_up(inner, FFT_W), FFT_THREADS, sm, st>>>(work, p->px, p->twx, inner, g, b.Normk);
+  { KTimer kt(KC_FFT_STRIDED, st, 16.0 * b.nd[0] * inner);
+  k_fft_x_poisson<<<exh_div_up(inner, FFT_W), FFT_THREADS, sm, st>>>(work, p->px, p->twx, inner, g, b.Normk); }
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   EXH_CUDA_TRY(launch_strided(CplxLoad{work, b.nd[1], p->nc}, CplxStore{work, b.nd[1], p->nc}, p->py, p->twy, 1.f,
@@ -296,6 +300,7 @@ int halo_displacements(Ctx& c, const BoxParams& b, const HaloDev& h, const Shell
   (void)c;
   if (h.nh == 0) return EXH_OK;
   const int64_t threads = h.nh * 32;
+  KTimer kt(KC_HALO_DISP, st, 0.0);
   k_halo_disp<<<exh_div_up(threads, 256), 256, 0, st>>>(h.hpeak, h.gfin, h.id, h.np, h.nh, t.off_all, t.start_all, S,
                                                         phi2, b.nd[0], b.nd[1], b.nd[2], lpt2_factor(b), o);
   count_launch(1);

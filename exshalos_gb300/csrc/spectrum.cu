@@ -66,13 +66,15 @@ int cic_assign(Ctx& c, const float* pos_dev, int64_t np, int nd, float L, float*
   EXH_CUDA_TRY(cudaMemsetAsync(grid_dev, 0, sizeof(float) * ng, st));
   const float Ld = L / (float)nd;
   if (np > 0) {
+    KTimer kt(KC_CIC, st, 12.0 * np + 32.0 * np);
     k_cic<<<exh_div_up(np, 256), 256, 0, st>>>(pos_dev, np, nd, L, Ld, grid_dev);
     count_launch(1);
     EXH_CUDA_TRY(cudaGetLastError());
   }
   // np == 0 gives 0/0 in the reference; the grid is returned as -1 + nan there.
   const float inv_mean = np > 0 ? (float)((double)ng / (double)np) : NAN;
-  k_cic_normalise<<<EXH_NUM_SMS * 8, 256, 0, st>>>(grid_dev, ng, inv_mean);
+  { KTimer kt(KC_CIC, st, 8.0 * ng);
+  k_cic_normalise<<<EXH_NUM_SMS * 8, 256, 0, st>>>(grid_dev, ng, inv_mean); }
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   return EXH_OK;
@@ -201,7 +203,8 @@ int power_spectrum(Ctx& c, const float* grid_dev, int nd, float L, int window, i
   unsigned* partN = reinterpret_cast<unsigned*>(partK + (size_t)nblk * Nk);
   const size_t sm = smem_strided(nd) + (size_t)Nk * (2 * sizeof(double) + sizeof(unsigned)) + 16;
   EXH_CUDA_TRY(set_smem(k_fft_x_bin, sm));
-  k_fft_x_bin<<<nblk, FFT_THREADS, sm, st>>>(work, p->px, p->twx, nd, p->nc, bp, partP, partK, partN);
+  { KTimer kt(KC_BIN, st, 8.0 * nd * inner);
+  k_fft_x_bin<<<nblk, FFT_THREADS, sm, st>>>(work, p->px, p->twx, nd, p->nc, bp, partP, partK, partN); }
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   k_bin_reduce<<<Nk, 256, 0, st>>>(partP, partK, partN, nblk, Nk, outP_dev, outK_dev, outN_dev);

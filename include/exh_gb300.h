@@ -138,9 +138,18 @@ int exh_density_grid_compute(exh_ctx *ctx, const float *k, const float *P, int N
 int exh_fft_r2c_3d(exh_ctx *ctx, int nx, int ny, int nz, const float *in, float *out, void *stream);
 int exh_fft_c2r_3d(exh_ctx *ctx, int nx, int ny, int nz, float *in, float *out, void *stream);
 
-/* Number of kernels launched by this context since creation (counted on the
- * host at each launch). */
+/* Number of kernels launched by this library in the process (counted on the
+ * host at each launch; the context argument may be NULL). */
 int64_t exh_launch_count(exh_ctx *ctx);
+
+/* Kernel-class timing with CUDA events on the launching streams (no
+ * reference counterpart; the reference only prints progress lines).
+ * exh_timing_enable(1) clears and starts recording, (0) stops.
+ * exh_timing_report fills, per class (FFT strided pass, FFT row pass,
+ * peaks, sort, growth, masses, LPT stencils, halo sums, CIC, P(k) binning,
+ * other), total milliseconds, launches and algorithmic bytes. */
+int exh_timing_enable(int on);
+int exh_timing_report(int n, double *ms, int64_t *launches, double *bytes);
 
 #ifdef __cplusplus
 }
