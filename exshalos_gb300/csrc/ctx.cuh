@@ -62,7 +62,8 @@ enum BufId {
   B_PHI1,         // first-order potential (float)
   B_PHI2,         // second-order potential (float)
   B_S,            // displacements [3][ng]
-  B_V,            // velocities [3][ng]
+  B_V,            // particle positions / velocities [ng][3]
+  B_VEL,          // velocity planes [3][ng]
   B_FLAG,         // int32 halo flag per cell
   B_PEAKS,        // peak keys/ids (sort ping-pong)
   B_PEAKS2,

@@ -191,7 +191,7 @@ int find_peaks(Ctx& c, const float* delta, const BoxParams& b, HaloDev* h, cudaS
 }
 
 // ------------------------------------------------------------------ sort
-constexpr int SORT_SMALL = 4096;     // segment size finished inside one block
+constexpr int SORT_SMALL = 2048;     // segment size finished inside one block
 constexpr int SORT_T = 512;
 constexpr int CH_T = 256, CH_ITEMS = 8, CH = CH_T * CH_ITEMS;
 
@@ -202,17 +202,13 @@ struct Seg {
 };
 
 // Final position (relative) of the > element at relative position a.
-// lam: nondecreasing L-counts before each > element (m of them).
-template <typename LamT>
-__device__ __forceinline__ int lomuto_g_dest(int a, int nL, int m, LamT lam) {
+// lam(q): number of <= elements before the q-th > element (nondecreasing);
+// posl(r): relative position of the <= element of rank r, so that
+// g(a) = posl(a) - a is the number of > elements before it.
+template <typename LamT, typename PosT>
+__device__ __forceinline__ int lomuto_g_dest(int a, int nL, int m, LamT lam, PosT posl) {
   while (a < nL) {
-    int lo = 0, hi = m;
-    while (lo < hi) {
-      const int mid = (lo + hi) >> 1;
-      if (lam(mid) <= a) lo = mid + 1;
-      else hi = mid;
-    }
-    const int c = lo;                              // >= 1 for consistent input
+    const int c = posl(a) - a;                     // >= 1 for consistent input
     if (c <= 0) return nL;                         // never loop on inconsistent input
     const int bnd = c < m ? min(lam(c), nL) : nL;
     const int steps = (bnd - a + c - 1) / c;
@@ -264,6 +260,7 @@ template <int PHASE>
 __global__ void k_qs_place(const float* __restrict__ key, const unsigned* __restrict__ id, const Seg* __restrict__ segs,
                            const int* __restrict__ cseg, const int* __restrict__ coff, int nchunks,
                            const int* __restrict__ cLoff, const int* __restrict__ segNL, int* __restrict__ lam,
+                           int* __restrict__ posl,
                            float* __restrict__ okey, unsigned* __restrict__ oid, float* __restrict__ fkey,
                            unsigned* __restrict__ fid) {
   const int ch = blockIdx.x;
@@ -294,6 +291,7 @@ __global__ void k_qs_place(const float* __restrict__ key, const unsigned* __rest
       if (PHASE == 1) {
         okey[s.lo + rank] = key[p];
         oid[s.lo + rank] = id[p];
+        posl[s.lo + rank] = p - s.lo;
       }
       rank++;
     } else {
@@ -302,7 +300,9 @@ __global__ void k_qs_place(const float* __restrict__ key, const unsigned* __rest
         lam[s.lo + (rel - rank)] = rank;
       } else {
         const int* lseg = lam + s.lo;
-        int a = lomuto_g_dest(rel, nL, m, [lseg](int i) { return __ldg(&lseg[i]); });
+        const int* pseg = posl + s.lo;
+        int a = lomuto_g_dest(rel, nL, m, [lseg](int i) { return __ldg(&lseg[i]); },
+                              [pseg](int i) { return __ldg(&pseg[i]); });
         const int dest = (a == nL) ? (s.hi - s.lo) : a;
         okey[s.lo + dest] = key[p];
         oid[s.lo + dest] = id[p];
@@ -338,7 +338,7 @@ struct SmallSortBuffers {
 // sub-segments (Lomuto, computed as in k_qs_place), then the block
 // collects the children for the next level.  No locks and no waits other
 // than block barriers; at most n levels.
-__device__ __forceinline__ void warp_partition(float* ka, unsigned* ia, float* kb, unsigned* ib, int* lam, int lo,
+__device__ __forceinline__ void warp_partition(float* ka, unsigned* ia, float* kb, unsigned* ib, int* lam, int* posl, int lo,
                                                int hi, int lane, int& nL_out) {
   const float pv = ka[hi];
   const int s = hi - lo + 1;
@@ -349,7 +349,7 @@ __device__ __forceinline__ void warp_partition(float* ka, unsigned* ia, float* k
     const unsigned msk = __ballot_sync(0xffffffffu, L);
     const int r = run + __popc(msk & ((1u << lane) - 1u));
     if (p < hi) {
-      if (L) { kb[lo + r] = ka[p]; ib[lo + r] = ia[p]; }
+      if (L) { kb[lo + r] = ka[p]; ib[lo + r] = ia[p]; posl[lo + r] = p - lo; }
       else lam[lo + (p - lo - r)] = r;
     }
     run += __popc(msk);
@@ -360,7 +360,8 @@ __device__ __forceinline__ void warp_partition(float* ka, unsigned* ia, float* k
     const int p = b0 + lane;
     if (p < hi && !(ka[p] <= pv)) {
       const int* ls = lam + lo;
-      const int a = lomuto_g_dest(p - lo, nL, m, [ls](int i) { return ls[i]; });
+      const int* ps = posl + lo;
+      const int a = lomuto_g_dest(p - lo, nL, m, [ls](int i) { return ls[i]; }, [ps](int i) { return ps[i]; });
       const int dest = (a == nL) ? (s - 1) : a;
       kb[lo + dest] = ka[p];
       ib[lo + dest] = ia[p];
@@ -382,7 +383,8 @@ k_qs_small(const Seg* __restrict__ segs, int nseg, SmallSortBuffers bufs, float*
   float* kb = reinterpret_cast<float*>(ia + SORT_SMALL);
   unsigned* ib = reinterpret_cast<unsigned*>(kb + SORT_SMALL);
   int* lam = reinterpret_cast<int*>(ib + SORT_SMALL);
-  int* cur = lam + SORT_SMALL;              // pending (lo, hi) pairs of this level
+  int* posl = lam + SORT_SMALL;
+  int* cur = posl + SORT_SMALL;             // pending (lo, hi) pairs of this level
   int* nxt = cur + SORT_SMALL;              // two child slots per pending segment
   __shared__ int ncur;
   if (blockIdx.x >= nseg) return;
@@ -402,7 +404,7 @@ k_qs_small(const Seg* __restrict__ segs, int nseg, SmallSortBuffers bufs, float*
     for (int q = w; q < nc; q += nw) {
       const int lo = cur[2 * q], hi = cur[2 * q + 1];
       int nL;
-      warp_partition(ka, ia, kb, ib, lam, lo, hi, lane, nL);
+      warp_partition(ka, ia, kb, ib, lam, posl, lo, hi, lane, nL);
       if (lane == 0) {
         const int m = hi - lo - nL;
         nxt[4 * q + 0] = nL >= 2 ? lo : -1;
@@ -432,10 +434,11 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
   unsigned* i1 = reinterpret_cast<unsigned*>(k1 + cap);
   float* fk = reinterpret_cast<float*>(i1 + cap);
   // final arrays live in B_PEAKS2
-  EXH_TRY(c.buf[B_PEAKS2].ensure((sizeof(float) + sizeof(unsigned)) * cap + sizeof(int) * cap));
+  EXH_TRY(c.buf[B_PEAKS2].ensure((sizeof(float) + sizeof(unsigned)) * cap + 2 * sizeof(int) * cap));
   fk = c.buf[B_PEAKS2].as<float>();
   unsigned* fi = reinterpret_cast<unsigned*>(fk + cap);
   int* lam = reinterpret_cast<int*>(fi + cap);
+  int* posl = lam + cap;
   if (np <= 1) {
     if (np == 1) {
       EXH_CUDA_TRY(cudaMemcpyAsync(fk, k0, sizeof(float), cudaMemcpyDeviceToDevice, st));
@@ -480,9 +483,9 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
     KTimer kt(KC_SORT, st, 0.0);
     k_qs_count<<<nch, CH_T, 0, st>>>(kb[buf], d_segs, d_cseg, d_coff, nch, d_cL);
     k_qs_seg_scan<<<nseg, 256, 0, st>>>(d_cfirst, nseg, d_cL, d_nl);
-    k_qs_place<1><<<nch, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, nch, d_cL, d_nl, lam,
+    k_qs_place<1><<<nch, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, nch, d_cL, d_nl, lam, posl,
                                         kb[buf ^ 1], ib[buf ^ 1], fk, fi);
-    k_qs_place<2><<<nch, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, nch, d_cL, d_nl, lam,
+    k_qs_place<2><<<nch, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, nch, d_cL, d_nl, lam, posl,
                                         kb[buf ^ 1], ib[buf ^ 1], fk, fi);
     count_launch(4);
     EXH_CUDA_TRY(cudaGetLastError());
@@ -528,7 +531,7 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
     EXH_TRY(c.buf[B_HOSTIO2].ensure(64));
     int* d_err = c.buf[B_HOSTIO2].as<int>();
     EXH_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
-    const size_t sm = (size_t)SORT_SMALL * (4 * 4 + 4) + sizeof(int) * 3 * (size_t)SORT_SMALL;
+    const size_t sm = (size_t)SORT_SMALL * (4 * 4 + 2 * 4) + sizeof(int) * 3 * (size_t)SORT_SMALL;
     EXH_CUDA_TRY(set_smem(k_qs_small, sm));
     SmallSortBuffers sb{{kb[0], kb[1]}, {ib[0], ib[1]}};
     { KTimer kt(KC_SORT, st, 16.0 * np);
@@ -572,10 +575,14 @@ __device__ __forceinline__ void peak_coords(unsigned cell, const HaloScalars& hs
   x = (int)(r / hs.n1);
 }
 
-// growth + shrink of find_halos.c:274-337.  flag == nullptr: exclusion-free.
-// Returns 0 ok, 1 count beyond the sigma table, 2 shell beyond the tables.
-__device__ int grow_one(const GrowArgs& A, const int* __restrict__ flag, int x0, int y0, int z0, float pden,
-                        int& count_out, int& gtmp_out) {
+// Growth + shrink of find_halos.c:274-337 by one warp.  Lanes gather the
+// cells of a shell 32 at a time; every lane then adds the gathered values to
+// its running mean in shell order (shuffles), so all lanes hold the same
+// double values the reference's sequential loop produces.
+// flag == nullptr: exclusion-free.  Returns 0 ok, 1 count beyond the sigma
+// table, 2 shell beyond the tables.
+__device__ int grow_warp(const GrowArgs& A, const int* __restrict__ flag, int x0, int y0, int z0, float pden,
+                         int lane, int& count_out, int& gtmp_out) {
   const HaloScalars& hs = A.hs;
   double den = (double)pden, den_tmp = (double)pden;
   int count = 0, count_tmp = 1, grows_tmp = 0, grows = 0;
@@ -589,11 +596,16 @@ __device__ int grow_one(const GrowArgs& A, const int* __restrict__ flag, int x0,
     if (grows_tmp > A.t.gmax) { count_out = count; gtmp_out = grows_tmp; return 2; }
     den_tmp = __dmul_rn(den, (double)count);
     const int s0 = A.t.start_cap[grows_tmp], s1 = A.t.start_cap[grows_tmp + 1];
-    for (int q = s0; q < s1; q++) {
-      const size_t cell = cell_at(x0, y0, z0, A.t.off_cap[q], hs);
-      const double v = (flag && flag[cell] != FLAG_FREE) ? mneg : (double)A.delta[cell];
-      den_tmp = __dadd_rn(den_tmp, v);
-      count_tmp++;
+    for (int base = s0; base < s1; base += 32) {
+      const int q = base + lane;
+      double v = 0.0;
+      if (q < s1) {
+        const size_t cell = cell_at(x0, y0, z0, A.t.off_cap[q], hs);
+        v = (flag && flag[cell] != FLAG_FREE) ? mneg : (double)A.delta[cell];
+      }
+      const int n = min(32, s1 - base);
+      for (int j = 0; j < n; j++) den_tmp = __dadd_rn(den_tmp, __shfl_sync(0xffffffffu, v, j));
+      count_tmp += n;
     }
     den_tmp = __ddiv_rn(den_tmp, (double)count_tmp);
   }
@@ -602,9 +614,13 @@ __device__ int grow_one(const GrowArgs& A, const int* __restrict__ flag, int x0,
     count_tmp = count;
     den = __dmul_rn(den, (double)count);
     const int s0 = A.t.start_cap[grows], s1 = A.t.start_cap[grows + 1];
-    for (int q = s0; q < s1; q++) {
-      den = __dsub_rn(den, (double)A.delta[cell_at(x0, y0, z0, A.t.off_cap[q], hs)]);
-      count--;
+    for (int base = s0; base < s1; base += 32) {
+      const int q = base + lane;
+      double v = 0.0;
+      if (q < s1) v = (double)A.delta[cell_at(x0, y0, z0, A.t.off_cap[q], hs)];
+      const int n = min(32, s1 - base);
+      for (int j = 0; j < n; j++) den = __dsub_rn(den, __shfl_sync(0xffffffffu, v, j));
+      count -= n;
     }
     if (count > 0) den = __ddiv_rn(den, (double)count);
     if (count < count_tmp) grows_tmp = grows;
@@ -615,44 +631,49 @@ __device__ int grow_one(const GrowArgs& A, const int* __restrict__ flag, int x0,
   return 0;
 }
 
-__global__ void k_gfree(GrowArgs A, int* __restrict__ gfree) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+constexpr int GROW_T = 256;   // 8 peaks (one per warp) per block
+
+__global__ void __launch_bounds__(GROW_T) k_gfree(GrowArgs A, int* __restrict__ gfree) {
+  const int r = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (r >= A.nproc) return;
   const int64_t l = A.np - 1 - r;
   int x, y, z;
   peak_coords(A.id[l], A.hs, x, y, z);
   int cnt, gt;
-  const int st = grow_one(A, nullptr, x, y, z, A.key[l], cnt, gt);
+  const int st = grow_warp(A, nullptr, x, y, z, A.key[l], lane, cnt, gt);
   // growth with exclusion reads at most the shells this one reads
-  gfree[r] = st ? A.t.gmax : min(gt, A.t.gmax);
+  if (lane == 0) gfree[r] = st ? A.t.gmax : min(gt, A.t.gmax);
 }
 
 __device__ __forceinline__ unsigned resv_key(int tag, int r) { return ((unsigned)tag << 24) | (0xFFFFFFu - (unsigned)r); }
 
-__global__ void k_reserve(GrowArgs A, const int* __restrict__ gfree, unsigned char* __restrict__ state,
-                          const int* __restrict__ flag, unsigned* __restrict__ resv, int tag, int* __restrict__ cnt,
-                          int* __restrict__ npend) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(GROW_T)
+k_reserve(GrowArgs A, const int* __restrict__ gfree, unsigned char* __restrict__ state, const int* __restrict__ flag,
+          unsigned* __restrict__ resv, int tag, int* __restrict__ cnt, int* __restrict__ npend) {
+  const int r = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (r >= A.nproc || state[r]) return;
   const int64_t l = A.np - 1 - r;
   const unsigned cell0 = A.id[l];
   if (flag[cell0] != FLAG_FREE) {        // find_halos.c:233: the peak is already inside a halo
-    state[r] = 1;
-    cnt[r] = 0;
+    if (lane == 0) { state[r] = 1; cnt[r] = 0; }
     return;
   }
-  atomicAdd(npend, 1);
+  if (lane == 0) atomicAdd(npend, 1);
   int x, y, z;
   peak_coords(cell0, A.hs, x, y, z);
   const unsigned key = resv_key(tag, r);
   const int e = A.t.start_all[gfree[r] + 1];
-  for (int q = 0; q < e; q++) atomicMax(&resv[cell_at(x, y, z, A.t.off_all[q], A.hs)], key);
+  for (int q = lane; q < e; q += 32) atomicMax(&resv[cell_at(x, y, z, A.t.off_all[q], A.hs)], key);
 }
 
-__global__ void k_commit(GrowArgs A, const int* __restrict__ gfree, unsigned char* __restrict__ state,
-                         int* __restrict__ flag, const unsigned* __restrict__ resv, int tag, int* __restrict__ cnt,
-                         int* __restrict__ gfin, int* __restrict__ err) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(GROW_T)
+k_commit(GrowArgs A, const int* __restrict__ gfree, unsigned char* __restrict__ state, int* __restrict__ flag,
+         const unsigned* __restrict__ resv, int tag, int* __restrict__ cnt, int* __restrict__ gfin,
+         int* __restrict__ err) {
+  const int r = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (r >= A.nproc || state[r]) return;
   const int64_t l = A.np - 1 - r;
   const unsigned cell0 = A.id[l];
@@ -660,18 +681,21 @@ __global__ void k_commit(GrowArgs A, const int* __restrict__ gfree, unsigned cha
   peak_coords(cell0, A.hs, x, y, z);
   const unsigned key = resv_key(tag, r);
   const int e = A.t.start_all[gfree[r] + 1];
-  for (int q = 0; q < e; q++)
-    if (resv[cell_at(x, y, z, A.t.off_all[q], A.hs)] != key) return;
+  bool mine = true;
+  for (int q = lane; q < e && mine; q += 32) mine = resv[cell_at(x, y, z, A.t.off_all[q], A.hs)] == key;
+  if (!__all_sync(0xffffffffu, mine)) return;
   int count, gt;
-  const int st = grow_one(A, flag, x, y, z, A.key[l], count, gt);
-  if (st) { atomicMax(err, st); state[r] = 1; cnt[r] = 0; return; }
-  state[r] = 1;
-  cnt[r] = count;
-  gfin[r] = gt;
+  const int st = grow_warp(A, flag, x, y, z, A.key[l], lane, count, gt);
+  if (st) {
+    if (lane == 0) { atomicMax(err, st); state[r] = 1; cnt[r] = 0; }
+    return;
+  }
+  if (lane == 0) { state[r] = 1; cnt[r] = count; gfin[r] = gt; }
   if (count == 0) return;                 // find_halos.c:339-340
   const int we = A.t.start_all[gt];       // cells with r^2 < grows_tmp
-  for (int q = 0; q < we; q++) flag[cell_at(x, y, z, A.t.off_all[q], A.hs)] = r;
-  flag[cell0] = -(r + 2);
+  for (int q = lane; q < we; q += 32) flag[cell_at(x, y, z, A.t.off_all[q], A.hs)] = r;
+  __syncwarp();
+  if (lane == 0) flag[cell0] = -(r + 2);
 }
 
 __global__ void k_kept(const int* __restrict__ cnt, const unsigned char* __restrict__ state, int nproc, int Nmin,
@@ -739,9 +763,10 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   if (nproc == 0) return EXH_OK;
   GrowArgs A{delta, h->key, h->id, np, (int)nproc, hs, Btab_dev, t};
   const unsigned nb = exh_div_up(nproc, 128);
+  const unsigned nbw = exh_div_up((size_t)nproc * 32, GROW_T);
   if (c.verbose) { printf("  %lld peaks above the barrier\n", (long long)nproc); fflush(stdout); }
   { KTimer kt(KC_GROW, st, 0.0);
-  k_gfree<<<nb, 128, 0, st>>>(A, h->gfree); }
+  k_gfree<<<nbw, GROW_T, 0, st>>>(A, h->gfree); }
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   // device counters: [0] pending this round, [1] error
@@ -753,8 +778,8 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
     if (round > 0 && tag == 1) EXH_CUDA_TRY(cudaMemsetAsync(h->resv, 0, sizeof(unsigned) * ng, st));
     EXH_CUDA_TRY(cudaMemsetAsync(dcnt, 0, sizeof(int) * 2, st));
     KTimer kt(KC_GROW, st, 0.0);
-    k_reserve<<<nb, 128, 0, st>>>(A, h->gfree, h->state, h->flag, h->resv, tag, h->cnt, dcnt);
-    k_commit<<<nb, 128, 0, st>>>(A, h->gfree, h->state, h->flag, h->resv, tag, h->cnt, h->gfin, dcnt + 1);
+    k_reserve<<<nbw, GROW_T, 0, st>>>(A, h->gfree, h->state, h->flag, h->resv, tag, h->cnt, dcnt);
+    k_commit<<<nbw, GROW_T, 0, st>>>(A, h->gfree, h->state, h->flag, h->resv, tag, h->cnt, h->gfin, dcnt + 1);
     count_launch(2);
     EXH_CUDA_TRY(cudaGetLastError());
     int hc[2];

@@ -53,71 +53,97 @@ struct Lpt1Gen {
 };
 
 // ---------------------------------------------------------------- stencils
-__device__ __forceinline__ double d6(const float* __restrict__ f, size_t c, size_t sp1, size_t sp2, size_t sp3,
-                                     size_t sm1, size_t sm2, size_t sm3) {
-  return 1.0 * f[sp3] - 9.0 * f[sp2] + 45.0 * f[sp1] - 45.0 * f[sm1] + 9.0 * f[sm2] - 1.0 * f[sm3];
+// Sixth-order central differences (1, -9, 45, 0, -45, 9, -1) / 60 of
+// lpt.c:64-68 on shared-memory bricks with a 3-cell periodic halo; the
+// differences of opposite neighbours are formed first, which keeps float
+// accuracy on smooth fields.
+constexpr int BZ = 32, BY = 8;
+constexpr int GX = 16;            // bricks of 16 x 8 x 32 cells for gradients
+constexpr int SX = 8;             // bricks of 8 x 8 x 32 cells for the 2LPT source
+constexpr int H = 3;
+
+__device__ __forceinline__ float d6f(float p1, float p2, float p3, float m1, float m2, float m3) {
+  return (p3 - m3) - 9.f * (p2 - m2) + 45.f * (p1 - m1);
 }
 
-struct Nb {
-  size_t p1, p2, p3, m1, m2, m3;
-};
-__device__ __forceinline__ Nb nb_axis(int i, int j, int k, int axis, int n0, int n1, int n2) {
-  int c[3] = {i, j, k};
-  const int n[3] = {n0, n1, n2};
-  Nb r;
-  size_t* out[6] = {&r.p1, &r.p2, &r.p3, &r.m1, &r.m2, &r.m3};
-  const int off[6] = {1, 2, 3, -1, -2, -3};
-#pragma unroll
-  for (int t = 0; t < 6; t++) {
-    int cc[3] = {c[0], c[1], c[2]};
-    cc[axis] = exh_wrap(c[axis], off[t], n[axis]);
-    *out[t] = ((size_t)cc[0] * n1 + cc[1]) * n2 + cc[2];
-  }
-  return r;
-}
-
-__device__ __forceinline__ double grad6(const float* __restrict__ f, int i, int j, int k, int axis, int n0, int n1,
-                                        int n2) {
-  const Nb b = nb_axis(i, j, k, axis, n0, n1, n2);
-  return d6(f, 0, b.p1, b.p2, b.p3, b.m1, b.m2, b.m3);
-}
-
-// S1 for every cell, planes S[a * ng + cell]
-__global__ void k_lpt1_disp(const float* __restrict__ phi, int n0, int n1, int n2, float fac, float* __restrict__ S) {
-  const size_t ng = (size_t)n0 * n1 * n2;
-  size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (; c < ng; c += stride) {
-    const int k = (int)(c % n2);
-    const size_t r = c / n2;
-    const int j = (int)(r % n1), i = (int)(r / n1);
-#pragma unroll
-    for (int a = 0; a < 3; a++) S[a * ng + c] = (float)(-grad6(phi, i, j, k, a, n0, n1, n2) * (double)fac);
+// load a (ex) x (ey) x (ez) tile whose origin is (x0 - hx, y0 - hy, z0 - hz)
+__device__ __forceinline__ void load_tile(const float* __restrict__ f, float* t, int ex, int ey, int ez, int x0, int y0,
+                                          int z0, int hx, int hy, int hz, int n0, int n1, int n2) {
+  const int tot = ex * ey * ez, tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
+  for (int q = tid; q < tot; q += nt) {
+    const int dz = q % ez, r = q / ez, dy = r % ey, dx = r / ey;
+    const int gx = exh_wrap(x0 - hx, dx, n0), gy = exh_wrap(y0 - hy, dy, n1), gz = exh_wrap(z0 - hz, dz, n2);
+    t[q] = f[((size_t)gx * n1 + gy) * n2 + gz];
   }
 }
 
-// second-order source (lpt.c:116-134)
-__global__ void k_lpt2_source(const float* __restrict__ S, int n0, int n1, int n2, float inv60lc,
-                              float* __restrict__ src) {
+// S[a] (=|+=) fac * D6_a(phi); V[a] (=|+=) fv * fac * D6_a(phi) when V
+template <bool ADD>
+__global__ void __launch_bounds__(256)
+k_brick_grad(const float* __restrict__ phi, int n0, int n1, int n2, float fac, float fv, float* __restrict__ S,
+             float* __restrict__ V) {
+  extern __shared__ float tile[];
+  constexpr int EY = BY + 2 * H, EZ = BZ + 2 * H;
+  const int z0 = blockIdx.x * BZ, y0 = blockIdx.y * BY, x0 = blockIdx.z * GX;
+  load_tile(phi, tile, GX + 2 * H, EY, EZ, x0, y0, z0, H, H, H, n0, n1, n2);
+  __syncthreads();
+  const int tz = threadIdx.x, ty = threadIdx.y;
+  const int gz = z0 + tz, gy = y0 + ty;
+  if (gz >= n2 || gy >= n1) return;
   const size_t ng = (size_t)n0 * n1 * n2;
-  size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  const float* Sx = S;
-  const float* Sy = S + ng;
-  const float* Sz = S + 2 * ng;
-  for (; c < ng; c += stride) {
-    const int k = (int)(c % n2);
-    const size_t r = c / n2;
-    const int j = (int)(r % n1), i = (int)(r / n1);
-    const double l = (double)inv60lc;
-    const float pxx = (float)(grad6(Sx, i, j, k, 0, n0, n1, n2) * l);
-    const float pxy = (float)(grad6(Sx, i, j, k, 1, n0, n1, n2) * l);
-    const float pxz = (float)(grad6(Sx, i, j, k, 2, n0, n1, n2) * l);
-    const float pyy = (float)(grad6(Sy, i, j, k, 1, n0, n1, n2) * l);
-    const float pyz = (float)(grad6(Sy, i, j, k, 2, n0, n1, n2) * l);
-    const float pzz = (float)(grad6(Sz, i, j, k, 2, n0, n1, n2) * l);
-    src[c] = (float)((double)(pxx * pyy + pxx * pzz + pyy * pzz) - (double)pxy * pxy - (double)pxz * pxz -
-                     (double)pyz * pyz);
+  for (int xx = 0; xx < GX && x0 + xx < n0; xx++) {
+    const int cx = xx + H, cy = ty + H, cz = tz + H;
+#define T(a, b, c) tile[((a) * EY + (b)) * EZ + (c)]
+    const float g[3] = {
+        d6f(T(cx + 1, cy, cz), T(cx + 2, cy, cz), T(cx + 3, cy, cz), T(cx - 1, cy, cz), T(cx - 2, cy, cz), T(cx - 3, cy, cz)),
+        d6f(T(cx, cy + 1, cz), T(cx, cy + 2, cz), T(cx, cy + 3, cz), T(cx, cy - 1, cz), T(cx, cy - 2, cz), T(cx, cy - 3, cz)),
+        d6f(T(cx, cy, cz + 1), T(cx, cy, cz + 2), T(cx, cy, cz + 3), T(cx, cy, cz - 1), T(cx, cy, cz - 2), T(cx, cy, cz - 3))};
+#undef T
+    const size_t c = ((size_t)(x0 + xx) * n1 + gy) * n2 + gz;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      const float s = g[a] * fac;
+      if (ADD) S[a * ng + c] += s; else S[a * ng + c] = s;
+      if (V) { if (ADD) V[a * ng + c] += fv * s; else V[a * ng + c] = fv * s; }
+    }
+  }
+}
+
+// second-order source (lpt.c:116-134) from the first-order displacement
+__global__ void __launch_bounds__(256)
+k_brick_source(const float* __restrict__ S, int n0, int n1, int n2, float inv60lc, float* __restrict__ src) {
+  extern __shared__ float sm[];
+  constexpr int EY = BY + 2 * H, EZ = BZ + 2 * H;
+  float* tx = sm;                                  // Sx: halo in x, y, z
+  float* ty_ = tx + (SX + 2 * H) * EY * EZ;         // Sy: halo in y, z
+  float* tz_ = ty_ + SX * EY * EZ;                  // Sz: halo in z
+  const size_t ng = (size_t)n0 * n1 * n2;
+  const int z0 = blockIdx.x * BZ, y0 = blockIdx.y * BY, x0 = blockIdx.z * SX;
+  load_tile(S, tx, SX + 2 * H, EY, EZ, x0, y0, z0, H, H, H, n0, n1, n2);
+  load_tile(S + ng, ty_, SX, EY, EZ, x0, y0, z0, 0, H, H, n0, n1, n2);
+  load_tile(S + 2 * ng, tz_, SX, BY, EZ, x0, y0, z0, 0, 0, H, n0, n1, n2);
+  __syncthreads();
+  const int tzz = threadIdx.x, tyy = threadIdx.y;
+  const int gz = z0 + tzz, gy = y0 + tyy;
+  if (gz >= n2 || gy >= n1) return;
+  for (int xx = 0; xx < SX && x0 + xx < n0; xx++) {
+    const int cz = tzz + H, cy = tyy + H;
+#define AX(a, b, c) tx[((a) * EY + (b)) * EZ + (c)]
+#define AY(a, b, c) ty_[((a) * EY + (b)) * EZ + (c)]
+#define AZ(a, b, c) tz_[((a) * BY + (b)) * EZ + (c)]
+    const int cx = xx + H;
+    const float pxx = inv60lc * d6f(AX(cx + 1, cy, cz), AX(cx + 2, cy, cz), AX(cx + 3, cy, cz), AX(cx - 1, cy, cz), AX(cx - 2, cy, cz), AX(cx - 3, cy, cz));
+    const float pxy = inv60lc * d6f(AX(cx, cy + 1, cz), AX(cx, cy + 2, cz), AX(cx, cy + 3, cz), AX(cx, cy - 1, cz), AX(cx, cy - 2, cz), AX(cx, cy - 3, cz));
+    const float pxz = inv60lc * d6f(AX(cx, cy, cz + 1), AX(cx, cy, cz + 2), AX(cx, cy, cz + 3), AX(cx, cy, cz - 1), AX(cx, cy, cz - 2), AX(cx, cy, cz - 3));
+    const float pyy = inv60lc * d6f(AY(xx, cy + 1, cz), AY(xx, cy + 2, cz), AY(xx, cy + 3, cz), AY(xx, cy - 1, cz), AY(xx, cy - 2, cz), AY(xx, cy - 3, cz));
+    const float pyz = inv60lc * d6f(AY(xx, cy, cz + 1), AY(xx, cy, cz + 2), AY(xx, cy, cz + 3), AY(xx, cy, cz - 1), AY(xx, cy, cz - 2), AY(xx, cy, cz - 3));
+    const float pzz = inv60lc * d6f(AZ(xx, tyy, cz + 1), AZ(xx, tyy, cz + 2), AZ(xx, tyy, cz + 3), AZ(xx, tyy, cz - 1), AZ(xx, tyy, cz - 2), AZ(xx, tyy, cz - 3));
+#undef AX
+#undef AY
+#undef AZ
+    const float diag = pxx * pyy + pxx * pzz + pyy * pzz;
+    src[((size_t)(x0 + xx) * n1 + gy) * n2 + gz] =
+        (float)((double)diag - (double)pxy * pxy - (double)pxz * pxz - (double)pyz * pyz);
   }
 }
 
@@ -163,62 +189,91 @@ k_fft_x_poisson(float2* __restrict__ work, RadixPlan pl, const float2* __restric
 }
 
 // ---------------------------------------------------------------- halos
-// one warp per halo: sum of S1 (+ S2 from D6(phi2)) over member cells
-__global__ void k_halo_disp(const int* __restrict__ hpeak, const int* __restrict__ gfin, const unsigned* __restrict__ pid,
-                            int64_t np, int64_t nh, const int* __restrict__ off_all, const int* __restrict__ start_all,
-                            const float* __restrict__ S, const float* __restrict__ phi2, int n0, int n1, int n2,
-                            float s2fac, HaloOut o) {
-  const int64_t h = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+// Displacement and velocity sums over the member cells of each halo
+// (lpt.c:70-80, 200-210) and the final positions (lpt.c:245-255).  A warp
+// owns 32 consecutive halos: each lane sums its own halo when it has at most
+// 32 cells; larger halos are summed by the whole warp, one after another.
+// The order of every sum is fixed, so the result is deterministic.
+__global__ void __launch_bounds__(256)
+k_halo_sum(const int* __restrict__ hpeak, const int* __restrict__ gfin, const unsigned* __restrict__ pid, int64_t np,
+           int64_t nh, const int* __restrict__ off_all, const int* __restrict__ start_all, const float* __restrict__ S,
+           const float* __restrict__ V, int n0, int n1, int n2, HaloOut o) {
+  const int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
-  if (h >= nh) return;
+  const bool valid = h < nh;
   const size_t ng = (size_t)n0 * n1 * n2;
-  const int r = hpeak[h];
-  const unsigned cell0 = pid[np - 1 - r];
-  const int z0 = (int)(cell0 % n2);
-  const unsigned rr = cell0 / n2;
-  const int y0 = (int)(rr % n1), x0 = (int)(rr / n1);
-  const int e = start_all[gfin[r]];
-  double s1[3] = {0, 0, 0}, s2[3] = {0, 0, 0};
-  for (int q = lane; q < e; q += 32) {
+  int x0 = 0, y0 = 0, z0 = 0, cnt = 0;
+  if (valid) {
+    const int r = hpeak[h];
+    const unsigned cell0 = pid[np - 1 - r];
+    z0 = (int)(cell0 % n2);
+    const unsigned rr = cell0 / n2;
+    y0 = (int)(rr % n1);
+    x0 = (int)(rr / n1);
+    cnt = start_all[gfin[r]];
+  }
+  double s[3] = {0, 0, 0}, v[3] = {0, 0, 0};
+  auto cell_of = [&](int q, int xa, int ya, int za) {
     const int pk = off_all[q];
-    const int i = exh_wrap(x0, (pk & 0xff) - 128, n0), j = exh_wrap(y0, ((pk >> 8) & 0xff) - 128, n1),
-              k = exh_wrap(z0, ((pk >> 16) & 0xff) - 128, n2);
-    const size_t c = ((size_t)i * n1 + j) * n2 + k;
+    const int i = exh_wrap(xa, (pk & 0xff) - 128, n0), j = exh_wrap(ya, ((pk >> 8) & 0xff) - 128, n1),
+              k = exh_wrap(za, ((pk >> 16) & 0xff) - 128, n2);
+    return ((size_t)i * n1 + j) * n2 + k;
+  };
+  const bool small = valid && cnt <= 32;
+  if (small) {
+    for (int q = 0; q < cnt; q++) {
+      const size_t c = cell_of(q, x0, y0, z0);
 #pragma unroll
-    for (int a = 0; a < 3; a++) s1[a] += (double)S[a * ng + c];
-    if (phi2) {
-#pragma unroll
-      for (int a = 0; a < 3; a++) s2[a] += (double)(float)(grad6(phi2, i, j, k, a, n0, n1, n2) * (double)s2fac);
+      for (int a = 0; a < 3; a++) {
+        s[a] += (double)S[a * ng + c];
+        if (V) v[a] += (double)V[a * ng + c];
+      }
     }
   }
+  unsigned big = __ballot_sync(0xffffffffu, valid && !small);
+  while (big) {
+    const int b = __ffs(big) - 1;
+    big &= big - 1;
+    const int bx = __shfl_sync(0xffffffffu, x0, b), by = __shfl_sync(0xffffffffu, y0, b);
+    const int bz = __shfl_sync(0xffffffffu, z0, b), bc = __shfl_sync(0xffffffffu, cnt, b);
+    double ts[3] = {0, 0, 0}, tv[3] = {0, 0, 0};
+    for (int q = lane; q < bc; q += 32) {
+      const size_t c = cell_of(q, bx, by, bz);
 #pragma unroll
-  for (int a = 0; a < 3; a++)
-#pragma unroll
-    for (int w = 16; w > 0; w >>= 1) {
-      s1[a] += __shfl_xor_sync(0xffffffffu, s1[a], w);
-      s2[a] += __shfl_xor_sync(0xffffffffu, s2[a], w);
+      for (int a = 0; a < 3; a++) {
+        ts[a] += (double)S[a * ng + c];
+        if (V) tv[a] += (double)V[a * ng + c];
+      }
     }
-  if (lane == 0) {
-    const int cnt = e;
-    const int xc[3] = {x0, y0, z0};
 #pragma unroll
-    for (int a = 0; a < 3; a++) {
-      const float disp = (float)(s1[a] + s2[a]);
-      // cysumf(x Lc + Lc/2, disp/count, L) of lpt.c:245-255
-      const float xq = (float)((double)((float)xc[a] * o.Lc) + (double)o.Lc / 2.0);
-      float p = xq + disp / (float)cnt;
-      if (p >= o.L[a]) p -= o.L[a];
-      if (p < 0.f) p += o.L[a];
-      o.posh[3 * h + a] = p;
-      if (o.velh) o.velh[3 * h + a] = (float)((o.f1 * s1[a] + o.f2 * s2[a]) / (double)cnt);
-    }
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int w = 16; w > 0; w >>= 1) {
+        ts[a] += __shfl_xor_sync(0xffffffffu, ts[a], w);
+        tv[a] += __shfl_xor_sync(0xffffffffu, tv[a], w);
+      }
+    if (lane == b)
+      for (int a = 0; a < 3; a++) { s[a] = ts[a]; v[a] = tv[a]; }
+  }
+  if (!valid) return;
+  const int xc[3] = {x0, y0, z0};
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const float disp = (float)s[a];
+    // cysumf(x Lc + Lc/2, disp / count, L), exshalos_h.c:13-19
+    const float xq = (float)((double)((float)xc[a] * o.Lc) + (double)o.Lc / 2.0);
+    float p = xq + disp / (float)cnt;
+    if (p >= o.L[a]) p -= o.L[a];
+    if (p < 0.f) p += o.L[a];
+    o.posh[3 * h + a] = p;
+    if (o.velh) o.velh[3 * h + a] = (float)(v[a] / (double)cnt);
   }
 }
 
-// particle positions q + S1 + S2 and velocities for every cell (lpt.c:82-92,
-// 212-222, 229-242); outputs interleaved [ng][3]
-__global__ void k_particles(const float* __restrict__ S, const float* __restrict__ phi2, int n0, int n1, int n2,
-                            float s2fac, HaloOut o, float* __restrict__ pos, float* __restrict__ vel) {
+// particle positions q + S and velocities (lpt.c:82-92, 212-222, 229-242),
+// interleaved [ng][3]
+__global__ void k_particles(const float* __restrict__ S, const float* __restrict__ V, int n0, int n1, int n2,
+                            HaloOut o, float* __restrict__ pos, float* __restrict__ vel) {
   const size_t ng = (size_t)n0 * n1 * n2;
   size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
@@ -229,54 +284,14 @@ __global__ void k_particles(const float* __restrict__ S, const float* __restrict
     const int xc[3] = {i, j, k};
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-      const float s1 = S[a * ng + c];
-      const float s2 = phi2 ? (float)(grad6(phi2, i, j, k, a, n0, n1, n2) * (double)s2fac) : 0.f;
-      const float s = s1 + s2;
       const float xq = (float)((double)((float)xc[a] * o.Lc) + (double)o.Lc / 2.0);
-      float p = xq + s;
+      float p = xq + S[a * ng + c];
       if (p >= o.L[a]) p -= o.L[a];
       if (p < 0.f) p += o.L[a];
       pos[3 * c + a] = p;
-      if (vel) vel[3 * c + a] = (float)(o.f1 * s1 + o.f2 * s2);
+      if (vel) vel[3 * c + a] = V[a * ng + c];
     }
   }
-}
-
-int lpt_run(Ctx& c, const BoxParams& b, const FieldModes& modes, float k_smooth, bool do2, float* S, float* phi1,
-            float* phi2, cudaStream_t st) {
-  FFTPlan3D* p;
-  EXH_TRY(c.get_plan(b.nd[0], b.nd[1], b.nd[2], &p));
-  const size_t nk = (size_t)b.nd[0] * b.nd[1] * p->nc;
-  EXH_TRY(c.buf[B_WORK].ensure(sizeof(float2) * nk));
-  float2* work = c.buf[B_WORK].as<float2>();
-  KGrid g{b.nd[0], b.nd[1], b.nd[2], b.kl[0], b.kl[1], b.kl[2], k_smooth};
-  EXH_CUDA_TRY(fft_c2r_3d(*p, Lpt1Gen{modes, g}, work, RealPairStore{phi1, b.nd[2], 1.f}, st));
-  const unsigned grid = EXH_NUM_SMS * 16;
-  { KTimer kt(KC_LPT_STENCIL, st, 16.0 * b.ng);
-  k_lpt1_disp<<<grid, 256, 0, st>>>(phi1, b.nd[0], b.nd[1], b.nd[2], (float)(b.Normx / (60.0 * b.Lc)), S); }
-  count_launch(1);
-  EXH_CUDA_TRY(cudaGetLastError());
-  if (!do2) return EXH_OK;
-  float* src = phi2;   // the source is transformed, then phi2 overwrites it
-  { KTimer kt(KC_LPT_STENCIL, st, 16.0 * b.ng);
-  k_lpt2_source<<<grid, 256, 0, st>>>(S, b.nd[0], b.nd[1], b.nd[2], (float)(1.0 / (60.0 * b.Lc)), src); }
-  count_launch(1);
-  EXH_CUDA_TRY(cudaGetLastError());
-  const size_t rows = (size_t)b.nd[0] * b.nd[1];
-  EXH_CUDA_TRY(launch_r2c_rows(RealPairLoad{src, b.nd[2]}, HalfStore{work, p->nc}, *p, rows, st));
-  EXH_CUDA_TRY(launch_strided(CplxLoad{work, b.nd[1], p->nc}, CplxStore{work, b.nd[1], p->nc}, p->py, p->twy, -1.f,
-                              b.nd[0], p->nc, st));
-  const int inner = b.nd[1] * p->nc;
-  const size_t sm = smem_strided(b.nd[0]);
-  EXH_CUDA_TRY(set_smem(k_fft_x_poisson, sm));
-  { KTimer kt(KC_FFT_STRIDED, st, 16.0 * b.nd[0] * inner);
-  k_fft_x_poisson<<<exh_div_up(inner, FFT_W), FFT_THREADS, sm, st>>>(work, p->px, p->twx, inner, g, b.Normk); }
-  count_launch(1);
-  EXH_CUDA_TRY(cudaGetLastError());
-  EXH_CUDA_TRY(launch_strided(CplxLoad{work, b.nd[1], p->nc}, CplxStore{work, b.nd[1], p->nc}, p->py, p->twy, 1.f,
-                              b.nd[0], p->nc, st));
-  EXH_CUDA_TRY(launch_c2r_rows(HalfLoad{work, p->nc}, RealPairStore{phi2, b.nd[2], 1.f}, *p, rows, st));
-  return EXH_OK;
 }
 
 float lpt2_factor(const BoxParams& b) {
@@ -295,22 +310,79 @@ HaloOut make_halo_out(const BoxParams& b, float* posh, float* velh) {
   return o;
 }
 
+static cudaError_t launch_grad(const BoxParams& b, const float* phi, float fac, float fv, float* S, float* V, bool add,
+                               cudaStream_t st) {
+  const dim3 grid(exh_div_up(b.nd[2], BZ), exh_div_up(b.nd[1], BY), exh_div_up(b.nd[0], GX));
+  const size_t sm = sizeof(float) * (GX + 2 * H) * (BY + 2 * H) * (BZ + 2 * H);
+  auto kern = add ? k_brick_grad<true> : k_brick_grad<false>;
+  cudaError_t e = set_smem(kern, sm);
+  if (e != cudaSuccess) return e;
+  KTimer kt(KC_LPT_STENCIL, st, (4.0 + (add ? 24.0 : 12.0) * (V ? 2 : 1)) * b.ng);
+  kern<<<grid, dim3(BZ, BY), sm, st>>>(phi, b.nd[0], b.nd[1], b.nd[2], fac, fv, S, V);
+  count_launch(1);
+  return cudaGetLastError();
+}
+
+int lpt_run(Ctx& c, const BoxParams& b, const FieldModes& modes, float k_smooth, bool do2, float* S, float* V,
+            float* phi1, float* phi2, cudaStream_t st) {
+  FFTPlan3D* p;
+  EXH_TRY(c.get_plan(b.nd[0], b.nd[1], b.nd[2], &p));
+  const size_t nk = (size_t)b.nd[0] * b.nd[1] * p->nc;
+  EXH_TRY(c.buf[B_WORK].ensure(sizeof(float2) * nk));
+  float2* work = c.buf[B_WORK].as<float2>();
+  const HaloOut o = make_halo_out(b, nullptr, nullptr);
+  KGrid g{b.nd[0], b.nd[1], b.nd[2], b.kl[0], b.kl[1], b.kl[2], k_smooth};
+  EXH_CUDA_TRY(fft_c2r_3d(*p, Lpt1Gen{modes, g}, work, RealPairStore{phi1, b.nd[2], 1.f}, st));
+  // S1 = -D6(phi1) Normx / (60 Lc)  (lpt.c:64-68)
+  EXH_CUDA_TRY(launch_grad(b, phi1, (float)(-b.Normx / (60.0 * b.Lc)), (float)o.f1, S, V, false, st));
+  if (!do2) return EXH_OK;
+  float* src = phi2;   // the source is transformed, then phi2 overwrites it
+  {
+    const dim3 grid(exh_div_up(b.nd[2], BZ), exh_div_up(b.nd[1], BY), exh_div_up(b.nd[0], SX));
+    const size_t sm = sizeof(float) * (BY + 2 * H) * (BZ + 2 * H) * ((SX + 2 * H) + SX) +
+                      sizeof(float) * SX * BY * (BZ + 2 * H);
+    EXH_CUDA_TRY(set_smem(k_brick_source, sm));
+    KTimer kt(KC_LPT_STENCIL, st, 16.0 * b.ng);
+    k_brick_source<<<grid, dim3(BZ, BY), sm, st>>>(S, b.nd[0], b.nd[1], b.nd[2], (float)(1.0 / (60.0 * b.Lc)), src);
+    count_launch(1);
+    EXH_CUDA_TRY(cudaGetLastError());
+  }
+  const size_t rows = (size_t)b.nd[0] * b.nd[1];
+  EXH_CUDA_TRY(launch_r2c_rows(RealPairLoad{src, b.nd[2]}, HalfStore{work, p->nc}, *p, rows, st));
+  EXH_CUDA_TRY(launch_strided(CplxLoad{work, b.nd[1], p->nc}, CplxStore{work, b.nd[1], p->nc}, p->py, p->twy, -1.f,
+                              b.nd[0], p->nc, st));
+  const int inner = b.nd[1] * p->nc;
+  const size_t sm = smem_strided(b.nd[0]);
+  EXH_CUDA_TRY(set_smem(k_fft_x_poisson, sm));
+  {
+    KTimer kt(KC_FFT_STRIDED, st, 16.0 * b.nd[0] * inner);
+    k_fft_x_poisson<<<exh_div_up(inner, FFT_W), FFT_THREADS, sm, st>>>(work, p->px, p->twx, inner, g, b.Normk);
+    count_launch(1);
+    EXH_CUDA_TRY(cudaGetLastError());
+  }
+  EXH_CUDA_TRY(launch_strided(CplxLoad{work, b.nd[1], p->nc}, CplxStore{work, b.nd[1], p->nc}, p->py, p->twy, 1.f,
+                              b.nd[0], p->nc, st));
+  EXH_CUDA_TRY(launch_c2r_rows(HalfLoad{work, p->nc}, RealPairStore{phi2, b.nd[2], 1.f}, *p, rows, st));
+  // S += S2, V += f2 S2 with S2 = D6(phi2) Normx / (60 Lc) (-3/7) Omega^(-1/143)
+  EXH_CUDA_TRY(launch_grad(b, phi2, lpt2_factor(b), (float)o.f2, S, V, true, st));
+  return EXH_OK;
+}
+
 int halo_displacements(Ctx& c, const BoxParams& b, const HaloDev& h, const ShellTable& t, const float* S,
-                       const float* phi2, const HaloOut& o, cudaStream_t st) {
+                       const float* V, const HaloOut& o, cudaStream_t st) {
   (void)c;
   if (h.nh == 0) return EXH_OK;
-  const int64_t threads = h.nh * 32;
   KTimer kt(KC_HALO_DISP, st, 0.0);
-  k_halo_disp<<<exh_div_up(threads, 256), 256, 0, st>>>(h.hpeak, h.gfin, h.id, h.np, h.nh, t.off_all, t.start_all, S,
-                                                        phi2, b.nd[0], b.nd[1], b.nd[2], lpt2_factor(b), o);
+  k_halo_sum<<<exh_div_up(h.nh, 256), 256, 0, st>>>(h.hpeak, h.gfin, h.id, h.np, h.nh, t.off_all, t.start_all, S, V,
+                                                    b.nd[0], b.nd[1], b.nd[2], o);
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   return EXH_OK;
 }
 
-int particles(const BoxParams& b, const float* S, const float* phi2, const HaloOut& o, float* pos, float* vel,
+int particles(const BoxParams& b, const float* S, const float* V, const HaloOut& o, float* pos, float* vel,
               cudaStream_t st) {
-  k_particles<<<EXH_NUM_SMS * 16, 256, 0, st>>>(S, phi2, b.nd[0], b.nd[1], b.nd[2], lpt2_factor(b), o, pos, vel);
+  k_particles<<<EXH_NUM_SMS * 16, 256, 0, st>>>(S, V, b.nd[0], b.nd[1], b.nd[2], o, pos, vel);
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   return EXH_OK;

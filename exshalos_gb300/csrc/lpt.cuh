@@ -14,13 +14,14 @@ struct HaloOut {
   double f1, f2;   // velocity factors of the first- and second-order terms
 };
 
-// phi1 -> S (planes [3][ng]); with do2, phi2 receives the second-order potential
-int lpt_run(Ctx& c, const BoxParams& b, const FieldModes& modes, float k_smooth, bool do2, float* S, float* phi1,
-            float* phi2, cudaStream_t st);
+// S (planes [3][ng]) = first (+ second) order displacement; V (optional) the
+// matching velocities; phi1, phi2 are the potentials (work arrays)
+int lpt_run(Ctx& c, const BoxParams& b, const FieldModes& modes, float k_smooth, bool do2, float* S, float* V,
+            float* phi1, float* phi2, cudaStream_t st);
 HaloOut make_halo_out(const BoxParams& b, float* posh, float* velh);
 int halo_displacements(Ctx& c, const BoxParams& b, const HaloDev& h, const ShellTable& t, const float* S,
-                       const float* phi2, const HaloOut& o, cudaStream_t st);
-int particles(const BoxParams& b, const float* S, const float* phi2, const HaloOut& o, float* pos, float* vel,
+                       const float* V, const HaloOut& o, cudaStream_t st);
+int particles(const BoxParams& b, const float* S, const float* V, const HaloOut& o, float* pos, float* vel,
               cudaStream_t st);
 FieldModes make_modes(const BoxParams& b, const float* A_dev, int fixed, float phase);
 int upload_amplitudes(Ctx& c, const BoxParams& b, const float* K, const float* P, int Nk, float** A_dev,

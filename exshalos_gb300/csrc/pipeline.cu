@@ -174,13 +174,18 @@ int exh_halos_box_from_pk(exh_ctx* ctx, const float* k, const float* P, int Nk, 
     EXH_TRY(c.buf[B_PHI2].ensure(sizeof(float) * ng));
     phi2 = c.buf[B_PHI2].as<float>();
   }
-  EXH_TRY(lpt_run(c, b, modes, prm->k_smooth, prm->DO_2LPT != 0, S, phi1, phi2, st));
+  float* V = nullptr;
+  if (prm->OUT_VEL) {
+    EXH_TRY(c.buf[B_VEL].ensure(sizeof(float) * 3 * ng));
+    V = c.buf[B_VEL].as<float>();
+  }
+  EXH_TRY(lpt_run(c, b, modes, prm->k_smooth, prm->DO_2LPT != 0, S, V, phi1, phi2, st));
   const size_t nh = std::max<int64_t>(h.nh, 1);
   EXH_TRY(c.buf[B_POSH].ensure(sizeof(float) * 6 * nh));
   float* posh = c.buf[B_POSH].as<float>();
   float* velh = prm->OUT_VEL ? posh + 3 * nh : nullptr;
   const HaloOut o = make_halo_out(b, posh, velh);
-  EXH_TRY(halo_displacements(c, b, h, t, S, phi2, o, st));
+  EXH_TRY(halo_displacements(c, b, h, t, S, V, o, st));
   HaloState& s = c.halos;
   s.posh = posh;
   s.velh = velh;
@@ -189,7 +194,7 @@ int exh_halos_box_from_pk(exh_ctx* ctx, const float* k, const float* P, int Nk, 
     EXH_TRY(c.buf[B_V].ensure(sizeof(float) * 6 * ng));
     float* pos = c.buf[B_V].as<float>();
     float* vel = prm->OUT_VEL ? pos + 3 * ng : nullptr;
-    EXH_TRY(particles(b, S, phi2, o, pos, vel, st));
+    EXH_TRY(particles(b, S, V, o, pos, vel, st));
     s.pos = pos;
     s.vel = vel;
   }
