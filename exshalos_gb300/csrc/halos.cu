@@ -576,81 +576,84 @@ __device__ __forceinline__ void peak_coords(unsigned cell, const HaloScalars& hs
 }
 
 // Growth + shrink of find_halos.c:274-337 by one warp.  Lanes gather the
-// cells of a shell 32 at a time; every lane then adds the gathered values to
-// its running mean in shell order (shuffles), so all lanes hold the same
-// double values the reference's sequential loop produces.
-// flag == nullptr: exclusion-free.  Returns 0 ok, 1 count beyond the sigma
-// table, 2 shell beyond the tables.
+// cells of a shell 32 at a time into a per-warp buffer; lane 0 alone adds
+// them to the running mean in shell order, so the double arithmetic is the
+// reference's sequential loop (and FP64 work is done once, not per lane).
+// Integer state is kept identical in all lanes; decisions that depend on the
+// mean are broadcast from lane 0.
+// Returns 0 ok, 1 count beyond the sigma table, 2 shell beyond the tables;
+// gexit is the last shell read (the rejected one).
 __device__ int grow_warp(const GrowArgs& A, const int* __restrict__ flag, int x0, int y0, int z0, float pden,
-                         int lane, int& count_out, int& gtmp_out) {
+                         int lane, double* wbuf, int& count_out, int& gtmp_out, int& gexit_out) {
   const HaloScalars& hs = A.hs;
-  double den = (double)pden, den_tmp = (double)pden;
+  double den = (double)pden, den_tmp = (double)pden;     // meaningful in lane 0
   int count = 0, count_tmp = 1, grows_tmp = 0, grows = 0;
   const double bmin = (double)hs.Bmin, mneg = -(double)hs.Mtot;
-  while (den_tmp >= bmin) {
+  while (__shfl_sync(0xffffffffu, (int)(den_tmp >= bmin), 0)) {
     if (count < count_tmp) grows = grows_tmp;
     grows_tmp++;
     den = den_tmp;
     count = count_tmp;
-    if (count >= hs.Ncells) { count_out = count; gtmp_out = grows_tmp; return 1; }
-    if (grows_tmp > A.t.gmax) { count_out = count; gtmp_out = grows_tmp; return 2; }
-    den_tmp = __dmul_rn(den, (double)count);
+    if (count >= hs.Ncells || grows_tmp > A.t.gmax) {
+      count_out = count;
+      gtmp_out = grows_tmp;
+      gexit_out = A.t.gmax;
+      return count >= hs.Ncells ? 1 : 2;
+    }
+    if (lane == 0) den_tmp = __dmul_rn(den, (double)count);
     const int s0 = A.t.start_cap[grows_tmp], s1 = A.t.start_cap[grows_tmp + 1];
     for (int base = s0; base < s1; base += 32) {
       const int q = base + lane;
-      double v = 0.0;
       if (q < s1) {
         const size_t cell = cell_at(x0, y0, z0, A.t.off_cap[q], hs);
-        v = (flag && flag[cell] != FLAG_FREE) ? mneg : (double)A.delta[cell];
+        wbuf[lane] = (flag[cell] != FLAG_FREE) ? mneg : (double)A.delta[cell];
       }
+      __syncwarp();
       const int n = min(32, s1 - base);
-      for (int j = 0; j < n; j++) den_tmp = __dadd_rn(den_tmp, __shfl_sync(0xffffffffu, v, j));
+      if (lane == 0)
+        for (int j = 0; j < n; j++) den_tmp = __dadd_rn(den_tmp, wbuf[j]);
+      __syncwarp();
       count_tmp += n;
     }
-    den_tmp = __ddiv_rn(den_tmp, (double)count_tmp);
+    if (lane == 0) den_tmp = __ddiv_rn(den_tmp, (double)count_tmp);
   }
-  while (count > 0 && den < (double)A.Btab[count]) {
-    den_tmp = den;
+  const int gexit = grows_tmp;
+  while (count > 0 && __shfl_sync(0xffffffffu, (int)(den < (double)A.Btab[count]), 0)) {
     count_tmp = count;
-    den = __dmul_rn(den, (double)count);
+    if (lane == 0) den = __dmul_rn(den, (double)count);
     const int s0 = A.t.start_cap[grows], s1 = A.t.start_cap[grows + 1];
     for (int base = s0; base < s1; base += 32) {
       const int q = base + lane;
-      double v = 0.0;
-      if (q < s1) v = (double)A.delta[cell_at(x0, y0, z0, A.t.off_cap[q], hs)];
+      if (q < s1) wbuf[lane] = (double)A.delta[cell_at(x0, y0, z0, A.t.off_cap[q], hs)];
+      __syncwarp();
       const int n = min(32, s1 - base);
-      for (int j = 0; j < n; j++) den = __dsub_rn(den, __shfl_sync(0xffffffffu, v, j));
+      if (lane == 0)
+        for (int j = 0; j < n; j++) den = __dsub_rn(den, wbuf[j]);
+      __syncwarp();
       count -= n;
     }
-    if (count > 0) den = __ddiv_rn(den, (double)count);
+    if (lane == 0 && count > 0) den = __ddiv_rn(den, (double)count);
     if (count < count_tmp) grows_tmp = grows;
     grows--;
   }
   count_out = count;
   gtmp_out = grows_tmp;
+  gexit_out = gexit;
   return 0;
 }
 
 constexpr int GROW_T = 256;   // 8 peaks (one per warp) per block
 
-__global__ void __launch_bounds__(GROW_T) k_gfree(GrowArgs A, int* __restrict__ gfree) {
-  const int r = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
-  if (r >= A.nproc) return;
-  const int64_t l = A.np - 1 - r;
-  int x, y, z;
-  peak_coords(A.id[l], A.hs, x, y, z);
-  int cnt, gt;
-  const int st = grow_warp(A, nullptr, x, y, z, A.key[l], lane, cnt, gt);
-  // growth with exclusion reads at most the shells this one reads
-  if (lane == 0) gfree[r] = st ? A.t.gmax : min(gt, A.t.gmax);
-}
-
 __device__ __forceinline__ unsigned resv_key(int tag, int r) { return ((unsigned)tag << 24) | (0xFFFFFFu - (unsigned)r); }
 
+// One round, part 1: every pending peak grows with the flags committed so
+// far (an upper bound of its final reads, since flags are only ever added),
+// keeps the result and reserves the cells up to the shell it read last.
 __global__ void __launch_bounds__(GROW_T)
-k_reserve(GrowArgs A, const int* __restrict__ gfree, unsigned char* __restrict__ state, const int* __restrict__ flag,
-          unsigned* __restrict__ resv, int tag, int* __restrict__ cnt, int* __restrict__ npend) {
+k_tentative(GrowArgs A, unsigned char* __restrict__ state, const int* __restrict__ flag, unsigned* __restrict__ resv,
+            int tag, int* __restrict__ cnt, int* __restrict__ gtmp, int* __restrict__ gexit, int* __restrict__ gst,
+            int* __restrict__ npend) {
+  __shared__ double wb[GROW_T / 32][32];
   const int r = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (r >= A.nproc || state[r]) return;
@@ -663,15 +666,24 @@ k_reserve(GrowArgs A, const int* __restrict__ gfree, unsigned char* __restrict__
   if (lane == 0) atomicAdd(npend, 1);
   int x, y, z;
   peak_coords(cell0, A.hs, x, y, z);
+  int count, gt, ge;
+  const int st = grow_warp(A, flag, x, y, z, A.key[l], lane, wb[threadIdx.x >> 5], count, gt, ge);
+  if (lane == 0) { cnt[r] = count; gtmp[r] = gt; gexit[r] = ge; gst[r] = st; }
   const unsigned key = resv_key(tag, r);
-  const int e = A.t.start_all[gfree[r] + 1];
-  for (int q = lane; q < e; q += 32) atomicMax(&resv[cell_at(x, y, z, A.t.off_all[q], A.hs)], key);
+  const int e = A.t.start_all[ge + 1];
+  for (int q = lane; q < e; q += 32) {
+    unsigned* pr = &resv[cell_at(x, y, z, A.t.off_all[q], A.hs)];
+    if (*pr < key) atomicMax(pr, key);
+  }
 }
 
+// One round, part 2: peaks that hold every cell they read keep their
+// tentative result (no pending peak of higher rank can change those cells)
+// and write their flags.
 __global__ void __launch_bounds__(GROW_T)
-k_commit(GrowArgs A, const int* __restrict__ gfree, unsigned char* __restrict__ state, int* __restrict__ flag,
-         const unsigned* __restrict__ resv, int tag, int* __restrict__ cnt, int* __restrict__ gfin,
-         int* __restrict__ err) {
+k_commit(GrowArgs A, unsigned char* __restrict__ state, int* __restrict__ flag, const unsigned* __restrict__ resv,
+         int tag, const int* __restrict__ cnt, const int* __restrict__ gtmp, const int* __restrict__ gexit,
+         const int* __restrict__ gst, int* __restrict__ gfin, int* __restrict__ err) {
   const int r = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (r >= A.nproc || state[r]) return;
@@ -680,17 +692,17 @@ k_commit(GrowArgs A, const int* __restrict__ gfree, unsigned char* __restrict__ 
   int x, y, z;
   peak_coords(cell0, A.hs, x, y, z);
   const unsigned key = resv_key(tag, r);
-  const int e = A.t.start_all[gfree[r] + 1];
+  const int e = A.t.start_all[gexit[r] + 1];
   bool mine = true;
   for (int q = lane; q < e && mine; q += 32) mine = resv[cell_at(x, y, z, A.t.off_all[q], A.hs)] == key;
   if (!__all_sync(0xffffffffu, mine)) return;
-  int count, gt;
-  const int st = grow_warp(A, flag, x, y, z, A.key[l], lane, count, gt);
+  const int st = gst[r];
   if (st) {
-    if (lane == 0) { atomicMax(err, st); state[r] = 1; cnt[r] = 0; }
+    if (lane == 0) { atomicMax(err, st); state[r] = 1; }
     return;
   }
-  if (lane == 0) { state[r] = 1; cnt[r] = count; gfin[r] = gt; }
+  const int count = cnt[r], gt = gtmp[r];
+  if (lane == 0) { state[r] = 1; gfin[r] = gt; }
   if (count == 0) return;                 // find_halos.c:339-340
   const int we = A.t.start_all[gt];       // cells with r^2 < grows_tmp
   for (int q = lane; q < we; q += 32) flag[cell_at(x, y, z, A.t.off_all[q], A.hs)] = r;
@@ -765,10 +777,10 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   const unsigned nb = exh_div_up(nproc, 128);
   const unsigned nbw = exh_div_up((size_t)nproc * 32, GROW_T);
   if (c.verbose) { printf("  %lld peaks above the barrier\n", (long long)nproc); fflush(stdout); }
-  { KTimer kt(KC_GROW, st, 0.0);
-  k_gfree<<<nbw, GROW_T, 0, st>>>(A, h->gfree); }
-  count_launch(1);
-  EXH_CUDA_TRY(cudaGetLastError());
+  // per processed peak during the rounds: gfree = last shell read,
+  // kept = growth status; both are rewritten after the rounds
+  int* gexit = h->gfree;
+  int* gst = kept;
   // device counters: [0] pending this round, [1] error
   EXH_TRY(c.buf[B_HOSTIO2].ensure(64));
   int* dcnt = c.buf[B_HOSTIO2].as<int>();
@@ -778,8 +790,9 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
     if (round > 0 && tag == 1) EXH_CUDA_TRY(cudaMemsetAsync(h->resv, 0, sizeof(unsigned) * ng, st));
     EXH_CUDA_TRY(cudaMemsetAsync(dcnt, 0, sizeof(int) * 2, st));
     KTimer kt(KC_GROW, st, 0.0);
-    k_reserve<<<nbw, GROW_T, 0, st>>>(A, h->gfree, h->state, h->flag, h->resv, tag, h->cnt, dcnt);
-    k_commit<<<nbw, GROW_T, 0, st>>>(A, h->gfree, h->state, h->flag, h->resv, tag, h->cnt, h->gfin, dcnt + 1);
+    k_tentative<<<nbw, GROW_T, 0, st>>>(A, h->state, h->flag, h->resv, tag, h->cnt, h->gfin, gexit, gst, dcnt);
+    k_commit<<<nbw, GROW_T, 0, st>>>(A, h->state, h->flag, h->resv, tag, h->cnt, h->gfin, gexit, gst, h->gfin,
+                                    dcnt + 1);
     count_launch(2);
     EXH_CUDA_TRY(cudaGetLastError());
     int hc[2];
