@@ -86,6 +86,14 @@ struct Ctx {
   HaloState halos;
   int64_t launches = 0;
   int verbose = 0;     // progress lines on stdout, as the reference's verbose flag
+  // host tables of the last distinct (P(k), cosmology, cell, barrier) input
+  std::string tab_key;
+  HostTables tab_cache;
+  // device tables reused while their inputs repeat
+  std::string amp_key;                  // field amplitudes (B_TAB)
+  int shell_ncells = -1, shell_nmin = -1, shell_gmax = 0;   // shell offsets (B_HALO2)
+  size_t shell_ncap = 0, shell_nall = 0;
+  std::string mass_key;                 // mass-function splines (B_WORK2)
   int get_plan(int nx, int ny, int nz, FFTPlan3D** out);
 };
 

@@ -25,6 +25,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "halos.cuh"
@@ -35,6 +36,16 @@ namespace exh {
 // ------------------------------------------------------------------ shells
 int build_shell_tables(Ctx& c, const BoxParams& b, int Ncells, ShellTable* t, cudaStream_t st) {
   const int T = b.nmin / 2;
+  if (c.shell_ncells == Ncells && c.shell_nmin == b.nmin && c.buf[B_HALO2].p) {
+    int* base = c.buf[B_HALO2].as<int>();
+    t->gmax = c.shell_gmax;
+    t->off_cap = base;
+    t->off_all = base + c.shell_ncap;
+    t->start_cap = t->off_all + c.shell_nall;
+    t->start_all = t->start_cap + (t->gmax + 2);
+    return EXH_OK;
+  }
+  c.shell_ncells = -1;
   const std::vector<int>& cis = cells_in_spheres();
   // last shell needed: the first r^2 whose cumulative count reaches Ncells
   long cum = 0;
@@ -91,6 +102,11 @@ int build_shell_tables(Ctx& c, const BoxParams& b, int Ncells, ShellTable* t, cu
   host.insert(host.end(), sa.begin(), sa.end());
   EXH_CUDA_TRY(cudaMemcpyAsync(base, host.data(), bytes, cudaMemcpyHostToDevice, st));
   EXH_CUDA_TRY(cudaStreamSynchronize(st));
+  c.shell_ncells = Ncells;
+  c.shell_nmin = b.nmin;
+  c.shell_gmax = gmax;
+  c.shell_ncap = oc.size();
+  c.shell_nall = oa.size();
   return EXH_OK;
 }
 
@@ -729,22 +745,31 @@ __global__ void k_halo_index(const int* __restrict__ kept, const int* __restrict
   }
 }
 
+__global__ void k_lower_bound(const float* __restrict__ key, int64_t n, float v, long long* out) {
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) / 2;
+    if (key[mid] < v) lo = mid + 1;
+    else hi = mid;
+  }
+  *out = lo;
+}
+
 int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars& hs, const float* Btab_dev,
                const ShellTable& t, HaloDev* h, cudaStream_t st) {
   const int64_t np = h->np;
   // the reference loop visits sorted indices np-1 .. 1 while den >= Bmin
   int64_t nproc = 0;
   if (np >= 2) {
-    // lower bound of Bmin in the ascending keys, on the host
-    std::vector<float> keys(np);
-    EXH_CUDA_TRY(cudaMemcpyAsync(keys.data(), h->key, sizeof(float) * np, cudaMemcpyDeviceToHost, st));
+    // lower bound of Bmin in the ascending keys
+    EXH_TRY(c.buf[B_HOSTIO2].ensure(64));
+    long long* dlb = c.buf[B_HOSTIO2].as<long long>();
+    k_lower_bound<<<1, 1, 0, st>>>(h->key, np, hs.Bmin, dlb);
+    count_launch(1);
+    EXH_CUDA_TRY(cudaGetLastError());
+    long long lo = 0;
+    EXH_CUDA_TRY(cudaMemcpyAsync(&lo, dlb, sizeof(lo), cudaMemcpyDeviceToHost, st));
     EXH_CUDA_TRY(cudaStreamSynchronize(st));
-    int64_t lo = 0, hi = np;
-    while (lo < hi) {
-      const int64_t mid = (lo + hi) / 2;
-      if (keys[mid] < hs.Bmin) lo = mid + 1;
-      else hi = mid;
-    }
     const int64_t L0 = std::max<int64_t>(lo, 1);
     nproc = np - L0;
   }
@@ -853,7 +878,6 @@ int flags_to_reference(const HaloDev& h, size_t ng, int64_t* out_dev, cudaStream
 // taus jump matrices: for component c and power 2^e, 32 column words
 struct TausJump {
   unsigned col[3][32][32];   // [component][bit e][column]
-  unsigned s0[3];            // state after seeding
 };
 
 static unsigned taus_step1(unsigned s, int c) {
@@ -862,7 +886,7 @@ static unsigned taus_step1(unsigned s, int c) {
   return ((s & 0xFFFFFFF0u) << 17) ^ (((s << 3) ^ s) >> 11);
 }
 
-static void taus_jump_tables(unsigned long seed, TausJump* J) {
+static void taus_seed_state(unsigned long seed, unsigned s0[3]) {
   // the seeding documented for gsl_rng_taus: LCG(69069) chain, minimum
   // values 2, 8, 16, six warm-up steps
   unsigned s = (unsigned)(seed & 0xFFFFFFFFul);
@@ -874,7 +898,12 @@ static void taus_jump_tables(unsigned long seed, TausJump* J) {
   unsigned s3 = 69069u * s2;
   if (s3 < 16u) s3 += 16u;
   for (int w = 0; w < 6; w++) { s1 = taus_step1(s1, 0); s2 = taus_step1(s2, 1); s3 = taus_step1(s3, 2); }
-  J->s0[0] = s1; J->s0[1] = s2; J->s0[2] = s3;
+  s0[0] = s1; s0[1] = s2; s0[2] = s3;
+}
+
+// one step of each component is linear over GF(2); column b of the step
+// matrix is the image of bit b.  Squaring gives the 2^e-step matrices.
+static void taus_jump_tables(TausJump* J) {
   for (int c = 0; c < 3; c++) {
     unsigned cur[32];
     for (int b = 0; b < 32; b++) cur[b] = taus_step1(1u << b, c);     // one step
@@ -924,7 +953,11 @@ struct DevSpline {
 
 constexpr int MASS_CHUNK = 32;
 
-__global__ void k_masses(const TausJump* __restrict__ J, DevSpline sI, DevSpline sInv, const int* __restrict__ hpeak,
+struct TausState {
+  unsigned s[3];
+};
+
+__global__ void k_masses(const TausJump* __restrict__ J, TausState s0, DevSpline sI, DevSpline sInv, const int* __restrict__ hpeak,
                          const int* __restrict__ cnt, const unsigned* __restrict__ pid, int64_t np,
                          const int* __restrict__ spheres, int nsph, int Ncells, float Mcell, int64_t nh,
                          HaloScalars hs, float* __restrict__ Mh, int* __restrict__ count_out, int* __restrict__ xc,
@@ -932,7 +965,7 @@ __global__ void k_masses(const TausJump* __restrict__ J, DevSpline sI, DevSpline
   const int64_t h0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * MASS_CHUNK;
   if (h0 >= nh) return;
   // state after h0 draws
-  unsigned s[3] = {J->s0[0], J->s0[1], J->s0[2]};
+  unsigned s[3] = {s0.s[0], s0.s[1], s0.s[2]};
   for (int e = 0; e < 32; e++)
     if ((h0 >> e) & 1)
       for (int c = 0; c < 3; c++) s[c] = gf2_apply(J->col[c][e], s[c]);
@@ -974,32 +1007,44 @@ __global__ void k_masses(const TausJump* __restrict__ J, DevSpline sI, DevSpline
 int halo_masses(Ctx& c, const BoxParams& b, const HaloDev& h, const HostTables& tab, float* Mh_dev, int* count_dev,
                 int* xc_dev, cudaStream_t st) {
   if (h.nh == 0) return EXH_OK;
-  TausJump J;
-  taus_jump_tables((unsigned long)b.seed, &J);
+  static TausJump J;
+  static bool J_ready = false;
+  if (!J_ready) { taus_jump_tables(&J); J_ready = true; }
+  TausState s0;
+  taus_seed_state((unsigned long)b.seed, s0.s);
   const std::vector<int>& sph = cells_in_spheres();
   const int Nr = tab.Nr;
-  // spline coefficients for I(M) and its inverse
-  Spline sI, sInv;
-  if (sI.init(tab.M.data(), tab.Int.data(), Nr) != EXH_OK || sInv.init(tab.Int.data(), tab.M.data(), Nr) != EXH_OK) {
-    exh_set_error_msg("mass-function integral is not increasing", __FILE__, __LINE__);
-    return EXH_E_RANGE;
-  }
   const size_t bytes = sizeof(TausJump) + sizeof(double) * 6 * Nr + sizeof(int) * sph.size() + 64;
+  // device copies of the jump matrices, the I(M) splines and the sphere
+  // table: uploaded once per distinct set of tables
+  std::string key(reinterpret_cast<const char*>(tab.M.data()), sizeof(double) * Nr);
+  key.append(reinterpret_cast<const char*>(tab.Int.data()), sizeof(double) * Nr);
+  const bool cached = key == c.mass_key && c.buf[B_WORK2].p && c.buf[B_WORK2].cap >= bytes;
+  if (!cached) c.mass_key.clear();
   EXH_TRY(c.buf[B_WORK2].ensure(bytes));
   char* base = c.buf[B_WORK2].as<char>();
   TausJump* dJ = reinterpret_cast<TausJump*>(base);
   double* dd = reinterpret_cast<double*>(base + ((sizeof(TausJump) + 15) & ~size_t(15)));
   int* dsph = reinterpret_cast<int*>(dd + 6 * Nr);
-  std::vector<double> hd(6 * Nr);
-  std::memcpy(&hd[0], sI.x.data(), sizeof(double) * Nr);
-  std::memcpy(&hd[Nr], sI.y.data(), sizeof(double) * Nr);
-  std::memcpy(&hd[2 * Nr], sI.c.data(), sizeof(double) * Nr);
-  std::memcpy(&hd[3 * Nr], sInv.x.data(), sizeof(double) * Nr);
-  std::memcpy(&hd[4 * Nr], sInv.y.data(), sizeof(double) * Nr);
-  std::memcpy(&hd[5 * Nr], sInv.c.data(), sizeof(double) * Nr);
-  EXH_CUDA_TRY(cudaMemcpyAsync(dJ, &J, sizeof(J), cudaMemcpyHostToDevice, st));
-  EXH_CUDA_TRY(cudaMemcpyAsync(dd, hd.data(), sizeof(double) * hd.size(), cudaMemcpyHostToDevice, st));
-  EXH_CUDA_TRY(cudaMemcpyAsync(dsph, sph.data(), sizeof(int) * sph.size(), cudaMemcpyHostToDevice, st));
+  if (!cached) {
+    Spline sI, sInv;
+    if (sI.init(tab.M.data(), tab.Int.data(), Nr) != EXH_OK || sInv.init(tab.Int.data(), tab.M.data(), Nr) != EXH_OK) {
+      exh_set_error_msg("mass-function integral is not increasing", __FILE__, __LINE__);
+      return EXH_E_RANGE;
+    }
+    std::vector<double> hd(6 * Nr);
+    std::memcpy(&hd[0], sI.x.data(), sizeof(double) * Nr);
+    std::memcpy(&hd[Nr], sI.y.data(), sizeof(double) * Nr);
+    std::memcpy(&hd[2 * Nr], sI.c.data(), sizeof(double) * Nr);
+    std::memcpy(&hd[3 * Nr], sInv.x.data(), sizeof(double) * Nr);
+    std::memcpy(&hd[4 * Nr], sInv.y.data(), sizeof(double) * Nr);
+    std::memcpy(&hd[5 * Nr], sInv.c.data(), sizeof(double) * Nr);
+    EXH_CUDA_TRY(cudaMemcpyAsync(dJ, &J, sizeof(J), cudaMemcpyHostToDevice, st));
+    EXH_CUDA_TRY(cudaMemcpyAsync(dd, hd.data(), sizeof(double) * hd.size(), cudaMemcpyHostToDevice, st));
+    EXH_CUDA_TRY(cudaMemcpyAsync(dsph, sph.data(), sizeof(int) * sph.size(), cudaMemcpyHostToDevice, st));
+    EXH_CUDA_TRY(cudaStreamSynchronize(st));   // the host vectors die here
+    c.mass_key = key;
+  }
   DevSpline dI{dd, dd + Nr, dd + 2 * Nr, Nr}, dInv{dd + 3 * Nr, dd + 4 * Nr, dd + 5 * Nr, Nr};
   EXH_TRY(c.buf[B_HOSTIO2].ensure(64));
   int* derr = c.buf[B_HOSTIO2].as<int>();
@@ -1008,13 +1053,13 @@ int halo_masses(Ctx& c, const BoxParams& b, const HaloDev& h, const HostTables& 
   hs.n0 = b.nd[0]; hs.n1 = b.nd[1]; hs.n2 = b.nd[2];
   const int64_t nchunk = (h.nh + MASS_CHUNK - 1) / MASS_CHUNK;
   { KTimer kt(KC_MASS, st, 0.0);
-  k_masses<<<exh_div_up(nchunk, 128), 128, 0, st>>>(dJ, dI, dInv, h.hpeak, h.cnt, h.id, h.np, dsph, (int)sph.size(),
+  k_masses<<<exh_div_up(nchunk, 128), 128, 0, st>>>(dJ, s0, dI, dInv, h.hpeak, h.cnt, h.id, h.np, dsph, (int)sph.size(),
                                                    tab.Ncells, b.Mcell, h.nh, hs, Mh_dev, count_dev, xc_dev, derr); }
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   int herr = 0;
   EXH_CUDA_TRY(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, st));
-  EXH_CUDA_TRY(cudaStreamSynchronize(st));   // host tables above must outlive the copies
+  EXH_CUDA_TRY(cudaStreamSynchronize(st));
   if (herr) {
     exh_set_error_msg("halo mass outside the mass-function tables", __FILE__, __LINE__);
     return EXH_E_RANGE;

@@ -4,6 +4,7 @@
 // (exshalos.c:46-121) and the result fetch.
 #include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "ctx.cuh"
@@ -45,9 +46,25 @@ namespace {
 int run_halo_finder(Ctx& c, const BoxParams& b, const float* k, const float* P, int Nk, int setup_fp64,
                     const float* delta, HaloDev* h, ShellTable* t, cudaStream_t st) {
   HostTables& tab = c.halos.tab;
-  EXH_TRY(halo_tables(b, k, P, Nk, setup_fp64, tab.Sig_grid, tab.Btab, tab.M, tab.Int));
-  tab.Ncells = (int)tab.Sig_grid.size();
-  tab.Nr = Nk;
+  // the tables depend on P(k), the cosmology, the cell and the barrier only:
+  // reuse them across realisations (the key holds every input bit)
+  std::string key;
+  {
+    const float scal[] = {b.Om0, b.redshift, b.dc, b.Lc, b.a, b.beta, b.alpha};
+    key.append(reinterpret_cast<const char*>(scal), sizeof(scal));
+    key.append(reinterpret_cast<const char*>(&setup_fp64), sizeof(int));
+    key.append(reinterpret_cast<const char*>(k), sizeof(float) * Nk);
+    key.append(reinterpret_cast<const char*>(P), sizeof(float) * Nk);
+  }
+  if (key != c.tab_key || c.tab_cache.Ncells == 0) {
+    HostTables fresh;
+    EXH_TRY(halo_tables(b, k, P, Nk, setup_fp64, fresh.Sig_grid, fresh.Btab, fresh.M, fresh.Int));
+    fresh.Ncells = (int)fresh.Sig_grid.size();
+    fresh.Nr = Nk;
+    c.tab_cache = fresh;
+    c.tab_key = key;
+  }
+  tab = c.tab_cache;
   EXH_TRY(build_shell_tables(c, b, tab.Ncells, t, st));
   EXH_TRY(c.buf[B_HOSTIO].ensure(sizeof(float) * tab.Ncells));
   float* Btab_dev = c.buf[B_HOSTIO].as<float>();

@@ -9,14 +9,35 @@
 // tables are bit-identical to what the reference computes with the same libm.
 #include "setup.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <thread>
+#include <vector>
 
 #include "../../include/exh_gb300.h"
 
 namespace exh {
 
 static const double kMmax = 1e+16;  // exshalos_h.h:47
+
+// f(i) for i in [0, n) on up to hardware_concurrency threads; every index is
+// computed by exactly one thread, so the results do not depend on the split.
+template <class F>
+static void parallel_for(int n, F f) {
+  int nt = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), 32u);
+  nt = std::min(nt, std::max(1, n / 16));
+  if (nt <= 1) {
+    for (int i = 0; i < n; i++) f(i);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; t++)
+    th.emplace_back([=]() {
+      for (int i = t; i < n; i += nt) f(i);
+    });
+  for (auto& x : th) x.join();
+}
 
 // The reference calls the C <math.h> functions, which take and return double
 // even for float arguments; these wrappers keep that promotion (the C++
@@ -162,7 +183,7 @@ int halo_tables(const BoxParams& b, const float* K, const float* P, int Nk, int 
       R[i] = r;
       M[i] = (double)4.0 / 3.0 * M_PI * ((float)b.rhomz * c_pow(r, 3));
     }
-    for (int i = 0; i < Nr; i++) sig[i] = (double)c_sqrt(sigma2_f(K, P, Nk, (float)R[i]));
+    parallel_for(Nr, [&](int i) { sig[i] = (double)c_sqrt(sigma2_f(K, P, Nk, (float)R[i])); });
   } else {
     const double Rmin = c_pow((double)b.Mcell * 0.9 * 3.0 / (4.0 * M_PI * (double)b.rhomz), 1.0 / 3.0);
     const double Rmax = c_pow(kMmax * 3.0 / (4.0 * M_PI * (double)b.rhomz), 1.0 / 3.0);
@@ -170,7 +191,7 @@ int halo_tables(const BoxParams& b, const float* K, const float* P, int Nk, int 
       R[i] = c_pow(10.0, c_log10(Rmin) + i * (c_log10(Rmax) - c_log10(Rmin)) / (Nr - 1));
       M[i] = 4.0 / 3.0 * M_PI * (double)b.rhomz * c_pow(R[i], 3);
     }
-    for (int i = 0; i < Nr; i++) sig[i] = c_sqrt(sigma2_d(K, P, Nk, R[i]));
+    parallel_for(Nr, [&](int i) { sig[i] = c_sqrt(sigma2_d(K, P, Nk, R[i])); });
   }
   Spline s;
   if (s.init(M.data(), sig.data(), Nr) != EXH_OK) return EXH_E_INVALID;
