@@ -666,13 +666,14 @@ __device__ __forceinline__ unsigned resv_key(int tag, int r) { return ((unsigned
 // far (an upper bound of its final reads, since flags are only ever added),
 // keeps the result and reserves the cells up to the shell it read last.
 __global__ void __launch_bounds__(GROW_T)
-k_tentative(GrowArgs A, unsigned char* __restrict__ state, const int* __restrict__ flag, unsigned* __restrict__ resv,
-            int tag, int* __restrict__ cnt, int* __restrict__ gtmp, int* __restrict__ gexit, int* __restrict__ gst,
-            int* __restrict__ npend) {
+k_tentative(GrowArgs A, const int* __restrict__ list, int nlist, unsigned char* __restrict__ state,
+            const int* __restrict__ flag, unsigned* __restrict__ resv, int tag, int* __restrict__ cnt,
+            int* __restrict__ gtmp, int* __restrict__ gexit, int* __restrict__ gst, int* __restrict__ npend) {
   __shared__ double wb[GROW_T / 32][32];
-  const int r = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
-  if (r >= A.nproc || state[r]) return;
+  if (w >= nlist) return;
+  const int r = list[w];
   const int64_t l = A.np - 1 - r;
   const unsigned cell0 = A.id[l];
   if (flag[cell0] != FLAG_FREE) {        // find_halos.c:233: the peak is already inside a halo
@@ -697,12 +698,15 @@ k_tentative(GrowArgs A, unsigned char* __restrict__ state, const int* __restrict
 // tentative result (no pending peak of higher rank can change those cells)
 // and write their flags.
 __global__ void __launch_bounds__(GROW_T)
-k_commit(GrowArgs A, unsigned char* __restrict__ state, int* __restrict__ flag, const unsigned* __restrict__ resv,
-         int tag, const int* __restrict__ cnt, const int* __restrict__ gtmp, const int* __restrict__ gexit,
+k_commit(GrowArgs A, const int* __restrict__ list, int nlist, int* __restrict__ next, int* __restrict__ nnext,
+         unsigned char* __restrict__ state, int* __restrict__ flag, const unsigned* __restrict__ resv, int tag,
+         const int* __restrict__ cnt, const int* __restrict__ gtmp, const int* __restrict__ gexit,
          const int* __restrict__ gst, int* __restrict__ gfin, int* __restrict__ err) {
-  const int r = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
-  if (r >= A.nproc || state[r]) return;
+  if (w >= nlist) return;
+  const int r = list[w];
+  if (state[r]) return;                   // resolved by the centre test this round
   const int64_t l = A.np - 1 - r;
   const unsigned cell0 = A.id[l];
   int x, y, z;
@@ -711,7 +715,10 @@ k_commit(GrowArgs A, unsigned char* __restrict__ state, int* __restrict__ flag, 
   const int e = A.t.start_all[gexit[r] + 1];
   bool mine = true;
   for (int q = lane; q < e && mine; q += 32) mine = resv[cell_at(x, y, z, A.t.off_all[q], A.hs)] == key;
-  if (!__all_sync(0xffffffffu, mine)) return;
+  if (!__all_sync(0xffffffffu, mine)) {   // still pending: next round
+    if (lane == 0) next[atomicAdd(nnext, 1)] = r;
+    return;
+  }
   const int st = gst[r];
   if (st) {
     if (lane == 0) { atomicMax(err, st); state[r] = 1; }
@@ -724,6 +731,11 @@ k_commit(GrowArgs A, unsigned char* __restrict__ state, int* __restrict__ flag, 
   for (int q = lane; q < we; q += 32) flag[cell_at(x, y, z, A.t.off_all[q], A.hs)] = r;
   __syncwarp();
   if (lane == 0) flag[cell0] = -(r + 2);
+}
+
+__global__ void k_iota(int* __restrict__ a, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = i;
 }
 
 __global__ void k_kept(const int* __restrict__ cnt, const unsigned char* __restrict__ state, int nproc, int Nmin,
@@ -809,18 +821,27 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   // device counters: [0] pending this round, [1] error
   EXH_TRY(c.buf[B_HOSTIO2].ensure(64));
   int* dcnt = c.buf[B_HOSTIO2].as<int>();
+  // pending peaks as a compacted list (misc and hid serve as the two lists
+  // during the rounds; both are rewritten afterwards)
+  int* lists[2] = {misc, h->hid};
+  k_iota<<<nb, 128, 0, st>>>(lists[0], (int)nproc);
+  count_launch(1);
+  int nlist = (int)nproc, cur = 0;
+  (void)nbw;
   int round = 0;
   while (true) {
     const int tag = (round % 255) + 1;
     if (round > 0 && tag == 1) EXH_CUDA_TRY(cudaMemsetAsync(h->resv, 0, sizeof(unsigned) * ng, st));
-    EXH_CUDA_TRY(cudaMemsetAsync(dcnt, 0, sizeof(int) * 2, st));
+    EXH_CUDA_TRY(cudaMemsetAsync(dcnt, 0, sizeof(int) * 3, st));
     KTimer kt(KC_GROW, st, 0.0);
-    k_tentative<<<nbw, GROW_T, 0, st>>>(A, h->state, h->flag, h->resv, tag, h->cnt, h->gfin, gexit, gst, dcnt);
-    k_commit<<<nbw, GROW_T, 0, st>>>(A, h->state, h->flag, h->resv, tag, h->cnt, h->gfin, gexit, gst, h->gfin,
-                                    dcnt + 1);
+    const unsigned nbl = exh_div_up((size_t)nlist * 32, GROW_T);
+    k_tentative<<<nbl, GROW_T, 0, st>>>(A, lists[cur], nlist, h->state, h->flag, h->resv, tag, h->cnt, h->gfin, gexit,
+                                        gst, dcnt);
+    k_commit<<<nbl, GROW_T, 0, st>>>(A, lists[cur], nlist, lists[cur ^ 1], dcnt + 2, h->state, h->flag, h->resv, tag,
+                                     h->cnt, h->gfin, gexit, gst, h->gfin, dcnt + 1);
     count_launch(2);
     EXH_CUDA_TRY(cudaGetLastError());
-    int hc[2];
+    int hc[3];
     EXH_CUDA_TRY(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
     EXH_CUDA_TRY(cudaStreamSynchronize(st));
     if (hc[1]) {
@@ -829,8 +850,10 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
                         __FILE__, __LINE__);
       return EXH_E_RANGE;
     }
-    if (c.verbose > 1) { printf("  growth round %d: %d pending\n", round, hc[0]); fflush(stdout); }
-    if (hc[0] == 0) break;
+    if (c.verbose > 1) { printf("  growth round %d: %d grown, %d left\n", round, hc[0], hc[2]); fflush(stdout); }
+    if (hc[2] == 0) break;
+    nlist = hc[2];
+    cur ^= 1;
     round++;
     if (round > nproc + 2) {
       exh_set_error_msg("halo growth made no progress", __FILE__, __LINE__);
