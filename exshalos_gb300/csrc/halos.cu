@@ -658,6 +658,119 @@ __device__ int grow_warp(const GrowArgs& A, const int* __restrict__ flag, int x0
   return 0;
 }
 
+// The same growth and shrink in FP32 with a running bound on the distance
+// between the FP32 mean and the reference's FP64 mean.  The outcome (count,
+// grows_tmp and the last shell read) depends only on the comparisons with
+// the barrier; when every comparison clears the bound, the outcome equals
+// the FP64 one and no FP64 arithmetic is needed.  Returns 3 when a
+// comparison falls inside the bound (the caller then runs grow_warp).
+// A claimed cell in a shell contributes -Mtot, far below any sum of
+// densities, so such a shell is rejected with certainty.
+struct FBound {
+  float f, e;   // value and bound on |f - reference double value|
+};
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int w = 16; w > 0; w >>= 1) v += __shfl_xor_sync(0xffffffffu, v, w);
+  return v;
+}
+
+// (prev * c + S) / cn with S a sum of n values (|.| summed to sabs), depth
+// the longest chain of float additions that formed S; the reference adds the
+// n values one after the other in double
+__device__ __forceinline__ FBound fb_update(FBound prev, int c, float S, float sabs, int depth, int n, int cn,
+                                            float sign) {
+  const float u = 5.9604645e-08f;                  // 2^-24
+  const float ud = 1.2e-16f;                       // > 2^-53
+  const float fc = (float)c, fcn = (float)cn;
+  const float prod = prev.f * fc;
+  const float num = prod + sign * S;
+  const float res = num / fcn;
+  // float side: product, the additions inside S and the final add/divide;
+  // double side: the same operations at 2^-53, n additions on partial sums
+  // bounded by |prod| + sabs
+  const float mag = fabsf(prod) + sabs;
+  float e = prev.e * fc + u * fabsf(prod) + (depth + 1) * u * mag + ud * (n + 3) * mag;
+  e = e / fcn + 2.f * u * fabsf(res) + ud * fabsf(res);
+  return FBound{res, e * 1.01f + 1e-30f};
+}
+
+// +1: f >= t for sure, 0: f < t for sure, -1: undecided
+__device__ __forceinline__ int fb_ge(FBound b, float t) {
+  const float slack = b.e + 3.6e-07f * (fabsf(b.f) + fabsf(t));
+  if (b.f - t >= slack) return 1;
+  if (t - b.f > slack) return 0;
+  return -1;
+}
+
+__device__ int grow_warp_f32(const GrowArgs& A, const int* __restrict__ flag, int x0, int y0, int z0, float pden,
+                             int lane, int& count_out, int& gtmp_out, int& gexit_out) {
+  const HaloScalars& hs = A.hs;
+  FBound den{pden, 0.f}, den_tmp{pden, 0.f};
+  bool rejected = false;                          // den_tmp is the -Mtot case
+  int count = 0, count_tmp = 1, grows_tmp = 0, grows = 0;
+  while (true) {
+    int d = rejected ? 0 : fb_ge(den_tmp, hs.Bmin);
+    if (d < 0) return 3;
+    if (!d) break;
+    if (count < count_tmp) grows = grows_tmp;
+    grows_tmp++;
+    den = den_tmp;
+    count = count_tmp;
+    if (count >= hs.Ncells || grows_tmp > A.t.gmax) {
+      count_out = count;
+      gtmp_out = grows_tmp;
+      gexit_out = A.t.gmax;
+      return count >= hs.Ncells ? 1 : 2;
+    }
+    const int s0 = A.t.start_cap[grows_tmp], s1 = A.t.start_cap[grows_tmp + 1];
+    float s = 0.f, sa = 0.f;
+    bool foreign = false;
+    int steps = 0;
+    for (int q = s0 + lane; q < s1; q += 32) {
+      const size_t cell = cell_at(x0, y0, z0, A.t.off_cap[q], hs);
+      if (flag[cell] != FLAG_FREE) foreign = true;
+      const float v = A.delta[cell];
+      s += v;
+      sa += fabsf(v);
+      steps++;
+    }
+    const int n = s1 - s0;
+    count_tmp += n;
+    if (__any_sync(0xffffffffu, foreign)) { rejected = true; continue; }
+    s = warp_sum(s);
+    sa = warp_sum(sa);
+    const int depth = (n + 31) / 32 + 5;
+    den_tmp = fb_update(den, count, s, sa, depth, n, count_tmp, 1.f);
+  }
+  const int gexit = grows_tmp;
+  while (count > 0) {
+    const int d = fb_ge(den, A.Btab[count]);      // shrink while den < B
+    if (d < 0) return 3;
+    if (d == 1) break;
+    count_tmp = count;
+    const int s0 = A.t.start_cap[grows], s1 = A.t.start_cap[grows + 1];
+    float s = 0.f, sa = 0.f;
+    for (int q = s0 + lane; q < s1; q += 32) {
+      const float v = A.delta[cell_at(x0, y0, z0, A.t.off_cap[q], hs)];
+      s += v;
+      sa += fabsf(v);
+    }
+    const int n = s1 - s0;
+    s = warp_sum(s);
+    sa = warp_sum(sa);
+    count -= n;
+    if (count > 0) den = fb_update(den, count_tmp, s, sa, (n + 31) / 32 + 5, n, count, -1.f);
+    if (count < count_tmp) grows_tmp = grows;
+    grows--;
+  }
+  count_out = count;
+  gtmp_out = grows_tmp;
+  gexit_out = gexit;
+  return 0;
+}
+
 constexpr int GROW_T = 256;   // 8 peaks (one per warp) per block
 
 __device__ __forceinline__ unsigned resv_key(int tag, int r) { return ((unsigned)tag << 24) | (0xFFFFFFu - (unsigned)r); }
@@ -684,7 +797,8 @@ k_tentative(GrowArgs A, const int* __restrict__ list, int nlist, unsigned char* 
   int x, y, z;
   peak_coords(cell0, A.hs, x, y, z);
   int count, gt, ge;
-  const int st = grow_warp(A, flag, x, y, z, A.key[l], lane, wb[threadIdx.x >> 5], count, gt, ge);
+  int st = grow_warp_f32(A, flag, x, y, z, A.key[l], lane, count, gt, ge);
+  if (st == 3) st = grow_warp(A, flag, x, y, z, A.key[l], lane, wb[threadIdx.x >> 5], count, gt, ge);
   if (lane == 0) { cnt[r] = count; gtmp[r] = gt; gexit[r] = ge; gst[r] = st; }
   const unsigned key = resv_key(tag, r);
   const int e = A.t.start_all[ge + 1];
