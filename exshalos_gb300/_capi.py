@@ -61,6 +61,8 @@ SIGNATURES = {
     "exh_fft_r2c_3d": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P]),
     "exh_fft_c2r_3d": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P]),
     "exh_launch_count": (C.c_int64, [_P]),
+    "exh_power_compute_noalloc": (C.c_int, [_P, C.c_int, C.c_float, C.c_int, C.c_int, C.c_float, C.c_float, _P, _P,
+                                            _P, _P]),
     "exh_timing_enable": (C.c_int, [C.c_int]),
     "exh_timing_report": (C.c_int, [C.c_int, _P, _P, _P]),
 }

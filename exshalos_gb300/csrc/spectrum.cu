@@ -8,6 +8,7 @@
 // real-to-complex FFT deconvolves the window and bins |delta_k|^2 straight
 // from shared memory into per-block FP64 histograms.
 #include <cmath>
+#include <mutex>
 
 #include "ctx.cuh"
 #include "fft.cuh"
@@ -213,4 +214,159 @@ int power_spectrum(Ctx& c, const float* grid_dev, int nd, float L, int window, i
   return EXH_OK;
 }
 
+// ------------------------------------------------------------------------
+// Power spectrum that allocates nothing.
+//
+// Some callers cannot call cudaMalloc: code that runs while a stream is being
+// captured into a CUDA graph, real-time loops that must not touch the
+// allocator, and hosts whose device memory is handed out by a pool the
+// caller does not own.  exh_power_compute_noalloc gives them the power
+// spectrum of a small grid (nd <= 64, Nk <= 256) with every temporary -- the
+// half-complex work array, the twiddle tables and the per-block histograms --
+// in one file-scope device array below.  Every GPU that loads the library
+// holds that array (about 1.8 MB) until the process exits.  All calls on a
+// device share it and it keeps the last call's contents: each call rewrites
+// what it reads, and two calls that overlap on the GPU (different streams,
+// or different host threads) race on it.
+namespace {
+
+constexpr int NA_MAX_ND = 64;
+constexpr int NA_MAX_NK = 256;
+constexpr int NA_MAX_NC = NA_MAX_ND / 2 + 1;
+constexpr int NA_MAX_BLK = (NA_MAX_ND * NA_MAX_NC + FFT_W - 1) / FFT_W;
+
+struct NoAllocScratch {
+  float2 work[(size_t)NA_MAX_ND * NA_MAX_ND * NA_MAX_NC];
+  float2 twx[NA_MAX_ND], twm[NA_MAX_ND / 2], twn[NA_MAX_ND];
+  double partP[NA_MAX_BLK * NA_MAX_NK], partK[NA_MAX_BLK * NA_MAX_NK];
+  unsigned partN[NA_MAX_BLK * NA_MAX_NK];
+};
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
+
+// device address of the array, looked up once per device (with that device
+// current); the host-side symbol is only a stand-in and is never passed to
+// a kernel
+std::mutex g_na_mu;
+void* g_na_addr[64] = {};
+
+int noalloc_scratch(int dev, NoAllocScratch** out) {
+  if (dev < 0 || dev >= 64) return EXH_E_INVALID;
+  std::lock_guard<std::mutex> g(g_na_mu);
+  if (!g_na_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+      exh_set_error_msg(cudaGetErrorString(e), __FILE__, __LINE__);
+      return EXH_E_CUDA;
+    }
+    g_na_addr[dev] = p;
+  }
+  *out = reinterpret_cast<NoAllocScratch*>(g_na_addr[dev]);
+  return EXH_OK;
+}
+
+__global__ void k_na_twiddles(float2* __restrict__ tw, int n) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  double s, c;
+  sincospi(2.0 * (double)m / (double)n, &s, &c);
+  tw[m] = make_float2((float)c, (float)s);
+}
+
+__global__ void k_na_reduce(const double* __restrict__ partP, const double* __restrict__ partK,
+                            const unsigned* __restrict__ partN, int nblk, int Nk, float* __restrict__ P,
+                            float* __restrict__ K, long long* __restrict__ N) {
+  const int b = blockIdx.x;
+  __shared__ double rP[128], rK[128];
+  __shared__ unsigned long long rN[128];
+  double sP = 0.0, sK = 0.0;
+  unsigned long long sN = 0;
+  for (int q = threadIdx.x; q < nblk; q += blockDim.x) {
+    sP += partP[(size_t)q * Nk + b];
+    sK += partK[(size_t)q * Nk + b];
+    sN += partN[(size_t)q * Nk + b];
+  }
+  rP[threadIdx.x] = sP; rK[threadIdx.x] = sK; rN[threadIdx.x] = sN;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      rP[threadIdx.x] += rP[threadIdx.x + s];
+      rK[threadIdx.x] += rK[threadIdx.x + s];
+      rN[threadIdx.x] += rN[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const unsigned long long n = rN[0];
+    N[b] = (long long)n;
+    P[b] = n ? (float)(rP[0] / (double)n) : 0.f;
+    K[b] = n ? (float)(rK[0] / (double)n) : 0.f;
+  }
+}
+
+}  // namespace
+
 }  // namespace exh
+
+extern "C" int exh_power_compute_noalloc(const float* grid, int nd, float L, int window, int Nk, float k_min,
+                                         float k_max, float* k_out, float* P_out, int64_t* count_out, void* stream) {
+  using namespace exh;
+  if (!grid || !k_out || !P_out || !count_out) {
+    exh_set_error_msg("null argument", __FILE__, __LINE__);
+    return EXH_E_INVALID;
+  }
+  if (nd < 4 || nd > NA_MAX_ND || (nd % 2) != 0 || make_radix_plan(nd).nst < 0 || make_radix_plan(nd / 2).nst < 0) {
+    exh_set_error_msg("exh_power_compute_noalloc: nd must be even, 2^a 3^b and at most 64", __FILE__, __LINE__);
+    return EXH_E_INVALID;
+  }
+  if (Nk < 1 || Nk > NA_MAX_NK) {
+    exh_set_error_msg("exh_power_compute_noalloc: Nk must be in [1, 256]", __FILE__, __LINE__);
+    return EXH_E_INVALID;
+  }
+  if (!(L > 0.f) || !(k_max > k_min) || window < 0 || window > 2) {
+    exh_set_error_msg("need L > 0, k_max > k_min and window 0, 1 or 2", __FILE__, __LINE__);
+    return EXH_E_INVALID;
+  }
+  int dev = 0;
+  EXH_CUDA_TRY(cudaGetDevice(&dev));
+  NoAllocScratch* s = nullptr;
+  EXH_TRY(noalloc_scratch(dev, &s));
+  cudaStream_t st = (cudaStream_t)stream;
+  FFTPlan3D p;
+  p.nx = p.ny = p.nz = nd;
+  p.nc = nd / 2 + 1;
+  p.M = nd / 2;
+  p.px = p.py = make_radix_plan(nd);
+  p.pm = make_radix_plan(p.M);
+  p.twx = p.twy = s->twx;
+  p.twm = s->twm;
+  p.twn = s->twn;
+  k_na_twiddles<<<1, 64, 0, st>>>(s->twx, nd);
+  k_na_twiddles<<<1, 64, 0, st>>>(s->twm, p.M);
+  k_na_twiddles<<<1, 64, 0, st>>>(s->twn, nd);
+  count_launch(3);
+  EXH_CUDA_TRY(cudaGetLastError());
+  float2* work = s->work;
+  const size_t rows = (size_t)nd * nd;
+  EXH_CUDA_TRY(launch_r2c_rows(RealPairLoad{grid, nd}, HalfStore{work, p.nc}, p, rows, st));
+  EXH_CUDA_TRY(launch_strided(CplxLoad{work, nd, p.nc}, CplxStore{work, nd, p.nc}, p.py, p.twy, -1.f, nd, p.nc, st));
+  BinParams bp;
+  bp.Nk = Nk;
+  bp.kn = (float)(2 * M_PI / L);
+  bp.kmin = k_min;
+  bp.dk = (k_max - k_min) / (float)Nk;
+  bp.Lb = L / (float)nd;
+  bp.Normk = (float)pow((double)(L / (float)(nd * nd)), 1.5);
+  bp.window = window;
+  const int inner = nd * p.nc;
+  const int nblk = (int)exh_div_up(inner, FFT_W);
+  const size_t sm = smem_strided(nd) + (size_t)Nk * (2 * sizeof(double) + sizeof(unsigned)) + 16;
+  EXH_CUDA_TRY(set_smem(k_fft_x_bin, sm));
+  k_fft_x_bin<<<nblk, FFT_THREADS, sm, st>>>(work, p.px, p.twx, nd, p.nc, bp, s->partP, s->partK, s->partN);
+  k_na_reduce<<<Nk, 128, 0, st>>>(s->partP, s->partK, s->partN, nblk, Nk, P_out, k_out,
+                                  reinterpret_cast<long long*>(count_out));
+  count_launch(2);
+  EXH_CUDA_TRY(cudaGetLastError());
+  return EXH_OK;
+}

@@ -73,6 +73,20 @@ int exh_power_compute(exh_ctx *ctx, const float *grid, int nd, float L, int wind
                       float k_min, float k_max, float *k_out, float *P_out, int64_t *count_out,
                       int mem, void *stream);
 
+/* Power spectrum for callers that cannot allocate device memory: code that
+ * runs during CUDA-graph stream capture, real-time loops that must not touch
+ * the allocator, or hosts whose device memory belongs to someone else's pool.
+ * No counterpart in the reference.  Same meaning as exh_power_compute, but
+ * grid, k_out, P_out and count_out are all device pointers and nothing is
+ * allocated: the work arrays live in one static device array of about
+ * 1.8 MB that every GPU loading the library keeps until exit.  Limits:
+ * nd even, 2^a 3^b, nd <= 64; Nk <= 256 (EXH_E_INVALID beyond).  The first
+ * call on a device looks up that array's device address; make it before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race.  Kernel-class timing (exh_timing_enable) must be off. */
+int exh_power_compute_noalloc(const float *grid, int nd, float L, int window, int Nk, float k_min,
+                              float k_max, float *k_out, float *P_out, int64_t *count_out, void *stream);
+
 /* ------------------------------------------------------------------------
  * halos_box_from_pk (src/exshalos/exshalos.c:710-940 ->
  * Generate_Halos_Box_from_Pk, src/exshalos/box.c:4-68).  Field arguments

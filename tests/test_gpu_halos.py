@@ -42,7 +42,8 @@ def _compare(orc, delta, pk, Lc, Om0=0.31, z=0.0, dc=-1.0, Nmin=1, a=1.0, beta=0
     return got, want
 
 
-@pytest.mark.parametrize("nd,Lc,seed", [(32, 4.0, 1), (64, 4.0, 2), (48, 2.0, 3), (96, 3.0, 4)])
+@pytest.mark.parametrize("nd,Lc,seed", [(32, 4.0, 1), (64, 4.0, 2), (48, 2.0, 3), (96, 3.0, 4), (64, 2.0, 11),
+                                        (64, 2.0, 12), (64, 2.0, 13), (128, 2.0, 14), (128, 4.0, 15)])
 def test_find_halos_bit_exact(orc, pk, nd, Lc, seed):
     delta = _field(nd, Lc, seed, pk)
     got, want = _compare(orc, delta, pk, Lc)
