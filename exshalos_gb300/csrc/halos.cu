@@ -781,7 +781,8 @@ __device__ __forceinline__ unsigned resv_key(int tag, int r) { return ((unsigned
 __global__ void __launch_bounds__(GROW_T)
 k_tentative(GrowArgs A, const int* __restrict__ list, int nlist, unsigned char* __restrict__ state,
             const int* __restrict__ flag, unsigned* __restrict__ resv, int tag, int* __restrict__ cnt,
-            int* __restrict__ gtmp, int* __restrict__ gexit, int* __restrict__ gst, int* __restrict__ npend) {
+            int* __restrict__ gtmp, int* __restrict__ gexit, int* __restrict__ gst, int* __restrict__ npend,
+            unsigned long long* __restrict__ nbytes) {
   __shared__ double wb[GROW_T / 32][32];
   const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
@@ -800,6 +801,9 @@ k_tentative(GrowArgs A, const int* __restrict__ list, int nlist, unsigned char* 
   int st = grow_warp_f32(A, flag, x, y, z, A.key[l], lane, count, gt, ge);
   if (st == 3) st = grow_warp(A, flag, x, y, z, A.key[l], lane, wb[threadIdx.x >> 5], count, gt, ge);
   if (lane == 0) { cnt[r] = count; gtmp[r] = gt; gexit[r] = ge; gst[r] = st; }
+  if (lane == 0 && nbytes)   // cells read by the growth (density + label) and reserved (read + atomic)
+    atomicAdd(nbytes, 8ull * (A.t.start_cap[min(ge, A.t.gmax) + 1] - A.t.start_cap[1]) +
+                          8ull * A.t.start_all[ge + 1] + 8ull);
   const unsigned key = resv_key(tag, r);
   const int e = A.t.start_all[ge + 1];
   for (int q = lane; q < e; q += 32) {
@@ -815,7 +819,8 @@ __global__ void __launch_bounds__(GROW_T)
 k_commit(GrowArgs A, const int* __restrict__ list, int nlist, int* __restrict__ next, int* __restrict__ nnext,
          unsigned char* __restrict__ state, int* __restrict__ flag, const unsigned* __restrict__ resv, int tag,
          const int* __restrict__ cnt, const int* __restrict__ gtmp, const int* __restrict__ gexit,
-         const int* __restrict__ gst, int* __restrict__ gfin, int* __restrict__ err) {
+         const int* __restrict__ gst, int* __restrict__ gfin, int* __restrict__ err,
+         unsigned long long* __restrict__ nbytes) {
   const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (w >= nlist) return;
@@ -829,6 +834,7 @@ k_commit(GrowArgs A, const int* __restrict__ list, int nlist, int* __restrict__ 
   const int e = A.t.start_all[gexit[r] + 1];
   bool mine = true;
   for (int q = lane; q < e && mine; q += 32) mine = resv[cell_at(x, y, z, A.t.off_all[q], A.hs)] == key;
+  if (lane == 0 && nbytes) atomicAdd(nbytes, 4ull * e);
   if (!__all_sync(0xffffffffu, mine)) {   // still pending: next round
     if (lane == 0) next[atomicAdd(nnext, 1)] = r;
     return;
@@ -843,6 +849,7 @@ k_commit(GrowArgs A, const int* __restrict__ list, int nlist, int* __restrict__ 
   if (count == 0) return;                 // find_halos.c:339-340
   const int we = A.t.start_all[gt];       // cells with r^2 < grows_tmp
   for (int q = lane; q < we; q += 32) flag[cell_at(x, y, z, A.t.off_all[q], A.hs)] = r;
+  if (lane == 0 && nbytes) atomicAdd(nbytes, 4ull * we);
   __syncwarp();
   if (lane == 0) flag[cell0] = -(r + 2);
 }
@@ -946,18 +953,24 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   while (true) {
     const int tag = (round % 255) + 1;
     if (round > 0 && tag == 1) EXH_CUDA_TRY(cudaMemsetAsync(h->resv, 0, sizeof(unsigned) * ng, st));
-    EXH_CUDA_TRY(cudaMemsetAsync(dcnt, 0, sizeof(int) * 3, st));
+    EXH_CUDA_TRY(cudaMemsetAsync(dcnt, 0, sizeof(int) * 6, st));
+    unsigned long long* dbytes = timing_on() ? reinterpret_cast<unsigned long long*>(dcnt + 4) : nullptr;
     KTimer kt(KC_GROW, st, 0.0);
     const unsigned nbl = exh_div_up((size_t)nlist * 32, GROW_T);
     k_tentative<<<nbl, GROW_T, 0, st>>>(A, lists[cur], nlist, h->state, h->flag, h->resv, tag, h->cnt, h->gfin, gexit,
-                                        gst, dcnt);
+                                        gst, dcnt, dbytes);
     k_commit<<<nbl, GROW_T, 0, st>>>(A, lists[cur], nlist, lists[cur ^ 1], dcnt + 2, h->state, h->flag, h->resv, tag,
-                                     h->cnt, h->gfin, gexit, gst, h->gfin, dcnt + 1);
+                                     h->cnt, h->gfin, gexit, gst, h->gfin, dcnt + 1, dbytes);
     count_launch(2);
     EXH_CUDA_TRY(cudaGetLastError());
-    int hc[3];
+    int hc[6];
     EXH_CUDA_TRY(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
     EXH_CUDA_TRY(cudaStreamSynchronize(st));
+    if (dbytes) {
+      unsigned long long nb = 0;
+      std::memcpy(&nb, hc + 4, sizeof(nb));
+      kt.bytes = (double)nb;
+    }
     if (hc[1]) {
       exh_set_error_msg(hc[1] == 1 ? "a halo grew past the sigma(M) table (find_halos.c:316 would read past Sig_Grid)"
                                    : "a halo grew past every shell of the box",
