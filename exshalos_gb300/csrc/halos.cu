@@ -782,7 +782,7 @@ __global__ void __launch_bounds__(GROW_T)
 k_tentative(GrowArgs A, const int* __restrict__ list, int nlist, unsigned char* __restrict__ state,
             const int* __restrict__ flag, unsigned* __restrict__ resv, int tag, int* __restrict__ cnt,
             int* __restrict__ gtmp, int* __restrict__ gexit, int* __restrict__ gst, int* __restrict__ npend,
-            unsigned long long* __restrict__ nbytes) {
+            unsigned* __restrict__ nwords) {
   __shared__ double wb[GROW_T / 32][32];
   const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
@@ -801,9 +801,8 @@ k_tentative(GrowArgs A, const int* __restrict__ list, int nlist, unsigned char* 
   int st = grow_warp_f32(A, flag, x, y, z, A.key[l], lane, count, gt, ge);
   if (st == 3) st = grow_warp(A, flag, x, y, z, A.key[l], lane, wb[threadIdx.x >> 5], count, gt, ge);
   if (lane == 0) { cnt[r] = count; gtmp[r] = gt; gexit[r] = ge; gst[r] = st; }
-  if (lane == 0 && nbytes)   // cells read by the growth (density + label) and reserved (read + atomic)
-    atomicAdd(nbytes, 8ull * (A.t.start_cap[min(ge, A.t.gmax) + 1] - A.t.start_cap[1]) +
-                          8ull * A.t.start_all[ge + 1] + 8ull);
+  if (lane == 0 && nwords)   // 4-byte words: cells read by the growth (density + label), reserved (read + atomic)
+    nwords[r] += 2u * (A.t.start_cap[min(ge, A.t.gmax) + 1] - A.t.start_cap[1]) + 2u * A.t.start_all[ge + 1] + 2u;
   const unsigned key = resv_key(tag, r);
   const int e = A.t.start_all[ge + 1];
   for (int q = lane; q < e; q += 32) {
@@ -820,7 +819,7 @@ k_commit(GrowArgs A, const int* __restrict__ list, int nlist, int* __restrict__ 
          unsigned char* __restrict__ state, int* __restrict__ flag, const unsigned* __restrict__ resv, int tag,
          const int* __restrict__ cnt, const int* __restrict__ gtmp, const int* __restrict__ gexit,
          const int* __restrict__ gst, int* __restrict__ gfin, int* __restrict__ err,
-         unsigned long long* __restrict__ nbytes) {
+         unsigned* __restrict__ nwords) {
   const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (w >= nlist) return;
@@ -834,7 +833,7 @@ k_commit(GrowArgs A, const int* __restrict__ list, int nlist, int* __restrict__ 
   const int e = A.t.start_all[gexit[r] + 1];
   bool mine = true;
   for (int q = lane; q < e && mine; q += 32) mine = resv[cell_at(x, y, z, A.t.off_all[q], A.hs)] == key;
-  if (lane == 0 && nbytes) atomicAdd(nbytes, 4ull * e);
+  if (lane == 0 && nwords) nwords[r] += (unsigned)e;
   if (!__all_sync(0xffffffffu, mine)) {   // still pending: next round
     if (lane == 0) next[atomicAdd(nnext, 1)] = r;
     return;
@@ -849,9 +848,17 @@ k_commit(GrowArgs A, const int* __restrict__ list, int nlist, int* __restrict__ 
   if (count == 0) return;                 // find_halos.c:339-340
   const int we = A.t.start_all[gt];       // cells with r^2 < grows_tmp
   for (int q = lane; q < we; q += 32) flag[cell_at(x, y, z, A.t.off_all[q], A.hs)] = r;
-  if (lane == 0 && nbytes) atomicAdd(nbytes, 4ull * we);
+  if (lane == 0 && nwords) nwords[r] += (unsigned)we;
   __syncwarp();
   if (lane == 0) flag[cell0] = -(r + 2);
+}
+
+__global__ void k_sum_words(const unsigned* __restrict__ w, int n, unsigned long long* __restrict__ out) {
+  unsigned long long s = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s += w[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
 }
 
 __global__ void k_iota(int* __restrict__ a, int n) {
@@ -916,7 +923,7 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   EXH_TRY(c.buf[B_FLAG].ensure(sizeof(int) * ng * 2));
   h->flag = c.buf[B_FLAG].as<int>();
   h->resv = reinterpret_cast<unsigned*>(h->flag + ng);
-  EXH_TRY(c.buf[B_HALO].ensure(npr * (sizeof(int) * 7 + 1) + 64));
+  EXH_TRY(c.buf[B_HALO].ensure(npr * (sizeof(int) * 8 + 1) + 64));
   h->gfree = c.buf[B_HALO].as<int>();
   h->gfin = h->gfree + npr;
   h->cnt = h->gfin + npr;
@@ -924,7 +931,8 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   h->hpeak = h->hid + npr;
   int* kept = h->hpeak + npr;
   int* misc = kept + npr;             // npr ints: scan scratch / counters
-  h->state = reinterpret_cast<unsigned char*>(misc + npr);
+  h->words = reinterpret_cast<unsigned*>(misc + npr);
+  h->state = reinterpret_cast<unsigned char*>(h->words + npr);
   EXH_CUDA_TRY(cudaMemsetAsync(h->flag, 0xff, sizeof(int) * ng, st));      // FLAG_FREE
   EXH_CUDA_TRY(cudaMemsetAsync(h->resv, 0, sizeof(unsigned) * ng, st));
   EXH_CUDA_TRY(cudaMemsetAsync(h->state, 0, npr, st));
@@ -949,28 +957,24 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   count_launch(1);
   int nlist = (int)nproc, cur = 0;
   (void)nbw;
+  if (timing_on()) EXH_CUDA_TRY(cudaMemsetAsync(h->words, 0, sizeof(unsigned) * npr, st));
+  KTimer kt(KC_GROW, st, 0.0);   // the whole growth phase is one timed unit
   int round = 0;
   while (true) {
     const int tag = (round % 255) + 1;
     if (round > 0 && tag == 1) EXH_CUDA_TRY(cudaMemsetAsync(h->resv, 0, sizeof(unsigned) * ng, st));
     EXH_CUDA_TRY(cudaMemsetAsync(dcnt, 0, sizeof(int) * 6, st));
-    unsigned long long* dbytes = timing_on() ? reinterpret_cast<unsigned long long*>(dcnt + 4) : nullptr;
-    KTimer kt(KC_GROW, st, 0.0);
+    unsigned* dwords = timing_on() ? h->words : nullptr;
     const unsigned nbl = exh_div_up((size_t)nlist * 32, GROW_T);
     k_tentative<<<nbl, GROW_T, 0, st>>>(A, lists[cur], nlist, h->state, h->flag, h->resv, tag, h->cnt, h->gfin, gexit,
-                                        gst, dcnt, dbytes);
+                                        gst, dcnt, dwords);
     k_commit<<<nbl, GROW_T, 0, st>>>(A, lists[cur], nlist, lists[cur ^ 1], dcnt + 2, h->state, h->flag, h->resv, tag,
-                                     h->cnt, h->gfin, gexit, gst, h->gfin, dcnt + 1, dbytes);
+                                     h->cnt, h->gfin, gexit, gst, h->gfin, dcnt + 1, dwords);
     count_launch(2);
     EXH_CUDA_TRY(cudaGetLastError());
     int hc[6];
     EXH_CUDA_TRY(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
     EXH_CUDA_TRY(cudaStreamSynchronize(st));
-    if (dbytes) {
-      unsigned long long nb = 0;
-      std::memcpy(&nb, hc + 4, sizeof(nb));
-      kt.bytes = (double)nb;
-    }
     if (hc[1]) {
       exh_set_error_msg(hc[1] == 1 ? "a halo grew past the sigma(M) table (find_halos.c:316 would read past Sig_Grid)"
                                    : "a halo grew past every shell of the box",
@@ -986,6 +990,17 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
       exh_set_error_msg("halo growth made no progress", __FILE__, __LINE__);
       return EXH_E_TIMEOUT;
     }
+  }
+  if (timing_on()) {
+    // algorithmic bytes of the growth rounds: one reduction over the peaks
+    unsigned long long* dsum = reinterpret_cast<unsigned long long*>(dcnt + 4);
+    EXH_CUDA_TRY(cudaMemsetAsync(dsum, 0, sizeof(unsigned long long), st));
+    k_sum_words<<<EXH_NUM_SMS, 256, 0, st>>>(h->words, (int)nproc, dsum);
+    count_launch(1);
+    unsigned long long nw = 0;
+    EXH_CUDA_TRY(cudaMemcpyAsync(&nw, dsum, sizeof(nw), cudaMemcpyDeviceToHost, st));
+    EXH_CUDA_TRY(cudaStreamSynchronize(st));
+    kt.bytes = 4.0 * (double)nw;
   }
   k_kept<<<nb, 128, 0, st>>>(h->cnt, h->state, (int)nproc, hs.Nmin, kept);
   count_launch(1);

@@ -38,6 +38,7 @@ struct HaloDev {
   int* hpeak = nullptr;       // processed-peak index of each halo
   int* flag = nullptr;        // per cell, temporary labels
   unsigned* resv = nullptr;   // per cell reservations
+  unsigned* words = nullptr;  // per processed peak: 4-byte words the growth touched (timing only)
 };
 
 struct HaloScalars {
