@@ -3,7 +3,7 @@
 #include <vector>
 
 #include "ctx.cuh"
-#include "fft.cuh"
+#include "fft4.cuh"
 
 namespace exh {
 

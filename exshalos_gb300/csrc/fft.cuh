@@ -280,7 +280,7 @@ inline cudaError_t set_smem(K kernel, size_t bytes) {
 template <class F> constexpr int io_bytes() { return F::io_bytes; }
 
 template <class Src, class Dst>
-inline cudaError_t launch_strided(Src src, Dst dst, const RadixPlan& pl, const float2* tw, float sgn,
+inline cudaError_t launch_strided_sh(Src src, Dst dst, const RadixPlan& pl, const float2* tw, float sgn,
                                   int outer, int inner, cudaStream_t st) {
   auto kern = k_fft_strided<Src, Dst>;
   size_t sm = smem_strided(pl.n);
@@ -294,7 +294,7 @@ inline cudaError_t launch_strided(Src src, Dst dst, const RadixPlan& pl, const f
 }
 
 template <class Src, class Dst>
-inline cudaError_t launch_r2c_rows(Src src, Dst dst, const FFTPlan3D& p, size_t rows, cudaStream_t st) {
+inline cudaError_t launch_r2c_rows_sh(Src src, Dst dst, const FFTPlan3D& p, size_t rows, cudaStream_t st) {
   auto kern = k_fft_r2c_rows<Src, Dst>;
   size_t sm = smem_r2c(p.M);
   cudaError_t e = set_smem(kern, sm);
@@ -306,7 +306,7 @@ inline cudaError_t launch_r2c_rows(Src src, Dst dst, const FFTPlan3D& p, size_t 
 }
 
 template <class Src, class Dst>
-inline cudaError_t launch_c2r_rows(Src src, Dst dst, const FFTPlan3D& p, size_t rows, cudaStream_t st) {
+inline cudaError_t launch_c2r_rows_sh(Src src, Dst dst, const FFTPlan3D& p, size_t rows, cudaStream_t st) {
   auto kern = k_fft_c2r_rows<Src, Dst>;
   size_t sm = smem_c2r(p.M);
   cudaError_t e = set_smem(kern, sm);
@@ -315,32 +315,6 @@ inline cudaError_t launch_c2r_rows(Src src, Dst dst, const FFTPlan3D& p, size_t 
   kern<<<exh_div_up(rows, FFT_ROWS), FFT_THREADS, sm, st>>>(src, dst, p.pm, p.twm, p.twn, rows);
   count_launch(1);
   return cudaGetLastError();
-}
-
-// real [nx][ny][nz] -> half complex [nx][ny][nc] in `work`; the x pass
-// writes through `xdst` (a CplxStore into work for a plain transform).
-template <class RSrc, class XDst>
-inline cudaError_t fft_r2c_3d(const FFTPlan3D& p, RSrc rsrc, float2* work, XDst xdst, cudaStream_t st) {
-  cudaError_t e;
-  const size_t rows = (size_t)p.nx * p.ny;
-  e = launch_r2c_rows(rsrc, HalfStore{work, p.nc}, p, rows, st);
-  if (e != cudaSuccess) return e;
-  e = launch_strided(CplxLoad{work, p.ny, p.nc}, CplxStore{work, p.ny, p.nc}, p.py, p.twy, -1.f, p.nx, p.nc, st);
-  if (e != cudaSuccess) return e;
-  return launch_strided(CplxLoad{work, p.nx, p.ny * p.nc}, xdst, p.px, p.twx, -1.f, 1, p.ny * p.nc, st);
-}
-
-// half complex -> real; the x pass reads through `xsrc` (a CplxLoad, or a
-// generator that synthesises the modes), `work` holds the intermediate.
-template <class XSrc, class RDst>
-inline cudaError_t fft_c2r_3d(const FFTPlan3D& p, XSrc xsrc, float2* work, RDst rdst, cudaStream_t st) {
-  cudaError_t e;
-  const size_t rows = (size_t)p.nx * p.ny;
-  e = launch_strided(xsrc, CplxStore{work, p.nx, p.ny * p.nc}, p.px, p.twx, 1.f, 1, p.ny * p.nc, st);
-  if (e != cudaSuccess) return e;
-  e = launch_strided(CplxLoad{work, p.ny, p.nc}, CplxStore{work, p.ny, p.nc}, p.py, p.twy, 1.f, p.nx, p.nc, st);
-  if (e != cudaSuccess) return e;
-  return launch_c2r_rows(HalfLoad{work, p.nc}, rdst, p, rows, st);
 }
 
 }  // namespace exh

@@ -5,7 +5,7 @@
 #include <vector>
 
 #include "ctx.cuh"
-#include "fft.cuh"
+#include "fft4.cuh"
 #include "field.cuh"
 #include "pipeline.cuh"
 

@@ -13,7 +13,7 @@
 #include <cmath>
 
 #include "ctx.cuh"
-#include "fft.cuh"
+#include "fft4.cuh"
 #include "field.cuh"
 #include "halos.cuh"
 #include "lpt.cuh"

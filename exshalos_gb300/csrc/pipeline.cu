@@ -11,6 +11,7 @@
 #include "halos.cuh"
 #include "lpt.cuh"
 #include "pipeline.cuh"
+#include "fft4.cuh"
 
 using namespace exh;
 

@@ -11,7 +11,7 @@
 #include <mutex>
 
 #include "ctx.cuh"
-#include "fft.cuh"
+#include "fft4.cuh"
 #include "spectrum.cuh"
 
 namespace exh {
