@@ -58,6 +58,8 @@ SIGNATURES = {
     "exh_halos_fetch": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, C.c_int, _P]),
     "exh_halo_tables": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), _P, _P, _P, _P]),
     "exh_density_grid_compute": (C.c_int, [_P, _P, _P, C.c_int, C.POINTER(HaloParams), _P, C.c_int, _P]),
+    "exh_smoothing_ladder": (C.c_int, [_P, _P, _P, C.c_int, C.POINTER(HaloParams), C.c_int, C.c_float, _P, _P, _P,
+                                       C.c_int, _P]),
     "exh_fft_r2c_3d": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P]),
     "exh_fft_c2r_3d": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P]),
     "exh_launch_count": (C.c_int64, [_P]),

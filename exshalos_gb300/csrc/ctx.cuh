@@ -64,6 +64,8 @@ enum BufId {
   B_S,            // displacements [3][ng]
   B_V,            // particle positions / velocities [ng][3]
   B_VEL,          // velocity planes [3][ng]
+  B_CROSS,        // first-crossing map staging (u8 per cell)
+  B_LADDER,       // Fourier modes kept for the smoothing ladder (float2[nk])
   B_FLAG,         // int32 halo flag per cell
   B_PEAKS,        // peak keys/ids (sort ping-pong)
   B_PEAKS2,

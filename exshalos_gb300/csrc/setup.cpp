@@ -216,6 +216,24 @@ int halo_tables(const BoxParams& b, const float* K, const float* P, int Nk, int 
   return EXH_OK;
 }
 
+int ladder_tables(const BoxParams& b, const float* K, const float* P, int Nk, int n_radii, float R_max,
+                  std::vector<float>& R, std::vector<float>& B) {
+  if (n_radii < 1 || n_radii > 255 || !(R_max >= b.Lc)) return EXH_E_INVALID;
+  R.assign(n_radii, 0.f);
+  B.assign(n_radii, 0.f);
+  // log-spaced radii from one cell to R_max; sigma^2(R) by the FP64 top-hat
+  // trapezoid on the input table, barrier of find_halos.c:200-212 at sigma^2
+  const double lo = std::log((double)b.Lc), hi = std::log((double)R_max);
+  std::vector<double> s2(n_radii);
+  parallel_for(n_radii, [&](int i) {
+    const double r = n_radii > 1 ? std::exp(lo + (hi - lo) * i / (n_radii - 1)) : (double)b.Lc;
+    R[i] = (float)r;
+    s2[i] = sigma2_d(K, P, Nk, r);
+  });
+  for (int i = 0; i < n_radii; i++) B[i] = barrier(b, (float)s2[i]);
+  return EXH_OK;
+}
+
 int amplitude_table(const BoxParams& b, const float* K, const float* P, int Nk, std::vector<float>& A) {
   if (b.nd[0] != b.nd[1] || b.nd[0] != b.nd[2]) return EXH_E_UNSUPPORTED;
   std::vector<double> kd(Nk), pd(Nk);

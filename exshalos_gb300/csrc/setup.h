@@ -38,6 +38,10 @@ int halo_tables(const BoxParams& b, const float* K, const float* P, int Nk, int 
                 std::vector<float>& Sig_grid, std::vector<float>& Btab, std::vector<double>& M,
                 std::vector<double>& Int);
 float barrier(const BoxParams& b, float S);
+// smoothing ladder: n_radii log-spaced radii from Lc to R_max and the
+// barrier B(sigma^2(R)) at each (sigma^2 by the FP64 trapezoid)
+int ladder_tables(const BoxParams& b, const float* K, const float* P, int Nk, int n_radii, float R_max,
+                  std::vector<float>& R, std::vector<float>& B);
 // Gaussian-field amplitude sqrt(P(k)/2) per integer |n|^2 for a cubic box
 int amplitude_table(const BoxParams& b, const float* K, const float* P, int Nk, std::vector<float>& A);
 // cumulative cells per non-empty shell (find_halos.c:382-420), lmax = 10000

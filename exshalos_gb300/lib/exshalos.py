@@ -128,6 +128,33 @@ def density_grid_compute(k, P, R_max, Ndx, Ndy, Ndz, Lc, outk, seed, fixed, phas
     return {"grid": grid}
 
 
+def smoothing_ladder(k, P, R_max, Ndx, Ndy, Ndz, Lc, seed=12345, n_radii=50, Om0=0.31, z=0.0, dc=1.686, a=1.0,
+                     beta=0.0, alpha=0.0, fixed=0, phase=0.0, k_smooth=100000.0, out=None, stream=None):
+    """First-crossing map of the top-hat smoothing ladder of the Gaussian
+    field that density_grid_compute makes with the same arguments.
+
+    Returns {"cross": u8 (Ndx, Ndy, Ndz) (index of the largest crossing
+    radius, 255 = none), "R": radii, "B": barriers}.  With ``out`` a CUDA
+    uint8 tensor of ng elements, the map is written there on the device.
+    """
+    k = np.ascontiguousarray(k, dtype=np.float32)
+    P = np.ascontiguousarray(P, dtype=np.float32)
+    prm = _params(R_max=float(R_max), ndx=int(Ndx), ndy=int(Ndy), ndz=int(Ndz), Lc=float(Lc), seed=int(seed),
+                  Om0=float(Om0), redshift=float(z), dc=float(dc), a=float(a), beta=float(beta), alpha=float(alpha),
+                  fixed=int(fixed), phase=float(phase), k_smooth=float(k_smooth))
+    R = np.zeros(int(n_radii), dtype=np.float32)
+    B = np.zeros(int(n_radii), dtype=np.float32)
+    if out is None:
+        cross = np.empty((int(Ndx), int(Ndy), int(Ndz)), dtype=np.uint8)
+        dst, mem = _capi.ptr(cross), _capi.EXH_MEM_HOST
+    else:
+        cross, dst, mem = out, out.data_ptr(), _capi.EXH_MEM_DEVICE
+    _capi.check(_capi.load().exh_smoothing_ladder(_capi.context(), _capi.ptr(k), _capi.ptr(P), k.size, prm,
+                                                  int(n_radii), float(R_max), dst, _capi.ptr(R), _capi.ptr(B), mem,
+                                                  stream))
+    return {"cross": cross, "R": R, "B": B}
+
+
 def halo_tables():
     """Sigma(M), barrier and mass-function tables of the last halo call."""
     import ctypes as C

@@ -144,6 +144,20 @@ int exh_halo_tables(exh_ctx *ctx, int *Ncells, int *Nr, float *Sig_grid, float *
 int exh_density_grid_compute(exh_ctx *ctx, const float *k, const float *P, int Nk,
                              const exh_halo_params *prm, float *delta, int mem, void *stream);
 
+/* Top-hat smoothing ladder and first-crossing map.  The field of
+ * exh_density_grid_compute (same parameters, Philox modes) is smoothed with
+ * the window W(kR) of src/exshalos/exshalos_h.c:35-40 at n_radii radii R_i
+ * log-spaced from Lc to R_max (n_radii in 1..255, R_max >= Lc), and each cell
+ * gets the largest i whose smoothed density reaches the barrier
+ * B(sigma^2(R_i)) of src/exshalos/find_halos.c:200-212 (a, beta, alpha of
+ * prm; sigma^2(R) by the top-hat integral of src/exshalos/find_halos.c:4-14,
+ * in FP64); 255 where no
+ * radius crosses.  cross[ng] is u8 (host or device per mem); radii_out and
+ * barrier_out (host, n_radii floats each) may be NULL. */
+int exh_smoothing_ladder(exh_ctx *ctx, const float *k, const float *P, int Nk, const exh_halo_params *prm,
+                         int n_radii, float R_max, uint8_t *cross, float *radii_out, float *barrier_out,
+                         int mem, void *stream);
+
 /* 3-D FFTs with FFTW conventions (unnormalised, half-complex last axis,
  * interleaved float2) — the transforms fftwf_plan_dft_r2c_3d /
  * fftwf_plan_dft_c2r_3d perform at src/spectrum/spectrum_h.c:103-107 and

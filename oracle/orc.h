@@ -112,6 +112,9 @@ int orc_field_modes(const orc_params *p, const float *K, const float *P, int Nk,
                     int stream, int fixed, float phase, float k_smooth, real *deltak);
 /* c2r then x Normx (density_grid.c:207-216); deltak is left intact */
 int orc_field_real(const orc_params *p, const real *deltak, real *delta);
+/* smoothing ladder and first-crossing map (largest radius first, 255 = never) */
+int orc_ladder(const orc_params *p, const real *deltak, int n_radii, const float *R, const float *B,
+               unsigned char *cross);
 
 /* --------------------------------------------------------------- halos */
 typedef struct { int x[3]; float den; } orc_peak;       /* exshalos_h.h:51-54 */

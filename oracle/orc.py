@@ -257,3 +257,13 @@ def lpt_posh(p, k, P, flag, hx, hcount, do_2lpt=1, k_smooth=10000.0, stream=1, k
         L.orc_pos(C.byref(p), _ptr(S))
         out["pos"] = S
     return out
+
+
+def ladder(p, modes, R, B, prec="f64"):
+    """First-crossing map of the smoothing ladder on given modes."""
+    R = np.ascontiguousarray(R, dtype=np.float32)
+    B = np.ascontiguousarray(B, dtype=np.float32)
+    out = np.zeros(tuple(p.nd), dtype=np.uint8)
+    if lib(prec).orc_ladder(C.byref(p), _ptr(np.ascontiguousarray(modes)), R.size, _ptr(R), _ptr(B), _ptr(out)):
+        raise RuntimeError("oracle ladder failed")
+    return out

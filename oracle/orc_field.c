@@ -140,3 +140,40 @@ int orc_field_real(const orc_params *p, const real *deltak, real *delta) {
   for (long i = 0; i < (long)p->ng; i++) delta[i] = delta[i] * nx;
   return 0;
 }
+
+/* Smoothing ladder (FP64 oracle of the build-added stage; the window is
+ * exshalos_h.c:35-40, the barrier find_halos.c:200-212): for i from n_radii-1
+ * down to 0, delta_R = c2r(delta_k W(k R_i)) Normx, and each cell keeps the
+ * first i with delta_R >= B_i; 255 = never. */
+int orc_ladder(const orc_params *p, const real *deltak, int n_radii, const float *R, const float *B,
+               unsigned char *cross) {
+  int n0 = p->nd[0], n1 = p->nd[1], n2 = p->nd[2], nz2 = p->nz2;
+  size_t nk = (size_t)n0 * n1 * nz2, ng = p->ng;
+  real *tmp = (real *)malloc(sizeof(real) * 2 * nk), *dr = (real *)malloc(sizeof(real) * ng);
+  if (!tmp || !dr) { free(tmp); free(dr); return 1; }
+  memset(cross, 255, ng);
+  for (int r = n_radii - 1; r >= 0; r--) {
+    double Rr = R[r];
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n0; i++) {
+      double kx = ((2 * i < n0) ? i : i - n0) * p->kl_d[0];
+      for (int j = 0; j < n1; j++) {
+        double ky = ((2 * j < n1) ? j : j - n1) * p->kl_d[1];
+        for (int k = 0; k < nz2; k++) {
+          double kz = ((k == n2 / 2) ? -(n2 / 2) : k) * p->kl_d[2];
+          double x = sqrt(kx * kx + ky * ky + kz * kz) * Rr;
+          double w = x > 0.0 ? 3.0 * (sin(x) - x * cos(x)) / (x * x * x) : 1.0;
+          size_t id = ((size_t)i * n1 + j) * nz2 + k;
+          tmp[2 * id] = (real)(deltak[2 * id] * w);
+          tmp[2 * id + 1] = (real)(deltak[2 * id + 1] * w);
+        }
+      }
+    }
+    orc_fft_c2r_3d(n0, n1, n2, tmp, dr);
+    double nx = ORC_F64 ? p->Normx_d : (double)p->Normx;
+    for (size_t c = 0; c < ng; c++)
+      if (cross[c] == 255 && (double)dr[c] * nx >= (double)B[r]) cross[c] = (unsigned char)r;
+  }
+  free(tmp); free(dr);
+  return 0;
+}

@@ -1,0 +1,45 @@
+"""Top-hat smoothing ladder and first-crossing map against the FP64 oracle (GPU)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("nd,Lc,n_radii,R_max", [(64, 4.0, 50, 40.0), (48, 2.0, 12, 30.0), (32, 8.0, 1, 8.0)])
+def test_ladder_matches_fp64_oracle(orc, pk, nd, Lc, n_radii, R_max):
+    from exshalos_gb300.lib import exshalos as ex
+    k, P = pk
+    seed = 77
+    r = ex.smoothing_ladder(k, P, R_max, nd, nd, nd, Lc, seed=seed, n_radii=n_radii, a=1.0, beta=0.12, alpha=0.0)
+    R, B = r["R"], r["B"]
+    assert R[0] == pytest.approx(Lc, rel=1e-6) and R[-1] == pytest.approx(R_max, rel=1e-6)
+    assert np.all(np.diff(B) <= 0) or n_radii == 1      # barrier falls with the radius
+    p = orc.make_params(nd, Lc, seed=seed)
+    want = orc.ladder(p, orc.field_modes(p, k, P, stream=1), R, B)
+    got = r["cross"]
+    crossed = np.mean(want != 255)
+    assert 0.0 < crossed < 1.0
+    # FP32 transforms against FP64: only cells within rounding of a barrier move
+    assert np.mean(got != want) < 1e-3
+
+
+def test_ladder_device_output_and_repeat(pk):
+    import torch
+    from exshalos_gb300.lib import exshalos as ex
+    k, P = pk
+    nd = 64
+    out = torch.empty(nd ** 3, dtype=torch.uint8, device="cuda")
+    ex.smoothing_ladder(k, P, 40.0, nd, nd, nd, 4.0, seed=5, n_radii=20, out=out)
+    torch.cuda.synchronize()
+    host = ex.smoothing_ladder(k, P, 40.0, nd, nd, nd, 4.0, seed=5, n_radii=20)["cross"]
+    assert np.array_equal(out.cpu().numpy().reshape(nd, nd, nd), host)
+
+
+def test_ladder_rejects_bad_arguments(pk):
+    from exshalos_gb300 import _capi
+    from exshalos_gb300.lib import exshalos as ex
+    k, P = pk
+    with pytest.raises(ValueError):
+        ex.smoothing_ladder(k, P, 2.0, 32, 32, 32, 4.0, n_radii=10)       # R_max < Lc
+    with pytest.raises(ValueError):
+        ex.smoothing_ladder(k, P, 40.0, 32, 32, 32, 4.0, n_radii=256)

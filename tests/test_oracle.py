@@ -147,3 +147,32 @@ def test_pipeline_consistency(orc, pk):
     np.testing.assert_array_equal(flag[centre[1:]], -np.arange(1, r["nh"]))
     assert np.all(np.isfinite(r["Mh"])) and np.all(r["Mh"] > 0)
     assert np.all((r["posh"] >= 0) & (r["posh"] < 128.0))
+
+
+def test_ladder_matches_numpy_restatement(orc, pk):
+    """The oracle ladder against an independent numpy irfftn of W(kR) delta_k."""
+    k, P = pk
+    nd, Lc = 32, 4.0
+    p = orc.make_params(nd, Lc, seed=3)
+    modes = orc.field_modes(p, k, P, stream=1)
+    dk = modes[..., 0] + 1j * modes[..., 1]
+    R = np.array([4.0, 9.0, 20.0], dtype=np.float32)
+    kf = 2 * np.pi / (nd * Lc)
+    f = np.fft.fftfreq(nd, 1.0 / nd)
+    fz = np.arange(nd // 2 + 1, dtype=np.float64)
+    fz[-1] = -(nd // 2)
+    kk = kf * np.sqrt(f[:, None, None] ** 2 + f[None, :, None] ** 2 + fz[None, None, :] ** 2)
+    fields = []
+    for r in R:
+        x = kk * float(r)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            w = np.where(x > 0, 3 * (np.sin(x) - x * np.cos(x)) / np.where(x > 0, x, 1) ** 3, 1.0)
+        fields.append(np.fft.irfftn(dk * w, s=(nd, nd, nd)) * nd ** 3 * p.Normx_d)
+    # barriers at the 90th percentile of each smoothed field
+    B = np.array([np.percentile(fl, 90) for fl in fields], dtype=np.float32)
+    want = np.full((nd, nd, nd), 255, dtype=np.uint8)
+    for i in range(len(R) - 1, -1, -1):
+        want[(want == 255) & (fields[i] >= float(B[i]))] = i
+    got = orc.ladder(p, modes, R, B)
+    assert np.mean(got != want) < 1e-4
+    assert np.mean(got == 2) > 0.05
