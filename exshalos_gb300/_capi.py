@@ -39,6 +39,10 @@ class HaloParams(C.Structure):
     ]
 
 
+class BatchItem(C.Structure):
+    _fields_ = [("nd", C.c_int), ("seed", C.c_int)]
+
+
 # every symbol the header declares, with its argument and result types
 _P = C.c_void_p
 SIGNATURES = {
@@ -58,6 +62,8 @@ SIGNATURES = {
     "exh_halos_fetch": (C.c_int, [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, C.c_int, _P]),
     "exh_halo_tables": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), _P, _P, _P, _P]),
     "exh_density_grid_compute": (C.c_int, [_P, _P, _P, C.c_int, C.POINTER(HaloParams), _P, C.c_int, _P]),
+    "exh_batch_run": (C.c_int, [_P, _P, _P, C.c_int, C.POINTER(HaloParams), _P, C.c_int, C.c_int, C.c_int, _P, _P,
+                                _P, _P, _P]),
     "exh_smoothing_ladder": (C.c_int, [_P, _P, _P, C.c_int, C.POINTER(HaloParams), C.c_int, C.c_float, _P, _P, _P,
                                        C.c_int, _P]),
     "exh_fft_r2c_3d": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P]),

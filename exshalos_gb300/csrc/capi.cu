@@ -78,6 +78,10 @@ int exh_ctx_destroy(exh_ctx* ctx) {
   if (!ctx) return EXH_OK;
   cudaSetDevice(ctx->c.device);
   cudaDeviceSynchronize();
+  for (size_t i = 0; i < ctx->c.lane_ctx.size(); i++) {
+    exh_ctx_destroy(ctx->c.lane_ctx[i]);
+    cudaStreamDestroy(ctx->c.lane_st[i]);
+  }
   for (auto& kv : ctx->c.plans) fft_plan_destroy(&kv.second);
   for (int i = 0; i < B_COUNT; i++) ctx->c.buf[i].release();
   halo_state_release(ctx->c);

@@ -66,12 +66,14 @@ enum BufId {
   B_VEL,          // velocity planes [3][ng]
   B_CROSS,        // first-crossing map staging (u8 per cell)
   B_LADDER,       // Fourier modes kept for the smoothing ladder (float2[nk])
+  B_CICACC,       // CIC fixed-point accumulator (u64 per cell)
   B_FLAG,         // int32 halo flag per cell
   B_PEAKS,        // peak keys/ids (sort ping-pong)
   B_PEAKS2,
   B_SORT,         // sort scratch
   B_HALO,         // halo records
   B_HALO2,
+  B_HALO3,        // growth hand-off lists
   B_POSH,         // halo positions / velocities
   B_MH,
   B_TAB,          // device copies of tables
@@ -96,6 +98,9 @@ struct Ctx {
   int shell_ncells = -1, shell_nmin = -1, shell_gmax = 0;   // shell offsets (B_HALO2)
   size_t shell_ncap = 0, shell_nall = 0;
   std::string mass_key;                 // mass-function splines (B_WORK2)
+  // lanes of the batched runner: contexts with their own streams
+  std::vector<exh_ctx*> lane_ctx;
+  std::vector<cudaStream_t> lane_st;
   int get_plan(int nx, int ny, int nz, FFTPlan3D** out);
 };
 

@@ -772,85 +772,256 @@ __device__ int grow_warp_f32(const GrowArgs& A, const int* __restrict__ flag, in
 }
 
 constexpr int GROW_T = 256;   // 8 peaks (one per warp) per block
+constexpr int LANE_GMAX = 6;          // shells one thread grows through (81 cells) before a warp takes over
+constexpr int LANE_COMMIT_MAX = 128;  // reserved cells one thread checks and labels
+constexpr int GROW_PERSIST = EXH_NUM_SMS * 8;   // blocks of the persistent warp passes
 
 __device__ __forceinline__ unsigned resv_key(int tag, int r) { return ((unsigned)tag << 24) | (0xFFFFFFu - (unsigned)r); }
 
-// One round, part 1: every pending peak grows with the flags committed so
-// far (an upper bound of its final reads, since flags are only ever added),
-// keeps the result and reserves the cells up to the shell it read last.
-__global__ void __launch_bounds__(GROW_T)
-k_tentative(GrowArgs A, const int* __restrict__ list, int nlist, unsigned char* __restrict__ state,
-            const int* __restrict__ flag, unsigned* __restrict__ resv, int tag, int* __restrict__ cnt,
-            int* __restrict__ gtmp, int* __restrict__ gexit, int* __restrict__ gst, int* __restrict__ npend,
-            unsigned* __restrict__ nwords) {
-  __shared__ double wb[GROW_T / 32][32];
-  const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+// warp-aggregated append to a device list
+__device__ __forceinline__ void list_push(int* list, int* n, int v) {
+  const unsigned m = __activemask();
   const int lane = threadIdx.x & 31;
-  if (w >= nlist) return;
-  const int r = list[w];
+  const int leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(n, __popc(m));
+  base = __shfl_sync(m, base, leader);
+  list[base + __popc(m & ((1u << lane) - 1u))] = v;
+}
+
+__device__ __forceinline__ void count_push(int* n) {
+  const unsigned m = __activemask();
+  if ((threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(n, __popc(m));
+}
+
+// grow_warp_f32 by one thread for the small spheres that most peaks grow:
+// the shell sums are sequential (bound depth = cells in the shell).  Returns
+// 3 when a comparison is undecided or the growth would pass shell LANE_GMAX;
+// the warp path then redoes the peak from the start.
+__device__ int grow_lane_f32(const GrowArgs& A, const int* __restrict__ flag, int x0, int y0, int z0, float pden,
+                             int& count_out, int& gtmp_out, int& gexit_out) {
+  const HaloScalars& hs = A.hs;
+  FBound den{pden, 0.f}, den_tmp{pden, 0.f};
+  bool rejected = false;
+  int count = 0, count_tmp = 1, grows_tmp = 0, grows = 0;
+  while (true) {
+    int d = rejected ? 0 : fb_ge(den_tmp, hs.Bmin);
+    if (d < 0) return 3;
+    if (!d) break;
+    if (count < count_tmp) grows = grows_tmp;
+    grows_tmp++;
+    den = den_tmp;
+    count = count_tmp;
+    if (count >= hs.Ncells || grows_tmp > A.t.gmax) {
+      count_out = count;
+      gtmp_out = grows_tmp;
+      gexit_out = A.t.gmax;
+      return count >= hs.Ncells ? 1 : 2;
+    }
+    if (grows_tmp > LANE_GMAX) return 3;
+    const int s0 = A.t.start_cap[grows_tmp], s1 = A.t.start_cap[grows_tmp + 1];
+    float sm = 0.f, sa = 0.f;
+    bool foreign = false;
+    for (int q = s0; q < s1; q++) {
+      const size_t cell = cell_at(x0, y0, z0, A.t.off_cap[q], hs);
+      foreign |= flag[cell] != FLAG_FREE;
+      const float v = A.delta[cell];
+      sm += v;
+      sa += fabsf(v);
+    }
+    const int n = s1 - s0;
+    count_tmp += n;
+    if (foreign) { rejected = true; continue; }
+    den_tmp = fb_update(den, count, sm, sa, n + 5, n, count_tmp, 1.f);
+  }
+  const int gexit = grows_tmp;
+  while (count > 0) {
+    const int d = fb_ge(den, A.Btab[count]);
+    if (d < 0) return 3;
+    if (d == 1) break;
+    count_tmp = count;
+    const int s0 = A.t.start_cap[grows], s1 = A.t.start_cap[grows + 1];
+    float sm = 0.f, sa = 0.f;
+    for (int q = s0; q < s1; q++) {
+      const float v = A.delta[cell_at(x0, y0, z0, A.t.off_cap[q], hs)];
+      sm += v;
+      sa += fabsf(v);
+    }
+    const int n = s1 - s0;
+    count -= n;
+    if (count > 0) den = fb_update(den, count_tmp, sm, sa, n + 5, n, count, -1.f);
+    if (count < count_tmp) grows_tmp = grows;
+    grows--;
+  }
+  count_out = count;
+  gtmp_out = grows_tmp;
+  gexit_out = gexit;
+  return 0;
+}
+
+struct RoundArgs {
+  unsigned char* state;
+  int* flag;
+  unsigned* resv;
+  int tag;
+  int* cnt;
+  int* gtmp;
+  int* gexit;
+  int* gst;
+  int* gfin;
+  int* npend;       // peaks grown this round (progress output only)
+  int* err;
+  int* next;        // peaks left for the next round
+  int* nnext;
+  int* wlist;       // peaks handed to the warp growth pass
+  int* nw;
+  int* clist;       // peaks handed to the warp commit pass
+  int* nc;
+  unsigned* nwords; // 4-byte words touched per peak (timing only) or null
+};
+
+__device__ __forceinline__ unsigned tentative_words(const GrowArgs& A, int ge) {
+  // cells read by the growth (density + label) and reserved (read + atomic)
+  return 2u * (A.t.start_cap[min(ge, A.t.gmax) + 1] - A.t.start_cap[1]) + 2u * A.t.start_all[ge + 1] + 2u;
+}
+
+// One round, part 1 (one thread per pending peak): every pending peak grows
+// with the flags committed so far (an upper bound of its final reads, since
+// flags are only ever added), keeps the result and reserves the cells up to
+// the shell it read last.  Peaks with larger spheres, or a comparison too
+// close to call in FP32, go to the warp pass.
+__global__ void __launch_bounds__(GROW_T)
+k_tentative(GrowArgs A, const int* __restrict__ list, int nlist, RoundArgs R) {
+  const int t = (int)(blockIdx.x * (size_t)blockDim.x + threadIdx.x);
+  if (t >= nlist) return;
+  const int r = list[t];
   const int64_t l = A.np - 1 - r;
   const unsigned cell0 = A.id[l];
-  if (flag[cell0] != FLAG_FREE) {        // find_halos.c:233: the peak is already inside a halo
-    if (lane == 0) { state[r] = 1; cnt[r] = 0; }
+  if (R.flag[cell0] != FLAG_FREE) {        // find_halos.c:233: the peak is already inside a halo
+    R.state[r] = 1;
+    R.cnt[r] = 0;
     return;
   }
-  if (lane == 0) atomicAdd(npend, 1);
+  count_push(R.npend);
   int x, y, z;
   peak_coords(cell0, A.hs, x, y, z);
   int count, gt, ge;
-  int st = grow_warp_f32(A, flag, x, y, z, A.key[l], lane, count, gt, ge);
-  if (st == 3) st = grow_warp(A, flag, x, y, z, A.key[l], lane, wb[threadIdx.x >> 5], count, gt, ge);
-  if (lane == 0) { cnt[r] = count; gtmp[r] = gt; gexit[r] = ge; gst[r] = st; }
-  if (lane == 0 && nwords)   // 4-byte words: cells read by the growth (density + label), reserved (read + atomic)
-    nwords[r] += 2u * (A.t.start_cap[min(ge, A.t.gmax) + 1] - A.t.start_cap[1]) + 2u * A.t.start_all[ge + 1] + 2u;
-  const unsigned key = resv_key(tag, r);
+  const int st = grow_lane_f32(A, R.flag, x, y, z, A.key[l], count, gt, ge);
+  if (st == 3) {
+    list_push(R.wlist, R.nw, r);
+    return;
+  }
+  R.cnt[r] = count; R.gtmp[r] = gt; R.gexit[r] = ge; R.gst[r] = st;
+  if (R.nwords) R.nwords[r] += tentative_words(A, ge);
+  const unsigned key = resv_key(R.tag, r);
   const int e = A.t.start_all[ge + 1];
-  for (int q = lane; q < e; q += 32) {
-    unsigned* pr = &resv[cell_at(x, y, z, A.t.off_all[q], A.hs)];
+  for (int q = 0; q < e; q++) {
+    unsigned* pr = &R.resv[cell_at(x, y, z, A.t.off_all[q], A.hs)];
     if (*pr < key) atomicMax(pr, key);
   }
 }
 
-// One round, part 2: peaks that hold every cell they read keep their
-// tentative result (no pending peak of higher rank can change those cells)
-// and write their flags.
+// part 1, warp pass over the peaks the thread pass handed on (persistent)
 __global__ void __launch_bounds__(GROW_T)
-k_commit(GrowArgs A, const int* __restrict__ list, int nlist, int* __restrict__ next, int* __restrict__ nnext,
-         unsigned char* __restrict__ state, int* __restrict__ flag, const unsigned* __restrict__ resv, int tag,
-         const int* __restrict__ cnt, const int* __restrict__ gtmp, const int* __restrict__ gexit,
-         const int* __restrict__ gst, int* __restrict__ gfin, int* __restrict__ err,
-         unsigned* __restrict__ nwords) {
-  const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+k_tentative_warp(GrowArgs A, RoundArgs R) {
+  __shared__ double wb[GROW_T / 32][32];
   const int lane = threadIdx.x & 31;
-  if (w >= nlist) return;
-  const int r = list[w];
-  if (state[r]) return;                   // resolved by the centre test this round
-  const int64_t l = A.np - 1 - r;
-  const unsigned cell0 = A.id[l];
+  const int nwarps = (int)((gridDim.x * (size_t)blockDim.x) >> 5);
+  const int n = *R.nw;
+  for (int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5); w < n; w += nwarps) {
+    const int r = R.wlist[w];
+    const int64_t l = A.np - 1 - r;
+    const unsigned cell0 = A.id[l];
+    int x, y, z;
+    peak_coords(cell0, A.hs, x, y, z);
+    int count, gt, ge;
+    int st = grow_warp_f32(A, R.flag, x, y, z, A.key[l], lane, count, gt, ge);
+    if (st == 3) st = grow_warp(A, R.flag, x, y, z, A.key[l], lane, wb[threadIdx.x >> 5], count, gt, ge);
+    if (lane == 0) { R.cnt[r] = count; R.gtmp[r] = gt; R.gexit[r] = ge; R.gst[r] = st; }
+    if (lane == 0 && R.nwords) R.nwords[r] += tentative_words(A, ge);
+    const unsigned key = resv_key(R.tag, r);
+    const int e = A.t.start_all[ge + 1];
+    for (int q = lane; q < e; q += 32) {
+      unsigned* pr = &R.resv[cell_at(x, y, z, A.t.off_all[q], A.hs)];
+      if (*pr < key) atomicMax(pr, key);
+    }
+  }
+}
+
+// the commit of a peak that holds every cell it read: the tentative result
+// stands (no pending peak of higher rank can change those cells)
+__device__ __forceinline__ bool commit_status(const RoundArgs& R, int r) {
+  const int st = R.gst[r];
+  if (st) {
+    atomicMax(R.err, st);
+    R.state[r] = 1;
+    return false;
+  }
+  R.state[r] = 1;
+  R.gfin[r] = R.gtmp[r];
+  return R.cnt[r] != 0;                  // find_halos.c:339-340
+}
+
+// One round, part 2 (one thread per pending peak with at most
+// LANE_COMMIT_MAX reserved cells; the others go to the warp pass)
+__global__ void __launch_bounds__(GROW_T)
+k_commit(GrowArgs A, const int* __restrict__ list, int nlist, RoundArgs R) {
+  const int t = (int)(blockIdx.x * (size_t)blockDim.x + threadIdx.x);
+  if (t >= nlist) return;
+  const int r = list[t];
+  if (R.state[r]) return;                // resolved by the centre test this round
+  const int e = A.t.start_all[R.gexit[r] + 1];
+  if (e > LANE_COMMIT_MAX) {
+    list_push(R.clist, R.nc, r);
+    return;
+  }
+  const unsigned cell0 = A.id[A.np - 1 - r];
   int x, y, z;
   peak_coords(cell0, A.hs, x, y, z);
-  const unsigned key = resv_key(tag, r);
-  const int e = A.t.start_all[gexit[r] + 1];
+  const unsigned key = resv_key(R.tag, r);
   bool mine = true;
-  for (int q = lane; q < e && mine; q += 32) mine = resv[cell_at(x, y, z, A.t.off_all[q], A.hs)] == key;
-  if (lane == 0 && nwords) nwords[r] += (unsigned)e;
-  if (!__all_sync(0xffffffffu, mine)) {   // still pending: next round
-    if (lane == 0) next[atomicAdd(nnext, 1)] = r;
+  for (int q = 0; q < e && mine; q++) mine = R.resv[cell_at(x, y, z, A.t.off_all[q], A.hs)] == key;
+  if (R.nwords) R.nwords[r] += (unsigned)e;
+  if (!mine) {
+    list_push(R.next, R.nnext, r);
     return;
   }
-  const int st = gst[r];
-  if (st) {
-    if (lane == 0) { atomicMax(err, st); state[r] = 1; }
-    return;
+  if (!commit_status(R, r)) return;
+  const int we = A.t.start_all[R.gtmp[r]];     // cells with r^2 < grows_tmp
+  for (int q = 0; q < we; q++) R.flag[cell_at(x, y, z, A.t.off_all[q], A.hs)] = r;
+  if (R.nwords) R.nwords[r] += (unsigned)we;
+  R.flag[cell0] = -(r + 2);
+}
+
+// part 2, warp pass (persistent) over the peaks handed on by k_commit
+__global__ void __launch_bounds__(GROW_T)
+k_commit_warp(GrowArgs A, RoundArgs R) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (int)((gridDim.x * (size_t)blockDim.x) >> 5);
+  const int n = *R.nc;
+  for (int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5); w < n; w += nwarps) {
+    const int r = R.clist[w];
+    const unsigned cell0 = A.id[A.np - 1 - r];
+    int x, y, z;
+    peak_coords(cell0, A.hs, x, y, z);
+    const unsigned key = resv_key(R.tag, r);
+    const int e = A.t.start_all[R.gexit[r] + 1];
+    bool mine = true;
+    for (int q = lane; q < e && mine; q += 32) mine = R.resv[cell_at(x, y, z, A.t.off_all[q], A.hs)] == key;
+    if (lane == 0 && R.nwords) R.nwords[r] += (unsigned)e;
+    if (!__all_sync(0xffffffffu, mine)) {
+      if (lane == 0) R.next[atomicAdd(R.nnext, 1)] = r;
+      continue;
+    }
+    bool keep = false;
+    if (lane == 0) keep = commit_status(R, r);
+    if (!__shfl_sync(0xffffffffu, (int)keep, 0)) continue;
+    const int we = A.t.start_all[R.gtmp[r]];
+    for (int q = lane; q < we; q += 32) R.flag[cell_at(x, y, z, A.t.off_all[q], A.hs)] = r;
+    if (lane == 0 && R.nwords) R.nwords[r] += (unsigned)we;
+    __syncwarp();
+    if (lane == 0) R.flag[cell0] = -(r + 2);
   }
-  const int count = cnt[r], gt = gtmp[r];
-  if (lane == 0) { state[r] = 1; gfin[r] = gt; }
-  if (count == 0) return;                 // find_halos.c:339-340
-  const int we = A.t.start_all[gt];       // cells with r^2 < grows_tmp
-  for (int q = lane; q < we; q += 32) flag[cell_at(x, y, z, A.t.off_all[q], A.hs)] = r;
-  if (lane == 0 && nwords) nwords[r] += (unsigned)we;
-  __syncwarp();
-  if (lane == 0) flag[cell0] = -(r + 2);
 }
 
 __global__ void k_sum_words(const unsigned* __restrict__ w, int n, unsigned long long* __restrict__ out) {
@@ -947,12 +1118,17 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   // kept = growth status; both are rewritten after the rounds
   int* gexit = h->gfree;
   int* gst = kept;
-  // device counters: [0] pending this round, [1] error
+  // device counters: [0] pending this round, [1] error, [2] next list,
+  // [3] warp growth list, [4] warp commit list, [6..7] byte total (timing)
   EXH_TRY(c.buf[B_HOSTIO2].ensure(64));
   int* dcnt = c.buf[B_HOSTIO2].as<int>();
   // pending peaks as a compacted list (misc and hid serve as the two lists
-  // during the rounds; both are rewritten afterwards)
+  // during the rounds; both are rewritten afterwards); the warp passes'
+  // lists live in the hand-off buffer
   int* lists[2] = {misc, h->hid};
+  EXH_TRY(c.buf[B_HALO3].ensure(sizeof(int) * 2 * npr));
+  int* wlist = c.buf[B_HALO3].as<int>();
+  int* clist = wlist + npr;
   k_iota<<<nb, 128, 0, st>>>(lists[0], (int)nproc);
   count_launch(1);
   int nlist = (int)nproc, cur = 0;
@@ -964,13 +1140,18 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
     const int tag = (round % 255) + 1;
     if (round > 0 && tag == 1) EXH_CUDA_TRY(cudaMemsetAsync(h->resv, 0, sizeof(unsigned) * ng, st));
     EXH_CUDA_TRY(cudaMemsetAsync(dcnt, 0, sizeof(int) * 6, st));
-    unsigned* dwords = timing_on() ? h->words : nullptr;
-    const unsigned nbl = exh_div_up((size_t)nlist * 32, GROW_T);
-    k_tentative<<<nbl, GROW_T, 0, st>>>(A, lists[cur], nlist, h->state, h->flag, h->resv, tag, h->cnt, h->gfin, gexit,
-                                        gst, dcnt, dwords);
-    k_commit<<<nbl, GROW_T, 0, st>>>(A, lists[cur], nlist, lists[cur ^ 1], dcnt + 2, h->state, h->flag, h->resv, tag,
-                                     h->cnt, h->gfin, gexit, gst, h->gfin, dcnt + 1, dwords);
-    count_launch(2);
+    RoundArgs R;
+    R.state = h->state; R.flag = h->flag; R.resv = h->resv; R.tag = tag;
+    R.cnt = h->cnt; R.gtmp = h->gfin; R.gexit = gexit; R.gst = gst; R.gfin = h->gfin;
+    R.npend = dcnt; R.err = dcnt + 1; R.next = lists[cur ^ 1]; R.nnext = dcnt + 2;
+    R.wlist = wlist; R.nw = dcnt + 3; R.clist = clist; R.nc = dcnt + 4;
+    R.nwords = timing_on() ? h->words : nullptr;
+    const unsigned nbl = exh_div_up((size_t)nlist, GROW_T);
+    k_tentative<<<nbl, GROW_T, 0, st>>>(A, lists[cur], nlist, R);
+    k_tentative_warp<<<std::min<unsigned>(GROW_PERSIST, exh_div_up((size_t)nlist * 32, GROW_T)), GROW_T, 0, st>>>(A, R);
+    k_commit<<<nbl, GROW_T, 0, st>>>(A, lists[cur], nlist, R);
+    k_commit_warp<<<std::min<unsigned>(GROW_PERSIST, exh_div_up((size_t)nlist * 32, GROW_T)), GROW_T, 0, st>>>(A, R);
+    count_launch(4);
     EXH_CUDA_TRY(cudaGetLastError());
     int hc[6];
     EXH_CUDA_TRY(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
@@ -993,7 +1174,7 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   }
   if (timing_on()) {
     // algorithmic bytes of the growth rounds: one reduction over the peaks
-    unsigned long long* dsum = reinterpret_cast<unsigned long long*>(dcnt + 4);
+    unsigned long long* dsum = reinterpret_cast<unsigned long long*>(dcnt + 6);
     EXH_CUDA_TRY(cudaMemsetAsync(dsum, 0, sizeof(unsigned long long), st));
     k_sum_words<<<EXH_NUM_SMS, 256, 0, st>>>(h->words, (int)nproc, dsum);
     count_launch(1);
@@ -1172,9 +1353,8 @@ __global__ void k_masses(const TausJump* __restrict__ J, TausState s0, DevSpline
 int halo_masses(Ctx& c, const BoxParams& b, const HaloDev& h, const HostTables& tab, float* Mh_dev, int* count_dev,
                 int* xc_dev, cudaStream_t st) {
   if (h.nh == 0) return EXH_OK;
-  static TausJump J;
-  static bool J_ready = false;
-  if (!J_ready) { taus_jump_tables(&J); J_ready = true; }
+  // built once per process; the initialisation of a local static is thread-safe
+  static const TausJump J = [] { TausJump t; taus_jump_tables(&t); return t; }();
   TausState s0;
   taus_seed_state((unsigned long)b.seed, s0.s);
   const std::vector<int>& sph = cells_in_spheres();

@@ -253,8 +253,9 @@ int amplitude_table(const BoxParams& b, const float* K, const float* P, int Nk, 
 }
 
 const std::vector<int>& cells_in_spheres() {
-  static std::vector<int> tab;
-  if (tab.empty()) {
+  // built once per process (thread-safe local static initialisation)
+  static const std::vector<int> tab = [] {
+    std::vector<int> tab;
     const int lmax = 10000, t = 100;
     std::vector<long> hist(lmax, 0);
     for (int i = -t; i <= t; i++)
@@ -266,7 +267,8 @@ const std::vector<int>& cells_in_spheres() {
     long cum = 0;
     for (int l = 0; l < lmax; l++)
       if (hist[l]) { cum += hist[l]; tab.push_back((int)cum); }
-  }
+    return tab;
+  }();
   return tab;
 }
 

@@ -19,8 +19,22 @@ namespace exh {
 // ------------------------------------------------------------------ CIC
 // One thread per tracer: the periodic wrap of spectrum_h.c:17-27, the cell
 // index of spectrum_h.c:73-80 and the eight weights of gridmodule.c:29-50.
+//
+// The weights are accumulated in 64-bit fixed point (quanta of 2^-40, one
+// rounding per weight) with integer atomics.  Integer addition is
+// associative, so the grid does not depend on the order in which threads
+// land: every run, every stream schedule and every batch gives the same
+// bits.  Each cell is rounded to float once, from the exact fixed-point sum.
+// Range: 2^23 tracers in one cell before the 64-bit sum overflows.
+constexpr double CIC_Q = 1099511627776.0;        // 2^40
+constexpr double CIC_INV_Q = 1.0 / 1099511627776.0;
+
+__device__ __forceinline__ void cic_add(unsigned long long* g, float w) {
+  atomicAdd(g, __double2ull_rn((double)w * CIC_Q));
+}
+
 __global__ void k_cic(const float* __restrict__ pos, int64_t np, int nd, float L, float Ld,
-                      float* __restrict__ grid) {
+                      unsigned long long* __restrict__ acc) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (p >= np) return;
   int xt[3], sg[3];
@@ -45,37 +59,44 @@ __global__ void k_cic(const float* __restrict__ pos, int64_t np, int nd, float L
   const int x0 = xt[0], y0 = xt[1], z0 = xt[2];
   const int x1 = exh_wrap(x0, sg[0], nd), y1 = exh_wrap(y0, sg[1], nd), z1 = exh_wrap(z0, sg[2], nd);
   const size_t n2 = (size_t)nd * nd;
-  atomicAdd(&grid[x0 * n2 + (size_t)y0 * nd + z0], t[0] * t[1] * t[2]);
-  atomicAdd(&grid[x1 * n2 + (size_t)y0 * nd + z0], dx[0] * t[1] * t[2]);
-  atomicAdd(&grid[x0 * n2 + (size_t)y1 * nd + z0], t[0] * dx[1] * t[2]);
-  atomicAdd(&grid[x0 * n2 + (size_t)y0 * nd + z1], t[0] * t[1] * dx[2]);
-  atomicAdd(&grid[x1 * n2 + (size_t)y1 * nd + z0], dx[0] * dx[1] * t[2]);
-  atomicAdd(&grid[x1 * n2 + (size_t)y0 * nd + z1], dx[0] * t[1] * dx[2]);
-  atomicAdd(&grid[x0 * n2 + (size_t)y1 * nd + z1], t[0] * dx[1] * dx[2]);
-  atomicAdd(&grid[x1 * n2 + (size_t)y1 * nd + z1], dx[0] * dx[1] * dx[2]);
+  cic_add(&acc[x0 * n2 + (size_t)y0 * nd + z0], t[0] * t[1] * t[2]);
+  cic_add(&acc[x1 * n2 + (size_t)y0 * nd + z0], dx[0] * t[1] * t[2]);
+  cic_add(&acc[x0 * n2 + (size_t)y1 * nd + z0], t[0] * dx[1] * t[2]);
+  cic_add(&acc[x0 * n2 + (size_t)y0 * nd + z1], t[0] * t[1] * dx[2]);
+  cic_add(&acc[x1 * n2 + (size_t)y1 * nd + z0], dx[0] * dx[1] * t[2]);
+  cic_add(&acc[x1 * n2 + (size_t)y0 * nd + z1], dx[0] * t[1] * dx[2]);
+  cic_add(&acc[x0 * n2 + (size_t)y1 * nd + z1], t[0] * dx[1] * dx[2]);
+  cic_add(&acc[x1 * n2 + (size_t)y1 * nd + z1], dx[0] * dx[1] * dx[2]);
 }
 
-// delta = rho / (np / ng) - 1   (gridmodule.c:206-211)
-__global__ void k_cic_normalise(float* __restrict__ grid, size_t ng, float inv_mean) {
+// rho = fixed-point sum rounded to float; delta = rho / (np / ng) - 1
+// (gridmodule.c:206-211)
+__global__ void k_cic_normalise(const unsigned long long* __restrict__ acc, float* __restrict__ grid, size_t ng,
+                                float inv_mean) {
   size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (; i < ng; i += stride) grid[i] = grid[i] * inv_mean - 1.f;
+  for (; i < ng; i += stride) {
+    const float rho = (float)((double)acc[i] * CIC_INV_Q);
+    grid[i] = rho * inv_mean - 1.f;
+  }
 }
 
 int cic_assign(Ctx& c, const float* pos_dev, int64_t np, int nd, float L, float* grid_dev, cudaStream_t st) {
   const size_t ng = (size_t)nd * nd * nd;
-  EXH_CUDA_TRY(cudaMemsetAsync(grid_dev, 0, sizeof(float) * ng, st));
+  EXH_TRY(c.buf[B_CICACC].ensure(sizeof(unsigned long long) * ng));
+  unsigned long long* acc = c.buf[B_CICACC].as<unsigned long long>();
+  EXH_CUDA_TRY(cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * ng, st));
   const float Ld = L / (float)nd;
   if (np > 0) {
-    KTimer kt(KC_CIC, st, 12.0 * np + 32.0 * np);
-    k_cic<<<exh_div_up(np, 256), 256, 0, st>>>(pos_dev, np, nd, L, Ld, grid_dev);
+    KTimer kt(KC_CIC, st, 12.0 * np + 64.0 * np);
+    k_cic<<<exh_div_up(np, 256), 256, 0, st>>>(pos_dev, np, nd, L, Ld, acc);
     count_launch(1);
     EXH_CUDA_TRY(cudaGetLastError());
   }
   // np == 0 gives 0/0 in the reference; the grid is returned as -1 + nan there.
   const float inv_mean = np > 0 ? (float)((double)ng / (double)np) : NAN;
-  { KTimer kt(KC_CIC, st, 8.0 * ng);
-  k_cic_normalise<<<EXH_NUM_SMS * 8, 256, 0, st>>>(grid_dev, ng, inv_mean); }
+  { KTimer kt(KC_CIC, st, 12.0 * ng);
+  k_cic_normalise<<<EXH_NUM_SMS * 8, 256, 0, st>>>(acc, grid_dev, ng, inv_mean); }
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   return EXH_OK;

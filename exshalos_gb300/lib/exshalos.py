@@ -155,6 +155,38 @@ def smoothing_ladder(k, P, R_max, Ndx, Ndy, Ndz, Lc, seed=12345, n_radii=50, Om0
     return {"cross": cross, "R": R, "B": B}
 
 
+def batch_run(k, P, nds, seeds, Lc=2.0, Nk_pk=64, lanes=8, **params):
+    """Halos and the 64-bin (Nk_pk) CIC power spectrum of the halos for many
+    boxes of uneven size, each from its own Philox seed, scheduled over
+    ``lanes`` streams (1 = the plain loop).  ``params`` are fields of the
+    halo parameters shared by every box (Om0, DO_2LPT, a, beta, ...).
+
+    Returns {"nh": i64[n], "k": f32[n, Nk_pk], "Pk": f32[n, Nk_pk], "Nk": i64[n, Nk_pk],
+    "status": i32[n]}: a box whose halo masses leave the mass-function
+    tables (where the reference aborts) has status 4 (EXH_E_RANGE) and nh -1;
+    the others still run.
+    """
+    k = np.ascontiguousarray(k, dtype=np.float32)
+    P = np.ascontiguousarray(P, dtype=np.float32)
+    nds = np.asarray(nds, dtype=np.int64).ravel()
+    seeds = np.asarray(seeds, dtype=np.int64).ravel()
+    if nds.shape != seeds.shape:
+        raise ValueError("nds and seeds must have the same length")
+    n = nds.size
+    items = (_capi.BatchItem * max(n, 1))()
+    for i in range(n):
+        items[i].nd = int(nds[i])
+        items[i].seed = int(seeds[i])
+    prm = _params(Lc=float(Lc), **params)
+    out = {"nh": np.zeros(n, dtype=np.int64), "k": np.zeros((n, Nk_pk), dtype=np.float32),
+           "Pk": np.zeros((n, Nk_pk), dtype=np.float32), "Nk": np.zeros((n, Nk_pk), dtype=np.int64),
+           "status": np.zeros(n, dtype=np.int32)}
+    _capi.check(_capi.load().exh_batch_run(_capi.context(), _capi.ptr(k), _capi.ptr(P), k.size, prm, items, n,
+                                           int(Nk_pk), int(lanes), _capi.ptr(out["nh"]), _capi.ptr(out["k"]),
+                                           _capi.ptr(out["Pk"]), _capi.ptr(out["Nk"]), _capi.ptr(out["status"])))
+    return out
+
+
 def halo_tables():
     """Sigma(M), barrier and mass-function tables of the last halo call."""
     import ctypes as C

@@ -158,6 +158,31 @@ int exh_smoothing_ladder(exh_ctx *ctx, const float *k, const float *P, int Nk, c
                          int n_radii, float R_max, uint8_t *cross, float *radii_out, float *barrier_out,
                          int mem, void *stream);
 
+/* Batched realisations.  Each item is one cubic box of nd cells per side
+ * (cell size base->Lc) from its own Philox seed; every other parameter comes
+ * from base.  Per item: the halos of exh_halos_box_from_pk
+ * (Generate_Halos_Box_from_Pk, pyexshalos/mock.py:11-39), their CIC grid
+ * (Compute_Density_Grid, pyexshalos/simulation.py:9-26) and its power
+ * spectrum with the CIC window in Nk_pk bins from 2 pi / L to pi nd / L
+ * (Compute_Power_Spectrum, pyexshalos/simulation.py:170-184).  Outputs (host):
+ * nh_out[n], and k_out, P_out, count_out of n * Nk_pk entries, item-major.
+ * status_out (n entries, may be NULL) receives each item's status; with it,
+ * an item whose halo masses leave the mass-function tables (EXH_E_RANGE,
+ * where the reference's spline evaluation aborts) gets nh_out = -1 and the
+ * batch goes on.  Without it, or on any other error, the first failing item
+ * stops the batch and its status is returned.
+ * The items run on `lanes` library contexts with their own streams and host
+ * threads (1 = the plain loop); the results do not depend on the lane count.
+ * Synchronous: returns when every item is done. */
+typedef struct {
+  int nd;    /* cells per side */
+  int seed;  /* Philox seed of the field */
+} exh_batch_item;
+
+int exh_batch_run(exh_ctx *ctx, const float *k, const float *P, int Nk, const exh_halo_params *base,
+                  const exh_batch_item *items, int n, int Nk_pk, int lanes, int64_t *nh_out, float *k_out,
+                  float *P_out, int64_t *count_out, int32_t *status_out);
+
 /* 3-D FFTs with FFTW conventions (unnormalised, half-complex last axis,
  * interleaved float2) — the transforms fftwf_plan_dft_r2c_3d /
  * fftwf_plan_dft_c2r_3d perform at src/spectrum/spectrum_h.c:103-107 and
