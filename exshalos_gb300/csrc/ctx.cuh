@@ -66,6 +66,7 @@ enum BufId {
   B_VEL,          // velocity planes [3][ng]
   B_CROSS,        // first-crossing map staging (u8 per cell)
   B_LADDER,       // Fourier modes kept for the smoothing ladder (float2[nk])
+  B_LADDERW,      // ladder window table W(kR) per radius and |n|^2
   B_CICACC,       // CIC fixed-point accumulator (u64 per cell)
   B_FLAG,         // int32 halo flag per cell
   B_PEAKS,        // peak keys/ids (sort ping-pong)
@@ -98,6 +99,7 @@ struct Ctx {
   int shell_ncells = -1, shell_nmin = -1, shell_gmax = 0;   // shell offsets (B_HALO2)
   size_t shell_ncap = 0, shell_nall = 0;
   std::string mass_key;                 // mass-function splines (B_WORK2)
+  std::string ladder_key;               // ladder window table (B_LADDERW)
   // lanes of the batched runner: contexts with their own streams
   std::vector<exh_ctx*> lane_ctx;
   std::vector<cudaStream_t> lane_st;

@@ -67,7 +67,7 @@ struct FsShape {
 
 // strided pass over data [outer][n][inner]: tile of W adjacent columns
 template <int N1, int N2, class Src, class Dst>
-__global__ void __launch_bounds__(FS_THREADS)
+__global__ void __launch_bounds__(FS_THREADS, 4)
 k_fft4_strided(Src src, Dst dst, const float2* __restrict__ tw, float sgn, int inner) {
   using S = FsShape<N1, N2>;
   constexpr int W = S::W;
@@ -100,12 +100,27 @@ k_fft4_strided(Src src, Dst dst, const float2* __restrict__ tw, float sgn, int i
   }
 }
 
+// Row stride (float2) of the row kernels' shared memory: room for the
+// padded intermediate of fs_rows_smem, and == 8 (mod 16) so that the 4 or 2
+// rows a warp touches at once fall on disjoint bank pairs.
+template <int N1, int N2>
+struct FsRows {
+  static constexpr int M = N1 * N2;
+  static constexpr int PAD = (N2 % 2 == 0) ? 1 : 0;   // odd group stride: conflict-free columns
+  static constexpr int NEED = (N1 * (N2 + PAD) > M + 1) ? N1 * (N2 + PAD) : M + 1;
+  static constexpr int LDA = NEED + ((8 - NEED % 16) + 16) % 16;
+};
+
 // Four-step transform of R rows of length M = N1 N2 held in shared memory
-// a[b * lda + m]; result in natural order in the same place.
+// a[b * lda + m]; result in natural order in the same place.  The
+// intermediate (after the twiddles) is stored with one float2 of padding
+// per group of N2, so the column reads of the second step hit distinct
+// banks.
 template <int N1, int N2>
 __device__ __forceinline__ void fs_rows_smem(float2* a, int lda, const float2* __restrict__ twM, float sgn) {
   using S = FsShape<N1, N2>;
   constexpr int R = S::R;
+  constexpr int G = N2 + FsRows<N1, N2>::PAD;
   float2 v[N1];
   {
     const int b = threadIdx.x / N2, jj = threadIdx.x % N2;
@@ -120,7 +135,7 @@ __device__ __forceinline__ void fs_rows_smem(float2* a, int lda, const float2* _
     __syncthreads();
     if (b < R) {
 #pragma unroll
-      for (int k1 = 0; k1 < N1; k1++) a[b * lda + k1 * N2 + jj] = v[k1];
+      for (int k1 = 0; k1 < N1; k1++) a[b * lda + k1 * G + jj] = v[k1];
     }
     __syncthreads();
   }
@@ -129,7 +144,7 @@ __device__ __forceinline__ void fs_rows_smem(float2* a, int lda, const float2* _
     float2 u[N2];
     if (b < R) {
 #pragma unroll
-      for (int j2 = 0; j2 < N2; j2++) u[j2] = a[b * lda + kk * N2 + j2];
+      for (int j2 = 0; j2 < N2; j2++) u[j2] = a[b * lda + kk * G + j2];
       RDft<N2>::run(u, sgn, [twM](int m) { return __ldg(&twM[m * N1]); });
     }
     __syncthreads();
@@ -146,11 +161,12 @@ template <int N1, int N2, class Src, class Dst>
 __global__ void __launch_bounds__(FS_THREADS)
 k_fft4_r2c_rows(Src src, Dst dst, const float2* __restrict__ twM, const float2* __restrict__ twN, size_t rows) {
   using S = FsShape<N1, N2>;
-  constexpr int M = S::n, R = S::R, LDA = M + 1;
+  constexpr int M = S::n, R = S::R, LDA = FsRows<N1, N2>::LDA;
   extern __shared__ float2 a[];                    // R * LDA
   const size_t r0 = (size_t)blockIdx.x * R;
   const int nb = (int)min((size_t)R, rows - r0);
-  for (int t = threadIdx.x; t < R * M; t += blockDim.x) {
+#pragma unroll
+  for (int t = threadIdx.x; t < R * M; t += FS_THREADS) {
     const int b = t / M, m = t % M;
     a[b * LDA + m] = (b < nb) ? src(r0 + b, m) : make_float2(0.f, 0.f);
   }
@@ -174,12 +190,13 @@ template <int N1, int N2, class Src, class Dst>
 __global__ void __launch_bounds__(FS_THREADS)
 k_fft4_c2r_rows(Src src, Dst dst, const float2* __restrict__ twM, const float2* __restrict__ twN, size_t rows) {
   using S = FsShape<N1, N2>;
-  constexpr int M = S::n, R = S::R, LDA = M + 1, nc = M + 1;
+  constexpr int M = S::n, R = S::R, LDA = FsRows<N1, N2>::LDA, nc = M + 1;
   extern __shared__ float2 x[];                    // 2 * R * LDA
   float2* a = x + R * LDA;
   const size_t r0 = (size_t)blockIdx.x * R;
   const int nb = (int)min((size_t)R, rows - r0);
-  for (int t = threadIdx.x; t < R * nc; t += blockDim.x) {
+#pragma unroll
+  for (int t = threadIdx.x; t < R * nc; t += FS_THREADS) {
     const int b = t / nc, k = t % nc;
     float2 v = (b < nb) ? src(r0 + b, k) : make_float2(0.f, 0.f);
     if (k == 0 || k == M) v.y = 0.f;
@@ -244,7 +261,7 @@ inline bool launch_fs_r2c(Src src, Dst dst, int M, const float2* twM, const floa
   switch (fs_split(M)) {
 #define X(a, b)                                                                               \
   case a * 1000 + b: {                                                                        \
-    const size_t sm = sizeof(float2) * FsShape<a, b>::R * (a * b + 1);                        \
+    const size_t sm = sizeof(float2) * FsShape<a, b>::R * FsRows<a, b>::LDA;                   \
     *err = set_smem(k_fft4_r2c_rows<a, b, Src, Dst>, sm);                                     \
     if (*err != cudaSuccess) return true;                                                     \
     k_fft4_r2c_rows<a, b, Src, Dst><<<exh_div_up(rows, FsShape<a, b>::R), FS_THREADS, sm, st>>>(src, dst, twM, twN, rows); \
@@ -263,7 +280,7 @@ inline bool launch_fs_c2r(Src src, Dst dst, int M, const float2* twM, const floa
   switch (fs_split(M)) {
 #define X(a, b)                                                                               \
   case a * 1000 + b: {                                                                        \
-    const size_t sm = 2 * sizeof(float2) * FsShape<a, b>::R * (a * b + 1);                    \
+    const size_t sm = 2 * sizeof(float2) * FsShape<a, b>::R * FsRows<a, b>::LDA;              \
     *err = set_smem(k_fft4_c2r_rows<a, b, Src, Dst>, sm);                                     \
     if (*err != cudaSuccess) return true;                                                     \
     k_fft4_c2r_rows<a, b, Src, Dst><<<exh_div_up(rows, FsShape<a, b>::R), FS_THREADS, sm, st>>>(src, dst, twM, twN, rows); \

@@ -12,6 +12,7 @@
 // update run in the epilogue of the last pass, so no smoothed field is ever
 // stored.
 #include <cmath>
+#include <string>
 #include <vector>
 
 #include "ctx.cuh"
@@ -33,32 +34,44 @@ __global__ void k_store_modes(FieldModes m, float2* __restrict__ out) {
   }
 }
 
-__device__ __forceinline__ float tophat(float x) {
-  if (x < 1e-2f) {                       // series: 1 - x^2/10 + x^4/280
-    const float x2 = x * x;
-    return 1.f - x2 * (0.1f - x2 * (1.f / 280.f));
+// W(k R) = 3 (sin x - x cos x) / x^3 (exshalos_h.c:35-40) for every radius
+// and every integer |n|^2 of a cubic box, k = kf |n|: computed once per
+// (box, radii) in FP64, where the difference s - x c loses no digits to
+// cancellation at small x, and rounded to float.
+__global__ void k_ladder_wtab(const float* __restrict__ R, int nr, int nn, double kf, float* __restrict__ w) {
+  const size_t total = (size_t)nr * nn;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(t / nn), n2 = (int)(t % nn);
+    const double x = kf * sqrt((double)n2) * (double)R[r];
+    double v;
+    if (x < 1e-3) {
+      const double x2 = x * x;
+      v = 1.0 - x2 * (0.1 - x2 * (1.0 / 280.0));
+    } else {
+      double sn, cs;
+      sincos(x, &sn, &cs);
+      v = 3.0 * (sn - x * cs) / (x * x * x);
+    }
+    w[t] = (float)v;
   }
-  float s, c;
-  sincosf(x, &s, &c);
-  return 3.f * (s - x * c) / (x * x * x);
 }
 
-// x-pass source: stored modes times W(|k| R)
+// x-pass source: stored modes times W(|k| R), W from the table row of R
 struct LadderGen {
   static constexpr int io_bytes = 8;
   const float2* __restrict__ dk;
-  int n0, n1, n2, nc;
-  float kl0, kl1, kl2, R;
+  const float* __restrict__ w;
+  int n0, nc, h;
   __device__ __forceinline__ float2 operator()(int, int e, int inner) const {
     const int j = inner / nc, k = inner % nc;
-    const float kx = (float)((2 * e < n0) ? e : e - n0) * kl0;
-    const float ky = (float)((2 * j < n1) ? j : j - n1) * kl1;
-    const float kz = (float)((k == n2 / 2) ? -(n2 / 2) : k) * kl2;
-    const float w = tophat(sqrtf(kx * kx + ky * ky + kz * kz) * R);
+    const int ii = (2 * e < n0) ? e : e - n0;
+    const int jj = (2 * j < n0) ? j : j - n0;
+    const int kk = (k == h) ? -h : k;
+    const float wv = __ldg(&w[ii * ii + jj * jj + kk * kk]);
     const float2 v = dk[(size_t)e * inner_size() + inner];
-    return make_float2(v.x * w, v.y * w);
+    return make_float2(v.x * wv, v.y * wv);
   }
-  __device__ __forceinline__ size_t inner_size() const { return (size_t)n1 * nc; }
+  __device__ __forceinline__ size_t inner_size() const { return (size_t)n0 * nc; }
 };
 
 // z-pass destination: barrier test, first crossing kept
@@ -91,9 +104,28 @@ int smoothing_ladder(Ctx& c, const BoxParams& b, const FieldModes& modes, int n_
     count_launch(1);
     EXH_CUDA_TRY(cudaGetLastError());
   }
+  // window table, reused while the box and the radii repeat
+  const int h = b.nd[0] / 2, nn = 3 * h * h + 1;
+  std::string key(reinterpret_cast<const char*>(b.nd), sizeof(b.nd));
+  key.append(reinterpret_cast<const char*>(&b.Lc), sizeof(float));
+  key.append(reinterpret_cast<const char*>(R), sizeof(float) * n_radii);
+  EXH_TRY(c.buf[B_LADDERW].ensure(sizeof(float) * ((size_t)n_radii * nn + n_radii)));
+  float* wtab = c.buf[B_LADDERW].as<float>();
+  if (key != c.ladder_key) {
+    c.ladder_key.clear();
+    float* dR = wtab + (size_t)n_radii * nn;
+    EXH_CUDA_TRY(cudaMemcpyAsync(dR, R, sizeof(float) * n_radii, cudaMemcpyHostToDevice, st));
+    const double kf = 2.0 * M_PI / ((double)b.Lc * b.nd[0]);
+    KTimer kt(KC_OTHER, st, 4.0 * n_radii * nn);
+    k_ladder_wtab<<<EXH_NUM_SMS * 8, 256, 0, st>>>(dR, n_radii, nn, kf, wtab);
+    count_launch(1);
+    EXH_CUDA_TRY(cudaGetLastError());
+    EXH_CUDA_TRY(cudaStreamSynchronize(st));    // R is the caller's host array
+    c.ladder_key = key;
+  }
   EXH_CUDA_TRY(cudaMemsetAsync(cross, 255, b.ng, st));
   for (int i = n_radii - 1; i >= 0; i--) {       // large scales first
-    LadderGen gen{dk, b.nd[0], b.nd[1], b.nd[2], p->nc, b.kl[0], b.kl[1], b.kl[2], R[i]};
+    LadderGen gen{dk, wtab + (size_t)i * nn, b.nd[0], p->nc, h};
     CrossStore cs{cross, b.nd[2], b.Normx, B[i], i};
     EXH_CUDA_TRY(fft_c2r_3d(*p, gen, work, cs, st));
   }
