@@ -246,6 +246,41 @@ def batched_summary(k, P, lanes, seed0=0):
             "timing": "host wall clock around the synchronous batch call"}
 
 
+def diff_summary(k, P, reps=3):
+    """Differentiable workload: white noise 256^3 (unit Gaussian, seed 7)
+    scaled by 20 log-spaced P(k) knots, 2LPT, CIC 256^3, 64-bin P(k), chi^2
+    against the seed-8 spectrum; forward and hand-written adjoint timed with
+    CUDA events (median of reps)."""
+    import torch
+    from exshalos_gb300 import diff
+    nd, L = 256, 512.0
+    knot_k, knot_P = diff.knots_from_spectrum(k, P, 20, 2 * np.pi / L, np.sqrt(3) * np.pi * nd / L * 1.01)
+    model = diff.pk_chi2_model(nd, L, knot_k, Nk=64)
+    g8 = torch.Generator(device="cuda").manual_seed(8)
+    w8 = torch.randn((nd, nd, nd), generator=g8, device="cuda", dtype=torch.float32)
+    _, target, _, _ = model.forward(w8, knot_P, np.ones(64, dtype=np.float32))
+    g7 = torch.Generator(device="cuda").manual_seed(7)
+    w = torch.randn((nd, nd, nd), generator=g7, device="cuda", dtype=torch.float32)
+    gw = torch.empty_like(w)
+    fw, bw = [], []
+    for r in range(reps + 1):
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        torch.cuda.synchronize()
+        e0.record()
+        loss, _, _, _ = model.forward(w, knot_P, target)
+        e1.record()
+        model.backward(1.0, gw)
+        e2.record()
+        torch.cuda.synchronize()
+        if r:
+            fw.append(e0.elapsed_time(e1))
+            bw.append(e1.elapsed_time(e2))
+    f, b = float(np.median(fw)), float(np.median(bw))
+    return {"workload": "diff_256: noise 256^3 seed 7, 20 knots, 2LPT, CIC 256^3, P(k) 64 bins, chi^2 vs seed 8",
+            "forward_ms": round(f, 3), "adjoint_ms": round(b, 3), "adjoint_over_forward": round(b / f, 3),
+            "loss": loss}
+
+
 def run_ours(args, ws, rank, local):
     os.environ["EXH_DEVICE"] = str(local)
     import ctypes as C
@@ -343,6 +378,7 @@ def run_ours(args, ws, rank, local):
                             "ms_per_launch": round(cms / cnl, 4)}
     traffic = committed_traffic().get(name)
     batched = None if args.no_batched else batched_summary(k, P, args.lanes, seed0=1000 * rank)
+    differentiable = None if args.no_batched else diff_summary(k, P)
     if rank != 0:
         return
     cpu = None
@@ -373,6 +409,7 @@ def run_ours(args, ws, rank, local):
         "clocks": clk,
         "cpu_baseline": cpu,
         "batched": batched,
+        "differentiable": differentiable,
     }
     print(json.dumps(line), flush=True)
 

@@ -43,6 +43,12 @@ class BatchItem(C.Structure):
     _fields_ = [("nd", C.c_int), ("seed", C.c_int)]
 
 
+class DiffParams(C.Structure):
+    _fields_ = [("nd", C.c_int), ("L", C.c_float), ("Om0", C.c_float), ("redshift", C.c_float),
+                ("do_2lpt", C.c_int), ("n_knots", C.c_int), ("Nk", C.c_int), ("k_min", C.c_float),
+                ("k_max", C.c_float)]
+
+
 # every symbol the header declares, with its argument and result types
 _P = C.c_void_p
 SIGNATURES = {
@@ -64,6 +70,9 @@ SIGNATURES = {
     "exh_density_grid_compute": (C.c_int, [_P, _P, _P, C.c_int, C.POINTER(HaloParams), _P, C.c_int, _P]),
     "exh_batch_run": (C.c_int, [_P, _P, _P, C.c_int, C.POINTER(HaloParams), _P, C.c_int, C.c_int, C.c_int, _P, _P,
                                 _P, _P, _P]),
+    "exh_diff_forward": (C.c_int, [_P, C.POINTER(DiffParams), _P, _P, _P, _P, _P, C.POINTER(C.c_double), _P, _P,
+                                   _P, _P]),
+    "exh_diff_backward": (C.c_int, [_P, C.c_double, _P, _P, _P]),
     "exh_smoothing_ladder": (C.c_int, [_P, _P, _P, C.c_int, C.POINTER(HaloParams), C.c_int, C.c_float, _P, _P, _P,
                                        C.c_int, _P]),
     "exh_fft_r2c_3d": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P]),

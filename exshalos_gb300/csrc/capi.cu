@@ -84,6 +84,7 @@ int exh_ctx_destroy(exh_ctx* ctx) {
   }
   for (auto& kv : ctx->c.plans) fft_plan_destroy(&kv.second);
   for (int i = 0; i < B_COUNT; i++) ctx->c.buf[i].release();
+  diff_state_release(ctx->c);
   halo_state_release(ctx->c);
   delete ctx;
   return EXH_OK;

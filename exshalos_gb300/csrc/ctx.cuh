@@ -84,6 +84,8 @@ enum BufId {
   B_COUNT
 };
 
+struct DiffState;     // differentiable forward kept for its adjoint (diff.cu)
+
 struct Ctx {
   int device = 0;
   std::map<std::tuple<int, int, int>, FFTPlan3D> plans;
@@ -100,11 +102,14 @@ struct Ctx {
   size_t shell_ncap = 0, shell_nall = 0;
   std::string mass_key;                 // mass-function splines (B_WORK2)
   std::string ladder_key;               // ladder window table (B_LADDERW)
+  DiffState* diff = nullptr;
   // lanes of the batched runner: contexts with their own streams
   std::vector<exh_ctx*> lane_ctx;
   std::vector<cudaStream_t> lane_st;
   int get_plan(int nx, int ny, int nz, FFTPlan3D** out);
 };
+
+void diff_state_release(Ctx& c);
 
 }  // namespace exh
 

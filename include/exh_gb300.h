@@ -183,6 +183,33 @@ int exh_batch_run(exh_ctx *ctx, const float *k, const float *P, int Nk, const ex
                   const exh_batch_item *items, int n, int Nk_pk, int lanes, int64_t *nh_out, float *k_out,
                   float *P_out, int64_t *count_out, int32_t *status_out);
 
+/* Differentiable forward model with a hand-written adjoint.  Noise w (a
+ * device real field nd^3) -> W = r2c(w) -> delta_k = W sqrt(p(k) / nd^3), p
+ * log-linear in log k between n_knots knots (constant beyond the ends) ->
+ * 1LPT and, with do_2lpt, 2LPT particles (src/exshalos/lpt.c:4-242, FD6
+ * gradients, cysumf wrap) -> CIC grid of the nd^3 particles
+ * (src/spectrum/gridmodule.c:21-53) -> P(k) in Nk bins from k_min to k_max with
+ * the CIC window (src/spectrum/powermodule.c:4-108) -> chi^2 against target_P
+ * with per-bin variance var (NULL: 2 T_b^2 / N_b).  The forward keeps its
+ * intermediates in the context; exh_diff_backward then writes d(grad_loss *
+ * chi^2)/dw into grad_noise (device, nd^3) and, if grad_knots is not NULL,
+ * d/dP_i into grad_knots (host, n_knots doubles).  P_out, k_out, count_out
+ * (host, Nk) may be NULL. */
+typedef struct {
+  int nd;              /* cells per side (cubic box), even, 8..1024 */
+  float L;             /* box side, Mpc/h */
+  float Om0, redshift; /* growth factor of the second order, Omega_m(z)^(-1/143) */
+  int do_2lpt;
+  int n_knots;         /* 2..64, increasing k */
+  int Nk;              /* P(k) bins */
+  float k_min, k_max;
+} exh_diff_params;
+
+int exh_diff_forward(exh_ctx *ctx, const exh_diff_params *prm, const float *noise, const float *knot_k,
+                     const float *knot_P, const float *target_P, const float *var, double *loss_out,
+                     float *P_out, float *k_out, int64_t *count_out, void *stream);
+int exh_diff_backward(exh_ctx *ctx, double grad_loss, float *grad_noise, double *grad_knots, void *stream);
+
 /* 3-D FFTs with FFTW conventions (unnormalised, half-complex last axis,
  * interleaved float2) — the transforms fftwf_plan_dft_r2c_3d /
  * fftwf_plan_dft_c2r_3d perform at src/spectrum/spectrum_h.c:103-107 and

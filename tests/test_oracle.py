@@ -176,3 +176,51 @@ def test_ladder_matches_numpy_restatement(orc, pk):
     got = orc.ladder(p, modes, R, B)
     assert np.mean(got != want) < 1e-4
     assert np.mean(got == 2) > 0.05
+
+
+def test_diff_oracle_recovers_input_spectrum(orc, pk):
+    """The FP64 differentiable-model oracle: with no displacement beyond first
+    order, the particles' CIC P(k) follows the knot spectrum on large scales."""
+    from oracle import diff_f64
+    k, P = pk
+    nd, L = 32, 256.0
+    knot_k = np.geomspace(2 * np.pi / L, np.sqrt(3) * np.pi * nd / L * 1.01, 20)
+    knot_P = np.exp(np.interp(np.log(knot_k), np.log(k.astype(np.float64)), np.log(P.astype(np.float64))))
+    Nk = 8
+    ps = []
+    for seed in range(4):
+        w = np.random.default_rng(seed).standard_normal((nd, nd, nd))
+        _, Pb, n = diff_f64.forward(w, knot_k, knot_P, L, np.ones(Nk), Nk, 2 * np.pi / L, np.pi * nd / L / 4,
+                                    do_2lpt=False)
+        ps.append(Pb)
+    Pm = np.mean(ps, axis=0)
+    kc = 2 * np.pi / L + (np.arange(Nk) + 0.5) * (np.pi * nd / L / 4 - 2 * np.pi / L) / Nk
+    want = np.exp(np.interp(np.log(kc), np.log(knot_k), np.log(knot_P)))
+    assert np.all(np.abs(Pm[1:] / want[1:] - 1) < 0.35)
+
+
+@pytest.mark.parametrize("do_2lpt", [False, True])
+def test_diff_oracle_adjoint_vs_finite_differences(orc, pk, do_2lpt):
+    """The FP64 adjoint restatement against FP64 central differences (nd = 16)."""
+    from oracle import diff_f64
+    k, P = pk
+    nd, L, Nk = 16, 64.0, 8
+    knot_k = np.geomspace(2 * np.pi / L, np.sqrt(3) * np.pi * nd / L * 1.01, 20)
+    knot_P = np.exp(np.interp(np.log(knot_k), np.log(k.astype(np.float64)), np.log(P.astype(np.float64))))
+    kmin, kmax = np.float32(2 * np.pi / L), np.float32(np.pi * nd / L)
+    w8 = np.random.default_rng(8).standard_normal((nd,) * 3)
+    _, T, _ = diff_f64.forward(w8, knot_k, knot_P, L, np.ones(Nk), Nk, kmin, kmax, do_2lpt=do_2lpt)
+    w = np.random.default_rng(7).standard_normal((nd,) * 3)
+    loss, gw, gk = diff_f64.gradient(w, knot_k, knot_P, L, T, Nk, kmin, kmax, do_2lpt=do_2lpt)
+
+    def f(ww, kk):
+        return diff_f64.forward(ww, knot_k, kk, L, T, Nk, kmin, kmax, do_2lpt=do_2lpt)[0]
+
+    assert abs(loss / f(w, knot_P) - 1) < 1e-5
+    v = np.random.default_rng(1).standard_normal(w.shape)
+    eps = 1e-6
+    fd = (f(w + eps * v, knot_P) - f(w - eps * v, knot_P)) / (2 * eps)
+    assert abs(np.sum(gw * v) - fd) < 1e-5 * abs(fd)
+    fdk = np.array([(f(w, knot_P * (1 + 1e-6 * (np.arange(20) == i))) -
+                     f(w, knot_P * (1 - 1e-6 * (np.arange(20) == i)))) / (2e-6 * knot_P[i]) for i in range(20)])
+    assert np.max(np.abs((gk - fdk) * knot_P)) < 1e-5 * np.max(np.abs(fdk * knot_P))
