@@ -323,6 +323,30 @@ static cudaError_t launch_grad(const BoxParams& b, const float* phi, float fac, 
   return cudaGetLastError();
 }
 
+// x pass of r2c(delta) for a given field (Compute_Denk, density_grid.c:220-235,
+// then lpt.c:11-45): phi1_k = Normk delta_k / (-k^2), 0 at k = 0 and k > k_smooth
+struct Lpt1FromGrid {
+  static constexpr int io_bytes = 8;
+  float2* __restrict__ out;
+  KGrid g;
+  int nc;
+  float Normk;
+  __device__ __forceinline__ void operator()(int, int e, int inner, float2 v) const {
+    const int j = inner / nc, k = inner % nc;
+    float kmod;
+    const float s = g.k2(e, j, k, kmod);
+    float2 r = make_float2(0.f, 0.f);
+    if (s != 0.f && kmod <= g.k_smooth) {
+      const float f = -(kmod * kmod);
+      r = make_float2(Normk * v.x / f, Normk * v.y / f);
+    }
+    out[(size_t)e * ((size_t)g.n1 * nc) + inner] = r;
+  }
+};
+
+static int lpt_from_phi1(Ctx& c, const BoxParams& b, float k_smooth, bool do2, float* S, float* V, float* phi1,
+                         float* phi2, cudaStream_t st);
+
 int lpt_run(Ctx& c, const BoxParams& b, const FieldModes& modes, float k_smooth, bool do2, float* S, float* V,
             float* phi1, float* phi2, cudaStream_t st) {
   FFTPlan3D* p;
@@ -330,9 +354,31 @@ int lpt_run(Ctx& c, const BoxParams& b, const FieldModes& modes, float k_smooth,
   const size_t nk = (size_t)b.nd[0] * b.nd[1] * p->nc;
   EXH_TRY(c.buf[B_WORK].ensure(sizeof(float2) * nk));
   float2* work = c.buf[B_WORK].as<float2>();
-  const HaloOut o = make_halo_out(b, nullptr, nullptr);
   KGrid g{b.nd[0], b.nd[1], b.nd[2], b.kl[0], b.kl[1], b.kl[2], k_smooth};
   EXH_CUDA_TRY(fft_c2r_3d(*p, Lpt1Gen{modes, g}, work, RealPairStore{phi1, b.nd[2], 1.f}, st));
+  return lpt_from_phi1(c, b, k_smooth, do2, S, V, phi1, phi2, st);
+}
+
+int lpt_run_grid(Ctx& c, const BoxParams& b, const float* delta, float k_smooth, bool do2, float* S, float* V,
+                 float* phi1, float* phi2, cudaStream_t st) {
+  FFTPlan3D* p;
+  EXH_TRY(c.get_plan(b.nd[0], b.nd[1], b.nd[2], &p));
+  const size_t nk = (size_t)b.nd[0] * b.nd[1] * p->nc;
+  EXH_TRY(c.buf[B_WORK].ensure(sizeof(float2) * nk));
+  float2* work = c.buf[B_WORK].as<float2>();
+  KGrid g{b.nd[0], b.nd[1], b.nd[2], b.kl[0], b.kl[1], b.kl[2], k_smooth};
+  EXH_CUDA_TRY(fft_r2c_3d(*p, RealPairLoad{delta, b.nd[2]}, work, Lpt1FromGrid{work, g, p->nc, b.Normk}, st));
+  EXH_CUDA_TRY(fft_c2r_3d(*p, CplxLoad{work, b.nd[0], b.nd[1] * p->nc}, work, RealPairStore{phi1, b.nd[2], 1.f}, st));
+  return lpt_from_phi1(c, b, k_smooth, do2, S, V, phi1, phi2, st);
+}
+
+static int lpt_from_phi1(Ctx& c, const BoxParams& b, float k_smooth, bool do2, float* S, float* V, float* phi1,
+                         float* phi2, cudaStream_t st) {
+  FFTPlan3D* p;
+  EXH_TRY(c.get_plan(b.nd[0], b.nd[1], b.nd[2], &p));
+  float2* work = c.buf[B_WORK].as<float2>();
+  const HaloOut o = make_halo_out(b, nullptr, nullptr);
+  KGrid g{b.nd[0], b.nd[1], b.nd[2], b.kl[0], b.kl[1], b.kl[2], k_smooth};
   // S1 = -D6(phi1) Normx / (60 Lc)  (lpt.c:64-68)
   EXH_CUDA_TRY(launch_grad(b, phi1, (float)(-b.Normx / (60.0 * b.Lc)), (float)o.f1, S, V, false, st));
   if (!do2) return EXH_OK;
@@ -378,6 +424,21 @@ int halo_displacements(Ctx& c, const BoxParams& b, const HaloDev& h, const Shell
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   return EXH_OK;
+}
+
+// [ng][3] -> planes [3][ng]
+__global__ void k_aos_to_planes(const float* __restrict__ in, size_t ng, float* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < 3 * ng; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t c = i / 3;
+    const int a = (int)(i % 3);
+    out[a * ng + c] = in[i];
+  }
+}
+
+int aos_to_planes(const float* in, size_t ng, float* out, cudaStream_t st) {
+  k_aos_to_planes<<<EXH_NUM_SMS * 16, 256, 0, st>>>(in, ng, out);
+  count_launch(1);
+  return cudaGetLastError() == cudaSuccess ? EXH_OK : EXH_E_CUDA;
 }
 
 int particles(const BoxParams& b, const float* S, const float* V, const HaloOut& o, float* pos, float* vel,

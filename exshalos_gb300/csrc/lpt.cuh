@@ -18,6 +18,11 @@ struct HaloOut {
 // matching velocities; phi1, phi2 are the potentials (work arrays)
 int lpt_run(Ctx& c, const BoxParams& b, const FieldModes& modes, float k_smooth, bool do2, float* S, float* V,
             float* phi1, float* phi2, cudaStream_t st);
+// the same from a given real field delta (device): delta_k = Normk r2c(delta)
+int lpt_run_grid(Ctx& c, const BoxParams& b, const float* delta, float k_smooth, bool do2, float* S, float* V,
+                 float* phi1, float* phi2, cudaStream_t st);
+// particle arrays [ng][3] -> planes [3][ng]
+int aos_to_planes(const float* in, size_t ng, float* out, cudaStream_t st);
 HaloOut make_halo_out(const BoxParams& b, float* posh, float* velh);
 int halo_displacements(Ctx& c, const BoxParams& b, const HaloDev& h, const ShellTable& t, const float* S,
                        const float* V, const HaloOut& o, cudaStream_t st);

@@ -258,6 +258,91 @@ int exh_find_halos(exh_ctx* ctx, const float* delta, int ndx, int ndy, int ndz, 
   return EXH_OK;
 }
 
+int exh_halos_box_from_grid(exh_ctx* ctx, const float* delta, int ndx, int ndy, int ndz, const float* k,
+                            const float* P, int Nk, const float* S_in, const float* V_in, const exh_halo_params* prm,
+                            int mem, int64_t* nh_out, void* stream) {
+  REQUIRE(ctx && delta && nh_out && prm, EXH_E_INVALID, "null argument");
+  REQUIRE(!(prm->OUT_VEL && S_in && !V_in), EXH_E_INVALID, "OUT_VEL with given displacements needs V");
+  exh_halo_params q = *prm;
+  q.ndx = ndx; q.ndy = ndy; q.ndz = ndz;
+  EXH_TRY(check_common(&q, k, P, Nk));
+  Ctx& c = ctx->c;
+  EXH_CUDA_TRY(cudaSetDevice(c.device));
+  cudaStream_t st = (cudaStream_t)stream;
+  halo_state_release(c);
+  c.verbose = prm->verbose;
+  BoxParams b;
+  // halos_box_from_grid binds the mass draws to seed 1234 (exshalos.c:987)
+  EXH_TRY(setup_box(&b, ndx, ndy, ndz, prm->Lc, prm->Om0, prm->redshift, prm->dc, prm->Nmin, prm->a, prm->beta,
+                    prm->alpha, 1234));
+  const size_t ng = b.ng;
+  const float* d = delta;
+  if (mem == EXH_MEM_HOST) {
+    EXH_TRY(c.buf[B_DELTA].ensure(sizeof(float) * ng));
+    EXH_CUDA_TRY(cudaMemcpyAsync(c.buf[B_DELTA].p, delta, sizeof(float) * ng, cudaMemcpyHostToDevice, st));
+    d = c.buf[B_DELTA].as<float>();
+  }
+  HaloDev h;
+  ShellTable t;
+  EXH_TRY(run_halo_finder(c, b, k, P, Nk, prm->setup_fp64, d, &h, &t, st));
+  EXH_TRY(c.buf[B_S].ensure(sizeof(float) * 3 * ng));
+  float* S = c.buf[B_S].as<float>();
+  float* V = nullptr;
+  if (prm->OUT_VEL) {
+    EXH_TRY(c.buf[B_VEL].ensure(sizeof(float) * 3 * ng));
+    V = c.buf[B_VEL].as<float>();
+  }
+  if (S_in) {
+    // box.c:89-105: the given displacements (and velocities), [ng][3]
+    const float* Sd = S_in;
+    const float* Vd = V_in;
+    if (mem == EXH_MEM_HOST) {
+      EXH_TRY(c.buf[B_V].ensure(sizeof(float) * 6 * ng));
+      float* stage = c.buf[B_V].as<float>();
+      EXH_CUDA_TRY(cudaMemcpyAsync(stage, S_in, sizeof(float) * 3 * ng, cudaMemcpyHostToDevice, st));
+      Sd = stage;
+      if (V && V_in) {
+        EXH_CUDA_TRY(cudaMemcpyAsync(stage + 3 * ng, V_in, sizeof(float) * 3 * ng, cudaMemcpyHostToDevice, st));
+        Vd = stage + 3 * ng;
+      }
+    }
+    EXH_TRY(aos_to_planes(Sd, ng, S, st));
+    if (V) EXH_TRY(aos_to_planes(Vd, ng, V, st));
+  } else {
+    // box.c:108-143: delta_k = Normk r2c(delta), then 1LPT (and 2LPT)
+    EXH_TRY(c.buf[B_PHI1].ensure(sizeof(float) * ng));
+    float* phi1 = c.buf[B_PHI1].as<float>();
+    float* phi2 = nullptr;
+    if (prm->DO_2LPT) {
+      EXH_TRY(c.buf[B_PHI2].ensure(sizeof(float) * ng));
+      phi2 = c.buf[B_PHI2].as<float>();
+    }
+    EXH_TRY(lpt_run_grid(c, b, d, prm->k_smooth, prm->DO_2LPT != 0, S, V, phi1, phi2, st));
+  }
+  const size_t nh = std::max<int64_t>(h.nh, 1);
+  EXH_TRY(c.buf[B_POSH].ensure(sizeof(float) * 6 * nh));
+  float* posh = c.buf[B_POSH].as<float>();
+  float* velh = prm->OUT_VEL ? posh + 3 * nh : nullptr;
+  const HaloOut o = make_halo_out(b, posh, velh);
+  EXH_TRY(halo_displacements(c, b, h, t, S, V, o, st));
+  HaloState& s = c.halos;
+  s.posh = posh;
+  s.velh = velh;
+  if (prm->OUT_LPT) {
+    // particle positions q + S wrapped (lpt.c:229-242); with given
+    // displacements the reference leaves its output array unset
+    // (exshalos.c:1001-1013), here it is filled the same way
+    EXH_TRY(c.buf[B_V].ensure(sizeof(float) * 6 * ng));
+    float* pos = c.buf[B_V].as<float>();
+    float* vel = prm->OUT_VEL ? pos + 3 * ng : nullptr;
+    EXH_TRY(particles(b, S, V, o, pos, vel, st));
+    s.pos = pos;
+    s.vel = vel;
+  }
+  *nh_out = s.nh;
+  return EXH_OK;
+}
+
 int exh_halos_fetch(exh_ctx* ctx, float* posh, float* velh, float* Mh, int32_t* xc, int32_t* count, float* grid,
                     float* pos, float* vel, int64_t* flag, int mem, void* stream) {
   REQUIRE(ctx, EXH_E_INVALID, "null context");

@@ -86,6 +86,46 @@ def halos_box_from_pk(k, P, R_max, Ndx, Ndy, Ndz, Lc, seed, k_smooth, Om0, redsh
     return out
 
 
+def halos_box_from_grid(k, P, grid, S, V, Lc, k_smooth, Om0, redshift, dc, Nmin, a, beta, alpha, OUT_LPT, OUT_VEL,
+                        DO_2LPT, OUT_FLAG, IN_disp, OUT_PROF, verbose, nthreads, _catalogue=False):
+    """Halo catalogue of a given density grid (exshalos.c:943-1103 /
+    box.c:71-150): the halos of `grid`, displaced by (2)LPT computed from the
+    grid or, with IN_disp, by the given displacements S[ng, 3] (and
+    velocities V with OUT_VEL).  Returns "posh", "Mh"; "velh" with OUT_VEL;
+    "pos" (and "vel") with OUT_LPT; "flag" with OUT_FLAG."""
+    if int(OUT_PROF):
+        raise NotImplementedError("Lagrangian profiles (OUT_PROF) are not built")
+    d = np.ascontiguousarray(grid, dtype=np.float32)
+    if d.ndim != 3:
+        raise ValueError("grid must be a 3-D array")
+    k = np.ascontiguousarray(k, dtype=np.float32)
+    P = np.ascontiguousarray(P, dtype=np.float32)
+    nd = tuple(int(x) for x in d.shape)
+    ng = nd[0] * nd[1] * nd[2]
+    Sd = Vd = None
+    if int(IN_disp):
+        Sd = np.ascontiguousarray(S, dtype=np.float32).reshape(ng, 3)
+        if int(OUT_VEL):
+            if V is None:
+                raise ValueError("OUT_VEL with given displacements needs V")
+            Vd = np.ascontiguousarray(V, dtype=np.float32).reshape(ng, 3)
+    prm = _params(ndx=nd[0], ndy=nd[1], ndz=nd[2], Lc=float(Lc), k_smooth=float(k_smooth), Om0=float(Om0),
+                  redshift=float(redshift), dc=float(dc), Nmin=int(Nmin), a=float(a), beta=float(beta),
+                  alpha=float(alpha), OUT_LPT=int(OUT_LPT), OUT_VEL=int(OUT_VEL), DO_2LPT=int(DO_2LPT),
+                  OUT_FLAG=int(OUT_FLAG), verbose=int(verbose), nthreads=int(nthreads))
+    import ctypes as C
+    nh = C.c_int64(0)
+    _capi.check(_capi.load().exh_halos_box_from_grid(_capi.context(), _capi.ptr(d), nd[0], nd[1], nd[2], _capi.ptr(k),
+                                                     _capi.ptr(P), k.size, _capi.ptr(Sd), _capi.ptr(Vd), prm,
+                                                     _capi.EXH_MEM_HOST, C.byref(nh), None))
+    out = _fetch_catalogue(nh.value, ng, want_vel=bool(OUT_VEL), want_pos=bool(OUT_LPT), want_flag=bool(OUT_FLAG),
+                           nd=nd)
+    if not _catalogue:
+        out.pop("x")
+        out.pop("count")
+    return out
+
+
 def find_halos(delta, k, P, Lc, Om0, redshift, dc, Nmin, a, beta, alpha, OUT_FLAG, OUT_PROF, verbose,
                _catalogue=False, setup_fp64=0):
     """Halos of a given density grid (exshalos.c:509-610): "posh" are the

@@ -122,6 +122,17 @@ int exh_find_halos(exh_ctx *ctx, const float *delta, int ndx, int ndy, int ndz, 
                    const float *P, int Nk, const exh_halo_params *prm, int mem, int64_t *nh_out,
                    void *stream);
 
+/* halos_box_from_grid (src/exshalos/exshalos.c:943-1103 ->
+ * Generate_Halos_Box_from_Grid, src/exshalos/box.c:71-150): halos of a
+ * caller-given float grid delta[ng] (mass draws seeded 1234 as exshalos.c:987),
+ * displaced by 1LPT (2LPT with DO_2LPT) computed from that grid, or, when S_in
+ * is not NULL, by the given displacements S_in[ng][3] (velocities V_in[ng][3]
+ * with OUT_VEL).  delta, S_in, V_in are in `mem`.  Results stay in the context
+ * (exh_halos_fetch); OUT_LPT also keeps the particles q + S. */
+int exh_halos_box_from_grid(exh_ctx *ctx, const float *delta, int ndx, int ndy, int ndz, const float *k,
+                            const float *P, int Nk, const float *S_in, const float *V_in,
+                            const exh_halo_params *prm, int mem, int64_t *nh_out, void *stream);
+
 /* Copy results of the last halos call into caller buffers (host or device
  * per `mem`; NULL skips an output).  posh/velh [3*nh], Mh[nh], Lagrangian
  * centre cells xc[3*nh], member counts count[nh]; grid[ng] the Gaussian

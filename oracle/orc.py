@@ -235,12 +235,24 @@ def halos_box_from_pk(k, P, nd=64, Lc=4.0, Om0=0.31, z=0.0, dc=-1.0, Nmin=1, a=1
     return out
 
 
-def lpt_posh(p, k, P, flag, hx, hcount, do_2lpt=1, k_smooth=10000.0, stream=1, keep_pos=False, prec="f64"):
+def grid_modes(p, delta, prec="f64"):
+    """Compute_Denk (density_grid.c:220-235): Normk r2c(delta), as modes"""
+    xk = fft_r2c_3d(delta, prec=prec) * (p.Normk_d if prec == "f64" else p.Normk)
+    out = np.zeros(xk.shape + (2,), dtype=real_dtype(prec))
+    out[..., 0] = xk.real
+    out[..., 1] = xk.imag
+    return out
+
+
+def lpt_posh(p, k, P, flag, hx, hcount, do_2lpt=1, k_smooth=10000.0, stream=1, keep_pos=False, prec="f64",
+             modes=None):
     """Compute_1LPT/Compute_2LPT/Compute_Posh (lpt.c) for a given halo
-    labelling, on the field modes of the given stream."""
+    labelling, on the field modes of the given stream (or given modes)."""
     L = lib(prec)
     rt = real_dtype(prec)
-    modes = field_modes(p, k, P, stream=stream, prec=prec)
+    if modes is None:
+        modes = field_modes(p, k, P, stream=stream, prec=prec)
+    modes = np.ascontiguousarray(modes, dtype=rt)
     nh = int(hcount.size)
     ng = int(p.ng)
     flag = np.ascontiguousarray(flag, dtype=np.int64).reshape(-1)

@@ -110,3 +110,62 @@ def test_halos_box_from_pk_vs_oracle(orc, pk, do2):
     dp = np.minimum(dp, L - dp)
     assert dp.max() < 2e-3
     assert np.all(np.isfinite(r["velh"]))
+
+
+@pytest.mark.parametrize("do2", [0, 1])
+def test_halos_box_from_grid_vs_oracle(orc, pk, do2):
+    """Generate_Halos_Box_from_Grid: the catalogue of a given grid bit for bit
+    (mass draws seeded 1234), LPT from Normk r2c(grid) against the FP64 oracle."""
+    from exshalos_gb300.lib import exshalos
+    k, P = pk
+    nd, Lc = 64, 4.0
+    p = orc.make_params(nd, Lc, seed=5)
+    grid = orc.field_real(p, orc.field_modes(p, k, P, stream=1)).astype(np.float32)
+    r = exshalos.halos_box_from_grid(k, P, grid, None, None, Lc, 1e4, 0.31, 0.0, -1.0, 1, 1.0, 0.0, 0.0, 1, 1, do2,
+                                     1, 0, 0, 0, 1, _catalogue=True)
+    pm = orc.make_params(nd, Lc, seed=1234)
+    ref = orc.find_halos(pm, grid, orc.sigma_tables(pm, k, P))
+    np.testing.assert_array_equal(r["x"], ref["x"])
+    np.testing.assert_array_equal(r["count"], ref["count"])
+    np.testing.assert_array_equal(r["Mh"].view(np.uint32), ref["Mh"].view(np.uint32))
+    np.testing.assert_array_equal(r["flag"].reshape(-1), ref["flag"])
+    lp = orc.lpt_posh(pm, k, P, ref["flag"], ref["x"], ref["count"], do_2lpt=do2, keep_pos=True,
+                      modes=orc.grid_modes(pm, grid.astype(np.float64)))
+    L = nd * Lc
+    d = np.abs(r["posh"] - lp["posh"])
+    assert np.minimum(d, L - d).max() < 2e-3
+    dp = np.abs(r["pos"] - lp["pos"])
+    assert np.minimum(dp, L - dp).max() < 2e-3
+    assert np.all(np.isfinite(r["velh"])) and np.all(np.isfinite(r["vel"]))
+
+
+def test_halos_box_from_grid_given_displacements(orc, pk):
+    """With S given, posh = cysumf(Lc (x + 1/2), sum of the members' S / count)
+    (box.c:89-105, lpt.c:245-255) and velh = sum of V / count."""
+    from exshalos_gb300 import mock
+    k, P = pk
+    nd, Lc = 48, 4.0
+    ng = nd ** 3
+    p = orc.make_params(nd, Lc, seed=9)
+    grid = orc.field_real(p, orc.field_modes(p, k, P, stream=1)).astype(np.float32)
+    rng = np.random.default_rng(4)
+    S = rng.normal(0, 3.0, (ng, 3)).astype(np.float32)
+    V = rng.normal(0, 100.0, (ng, 3)).astype(np.float32)
+    r = mock.Generate_Halos_Box_from_Grid(grid, k, P, S=S, V=V, Lc=Lc, OUT_VEL=True, OUT_FLAG=True)
+    flag = r["flag"].reshape(-1)
+    nh = r["posh"].shape[0]
+    owner = np.abs(flag)
+    m = owner < ng
+    sS = np.stack([np.bincount(owner[m], weights=S[m, a].astype(np.float64), minlength=nh) for a in range(3)], 1)
+    sV = np.stack([np.bincount(owner[m], weights=V[m, a].astype(np.float64), minlength=nh) for a in range(3)], 1)
+    pm = orc.make_params(nd, Lc, seed=1234)
+    ref = orc.find_halos(pm, grid, orc.sigma_tables(pm, k, P))
+    assert ref["nh"] == nh
+    cnt = ref["count"].astype(np.float64)          # Compute_Posh divides by the halo's count
+    L = nd * Lc
+    want = np.mod(Lc * (ref["x"] + 0.5) + sS / cnt[:, None], L)
+    d = np.abs(r["posh"] - want)
+    assert np.minimum(d, L - d).max() < 1e-3
+    np.testing.assert_allclose(r["velh"], sV / cnt[:, None], rtol=1e-4, atol=1e-3)
+    with pytest.raises(ValueError):
+        mock.Generate_Halos_Box_from_Grid(grid, k, P, S=S[:-1], Lc=Lc)
