@@ -235,9 +235,9 @@ __device__ __forceinline__ int lomuto_g_dest(int a, int nL, int m, LamT lam, Pos
 
 // per-chunk L counts
 __global__ void k_qs_count(const float* __restrict__ key, const Seg* __restrict__ segs, const int* __restrict__ cseg,
-                           const int* __restrict__ coff, int nchunks, int* __restrict__ cL) {
+                           const int* __restrict__ coff, const int* __restrict__ nchunks, int* __restrict__ cL) {
   const int ch = blockIdx.x;
-  if (ch >= nchunks) return;
+  if (ch >= *nchunks) return;
   const Seg s = segs[cseg[ch]];
   const float pv = key[s.hi];
   const int start = s.lo + coff[ch], end = min(start + CH, s.hi);
@@ -249,10 +249,10 @@ __global__ void k_qs_count(const float* __restrict__ key, const Seg* __restrict_
   if (threadIdx.x == 0) cL[ch] = tot;
 }
 
-__global__ void k_qs_seg_scan(const int* __restrict__ cfirst, int nseg, int* __restrict__ cL,
+__global__ void k_qs_seg_scan(const int* __restrict__ cfirst, const int* __restrict__ nseg, int* __restrict__ cL,
                               int* __restrict__ segNL) {
   const int sidx = blockIdx.x;
-  if (sidx >= nseg) return;
+  if (sidx >= *nseg) return;
   const int c0 = cfirst[sidx], c1 = cfirst[sidx + 1];
   __shared__ int ws[32];
   __shared__ int carry;
@@ -271,22 +271,27 @@ __global__ void k_qs_seg_scan(const int* __restrict__ cfirst, int nseg, int* __r
   if (threadIdx.x == 0) segNL[sidx] = carry;
 }
 
-// L placement, lam, pivot (phase 1) and > placement (phase 2)
+// L placement, lam, pivot (phase 1); the run end of every L rank (phase 3);
+// > placement (phase 2).  chain[rank] = (posl(rank), run end): the position
+// of the L element of that rank and the L count at the end of its run of L
+// elements (min(lam(g), nL), or nL when no > element follows), so a step of
+// the > chain is one 8-byte load.
 template <int PHASE>
-__global__ void k_qs_place(const float* __restrict__ key, const unsigned* __restrict__ id, const Seg* __restrict__ segs,
-                           const int* __restrict__ cseg, const int* __restrict__ coff, int nchunks,
-                           const int* __restrict__ cLoff, const int* __restrict__ segNL, int* __restrict__ lam,
-                           int* __restrict__ posl,
-                           float* __restrict__ okey, unsigned* __restrict__ oid, float* __restrict__ fkey,
-                           unsigned* __restrict__ fid) {
+__global__ void __launch_bounds__(CH_T)
+k_qs_place(const float* __restrict__ key, const unsigned* __restrict__ id, const Seg* __restrict__ segs,
+           const int* __restrict__ cseg, const int* __restrict__ coff, const int* __restrict__ nchunks,
+           const int* __restrict__ cLoff, const int* __restrict__ segNL, int* __restrict__ lam,
+           int2* __restrict__ chain, float* __restrict__ okey, unsigned* __restrict__ oid, float* __restrict__ fkey,
+           unsigned* __restrict__ fid) {
   const int ch = blockIdx.x;
-  if (ch >= nchunks) return;
+  if (ch >= *nchunks) return;
   const int sidx = cseg[ch];
   const Seg s = segs[sidx];
   const float pv = key[s.hi];
   const int nL = segNL[sidx];
   const int start = s.lo + coff[ch], end = min(start + CH, s.hi);
   const int base = start + threadIdx.x * CH_ITEMS;
+  const int m = (s.hi - s.lo) - nL;
   bool isL[CH_ITEMS];
   int n = 0;
 #pragma unroll
@@ -295,34 +300,63 @@ __global__ void k_qs_place(const float* __restrict__ key, const unsigned* __rest
     isL[q] = p < end && key[p] <= pv;
     n += isL[q];
   }
+  if (PHASE == 2) {
+    // every > element follows its chain; the thread's chains advance in
+    // lockstep so their loads overlap
+    int a[CH_ITEMS];
+    bool act[CH_ITEMS];
+#pragma unroll
+    for (int q = 0; q < CH_ITEMS; q++) {
+      const int p = base + q;
+      act[q] = p < end && !isL[q];
+      a[q] = p - s.lo;
+    }
+    const int2* cs = chain + s.lo;
+    for (int it = 0; it <= s.hi - s.lo; it++) {      // each step moves a chain forward
+      bool any = false;
+#pragma unroll
+      for (int q = 0; q < CH_ITEMS; q++) {
+        if (act[q] && a[q] < nL) {
+          const int2 v = __ldg(&cs[a[q]]);
+          const int c = v.x - a[q];
+          if (c <= 0) { a[q] = nL; continue; }          // never loop on inconsistent input
+          const int steps = (v.y - a[q] + c - 1) / c;
+          a[q] += c * max(steps, 1);
+          any = true;
+        }
+      }
+      if (!any) break;
+    }
+#pragma unroll
+    for (int q = 0; q < CH_ITEMS; q++) {
+      if (!act[q]) continue;
+      const int p = base + q;
+      const int dest = (a[q] >= nL) ? ((a[q] == nL) ? (s.hi - s.lo) : a[q]) : a[q];
+      okey[s.lo + dest] = key[p];
+      oid[s.lo + dest] = id[p];
+    }
+    return;
+  }
   __shared__ int ws[32];
   int tot;
   int rank = block_exclusive_scan<int>(n, ws, tot) + cLoff[ch];
-  const int m = (s.hi - s.lo) - nL;
 #pragma unroll
   for (int q = 0; q < CH_ITEMS; q++) {
     const int p = base + q;
     if (p >= end) break;
+    const int rel = p - s.lo;
     if (isL[q]) {
       if (PHASE == 1) {
         okey[s.lo + rank] = key[p];
         oid[s.lo + rank] = id[p];
-        posl[s.lo + rank] = p - s.lo;
+        chain[s.lo + rank].x = rel;
+      } else {                                   // PHASE 3: run end of this rank
+        const int c = rel - rank;                // > elements before it
+        chain[s.lo + rank].y = c < m ? min(lam[s.lo + c], nL) : nL;
       }
       rank++;
-    } else {
-      const int rel = p - s.lo;
-      if (PHASE == 1) {
-        lam[s.lo + (rel - rank)] = rank;
-      } else {
-        const int* lseg = lam + s.lo;
-        const int* pseg = posl + s.lo;
-        int a = lomuto_g_dest(rel, nL, m, [lseg](int i) { return __ldg(&lseg[i]); },
-                              [pseg](int i) { return __ldg(&pseg[i]); });
-        const int dest = (a == nL) ? (s.hi - s.lo) : a;
-        okey[s.lo + dest] = key[p];
-        oid[s.lo + dest] = id[p];
-      }
+    } else if (PHASE == 1) {
+      lam[s.lo + (rel - rank)] = rank;
     }
   }
   if (PHASE == 1 && coff[ch] == 0 && threadIdx.x == 0) {
@@ -333,15 +367,91 @@ __global__ void k_qs_place(const float* __restrict__ key, const unsigned* __rest
   }
 }
 
+// level bookkeeping on the device: counters of the level loop
+struct SortCtl {
+  int nseg, nch, nnext, nsmall, nsingle, err, pad0, pad1;
+};
+
+struct SortBufs {
+  float* kb[2];
+  unsigned* ib[2];
+};
+
+// children of every partitioned segment: large ones to the next level,
+// 2..SORT_SMALL elements to the block sort, single elements to the copy list
+__global__ void k_qs_children(const Seg* __restrict__ segs, const int* __restrict__ segNL, SortCtl* ctl,
+                              Seg* __restrict__ next, Seg* __restrict__ small, int2* __restrict__ single, int cap_next,
+                              int cap_small) {
+  const int sidx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (sidx >= ctl->nseg) return;
+  const Seg sg = segs[sidx];
+  const int nL = segNL[sidx];
+  const int nb = sg.buf ^ 1;
+  const Seg ch[2] = {{sg.lo, sg.lo + nL - 1, nb, 0}, {sg.lo + nL + 1, sg.hi, nb, 0}};
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const int len = ch[q].hi - ch[q].lo + 1;
+    if (len > SORT_SMALL) {
+      const int i = atomicAdd(&ctl->nnext, 1);
+      if (i < cap_next) next[i] = ch[q]; else atomicExch(&ctl->err, 1);
+    } else if (len >= 2) {
+      const int i = atomicAdd(&ctl->nsmall, 1);
+      if (i < cap_small) small[i] = ch[q]; else atomicExch(&ctl->err, 1);
+    } else if (len == 1) {
+      const int i = atomicAdd(&ctl->nsingle, 1);
+      if (i < cap_small) single[i] = make_int2(ch[q].lo, nb); else atomicExch(&ctl->err, 1);
+    }
+  }
+}
+
+// next level's segment list and chunk tables (one block)
+constexpr int QS_CHUNK_T = 1024;
+__global__ void __launch_bounds__(QS_CHUNK_T)
+k_qs_chunks(SortCtl* ctl, const Seg* __restrict__ next, Seg* __restrict__ segs, int* __restrict__ cfirst,
+            int* __restrict__ cseg, int* __restrict__ coff, int cap_chunks) {
+  __shared__ int ws[32];
+  __shared__ int carry;
+  const int nseg = ctl->nnext;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nseg; base += QS_CHUNK_T) {
+    const int i = base + threadIdx.x;
+    Seg sg{0, 0, 0, 0};
+    int n = 0;
+    if (i < nseg) {
+      sg = next[i];
+      n = (sg.hi - sg.lo + CH - 1) / CH;        // chunks over the elements before the pivot
+      segs[i] = sg;
+    }
+    int tot;
+    const int ex = block_exclusive_scan<int>(n, ws, tot) + carry;
+    if (i < nseg) {
+      cfirst[i] = ex;
+      for (int o = 0; o < n; o++) {
+        if (ex + o < cap_chunks) { cseg[ex + o] = i; coff[ex + o] = o * CH; }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    cfirst[nseg] = carry;
+    if (carry > cap_chunks) ctl->err = 1;
+    ctl->nseg = nseg;
+    ctl->nch = min(carry, cap_chunks);
+    ctl->nnext = 0;
+  }
+}
+
 // copy finished single elements into the final arrays
-__global__ void k_qs_copy_single(const int* __restrict__ pos, const int* __restrict__ bufi, int n,
-                                 float* const* __restrict__ kb, unsigned* const* __restrict__ ib,
+__global__ void k_qs_copy_single(const int2* __restrict__ single, const SortCtl* ctl, SortBufs b,
                                  float* __restrict__ fkey, unsigned* __restrict__ fid) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const int p = pos[t];
-  fkey[p] = kb[bufi[t]][p];
-  fid[p] = ib[bufi[t]][p];
+  if (t >= ctl->nsingle) return;
+  const int2 e = single[t];
+  fkey[e.x] = b.kb[e.y][e.x];
+  fid[e.x] = b.ib[e.y][e.x];
 }
 
 struct SmallSortBuffers {
@@ -450,11 +560,12 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
   unsigned* i1 = reinterpret_cast<unsigned*>(k1 + cap);
   float* fk = reinterpret_cast<float*>(i1 + cap);
   // final arrays live in B_PEAKS2
-  EXH_TRY(c.buf[B_PEAKS2].ensure((sizeof(float) + sizeof(unsigned)) * cap + 2 * sizeof(int) * cap));
+  EXH_TRY(c.buf[B_PEAKS2].ensure((sizeof(float) + sizeof(unsigned)) * cap + sizeof(int) * (cap + 1) +
+                                  sizeof(int2) * cap));
   fk = c.buf[B_PEAKS2].as<float>();
   unsigned* fi = reinterpret_cast<unsigned*>(fk + cap);
   int* lam = reinterpret_cast<int*>(fi + cap);
-  int* posl = lam + cap;
+  int2* chain = reinterpret_cast<int2*>(lam + cap + (cap & 1));     // 8-byte aligned
   if (np <= 1) {
     if (np == 1) {
       EXH_CUDA_TRY(cudaMemcpyAsync(fk, k0, sizeof(float), cudaMemcpyDeviceToDevice, st));
@@ -466,96 +577,87 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
   }
   float* kb[2] = {k0, k1};
   unsigned* ib[2] = {i0, i1};
-  std::vector<Seg> large, small;
-  std::vector<int> single_pos, single_buf;
-  if (np > SORT_SMALL) large.push_back({0, np - 1, 0, 0});
-  else small.push_back({0, np - 1, 0, 0});
-  // scratch: segments, chunk tables, counts
-  const int max_chunks = np / CH + 2 * (np / SORT_SMALL + 2) + 8;
+  // device-side level loop: segment lists, chunk tables and counters live
+  // on the device; the host launches levels and reads the counters back
+  // every few levels only
   const int max_segs = np / SORT_SMALL + 8;
-  const size_t scratch = sizeof(Seg) * (size_t)max_segs + sizeof(int) * ((size_t)max_chunks * 3 + 2 * (size_t)max_segs + 8);
-  EXH_TRY(c.buf[B_SCRATCH].ensure(std::max<size_t>(scratch, sizeof(Seg) * (size_t)(np / 2 + 8))));
-  Seg* d_segs = c.buf[B_SCRATCH].as<Seg>();
-  int* d_cseg = reinterpret_cast<int*>(d_segs + max_segs);
+  const int max_chunks = np / CH + max_segs + 8;
+  const int cap_small = np / 2 + 8;
+  const size_t need = sizeof(SortCtl) + sizeof(Seg) * (2 * (size_t)max_segs + cap_small) +
+                      sizeof(int2) * (size_t)cap_small +
+                      sizeof(int) * (3 * (size_t)max_chunks + 2 * (size_t)max_segs + 8) + 64;
+  EXH_TRY(c.buf[B_SCRATCH].ensure(need));
+  SortCtl* ctl = c.buf[B_SCRATCH].as<SortCtl>();
+  Seg* d_segs = reinterpret_cast<Seg*>(ctl + 1);
+  Seg* d_next = d_segs + max_segs;
+  Seg* d_small = d_next + max_segs;
+  int2* d_single = reinterpret_cast<int2*>(d_small + cap_small);
+  int* d_cseg = reinterpret_cast<int*>(d_single + cap_small);
   int* d_coff = d_cseg + max_chunks;
   int* d_cL = d_coff + max_chunks;
   int* d_cfirst = d_cL + max_chunks;
   int* d_nl = d_cfirst + max_segs + 1;
-  std::vector<int> hcseg, hcoff, hcfirst, hnl;
-  while (!large.empty()) {
-    const int buf = large[0].buf;   // every large segment of a level sits in the same buffer
-    hcseg.clear(); hcoff.clear(); hcfirst.clear();
-    for (size_t sidx = 0; sidx < large.size(); sidx++) {
-      hcfirst.push_back((int)hcseg.size());
-      const int len = large[sidx].hi - large[sidx].lo;   // elements before the pivot
-      for (int o = 0; o < len; o += CH) { hcseg.push_back((int)sidx); hcoff.push_back(o); }
-    }
-    hcfirst.push_back((int)hcseg.size());
-    const int nseg = (int)large.size(), nch = (int)hcseg.size();
-    EXH_CUDA_TRY(cudaMemcpyAsync(d_segs, large.data(), sizeof(Seg) * nseg, cudaMemcpyHostToDevice, st));
-    EXH_CUDA_TRY(cudaMemcpyAsync(d_cseg, hcseg.data(), sizeof(int) * nch, cudaMemcpyHostToDevice, st));
-    EXH_CUDA_TRY(cudaMemcpyAsync(d_coff, hcoff.data(), sizeof(int) * nch, cudaMemcpyHostToDevice, st));
-    EXH_CUDA_TRY(cudaMemcpyAsync(d_cfirst, hcfirst.data(), sizeof(int) * (nseg + 1), cudaMemcpyHostToDevice, st));
-    KTimer kt(KC_SORT, st, 0.0);
-    k_qs_count<<<nch, CH_T, 0, st>>>(kb[buf], d_segs, d_cseg, d_coff, nch, d_cL);
-    k_qs_seg_scan<<<nseg, 256, 0, st>>>(d_cfirst, nseg, d_cL, d_nl);
-    k_qs_place<1><<<nch, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, nch, d_cL, d_nl, lam, posl,
-                                        kb[buf ^ 1], ib[buf ^ 1], fk, fi);
-    k_qs_place<2><<<nch, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, nch, d_cL, d_nl, lam, posl,
-                                        kb[buf ^ 1], ib[buf ^ 1], fk, fi);
-    count_launch(4);
-    EXH_CUDA_TRY(cudaGetLastError());
-    hnl.resize(nseg);
-    EXH_CUDA_TRY(cudaMemcpyAsync(hnl.data(), d_nl, sizeof(int) * nseg, cudaMemcpyDeviceToHost, st));
-    EXH_CUDA_TRY(cudaStreamSynchronize(st));
-    std::vector<Seg> next;
-    for (int sidx = 0; sidx < nseg; sidx++) {
-      const Seg s = large[sidx];
-      const int nL = hnl[sidx];
-      const Seg ch[2] = {{s.lo, s.lo + nL - 1, buf ^ 1, 0}, {s.lo + nL + 1, s.hi, buf ^ 1, 0}};
-      for (const Seg& cs : ch) {
-        const int len = cs.hi - cs.lo + 1;
-        if (len == 1) { single_pos.push_back(cs.lo); single_buf.push_back(buf ^ 1); }
-        else if (len > SORT_SMALL) next.push_back(cs);
-        else if (len >= 2) small.push_back(cs);
+  SortCtl h0{};
+  const Seg whole{0, np - 1, 0, 0};
+  if (np > SORT_SMALL) h0.nnext = 1; else h0.nsmall = 1;
+  EXH_CUDA_TRY(cudaMemcpyAsync(np > SORT_SMALL ? d_next : d_small, &whole, sizeof(Seg), cudaMemcpyHostToDevice, st));
+  EXH_CUDA_TRY(cudaMemcpyAsync(ctl, &h0, sizeof(SortCtl), cudaMemcpyHostToDevice, st));
+  SortCtl hc = h0;
+  if (np > SORT_SMALL) {
+    k_qs_chunks<<<1, QS_CHUNK_T, 0, st>>>(ctl, d_next, d_segs, d_cfirst, d_cseg, d_coff, max_chunks);
+    count_launch(1);
+    constexpr int LEVELS_PER_CHECK = 4;
+    for (int level = 0;; level++) {
+      const int buf = level & 1;       // every large segment of a level sits in the same buffer
+      {
+        KTimer kt(KC_SORT, st, 0.0);
+        k_qs_count<<<max_chunks, CH_T, 0, st>>>(kb[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL);
+        k_qs_seg_scan<<<max_segs, 256, 0, st>>>(d_cfirst, &ctl->nseg, d_cL, d_nl);
+        k_qs_place<1><<<max_chunks, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL, d_nl,
+                                                   lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi);
+        k_qs_place<3><<<max_chunks, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL, d_nl,
+                                                   lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi);
+        k_qs_place<2><<<max_chunks, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL, d_nl,
+                                                   lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi);
+        k_qs_children<<<exh_div_up(max_segs, 128), 128, 0, st>>>(d_segs, d_nl, ctl, d_next, d_small, d_single,
+                                                                 max_segs, cap_small);
+        k_qs_chunks<<<1, QS_CHUNK_T, 0, st>>>(ctl, d_next, d_segs, d_cfirst, d_cseg, d_coff, max_chunks);
+        count_launch(7);
+        EXH_CUDA_TRY(cudaGetLastError());
+      }
+      if ((level + 1) % LEVELS_PER_CHECK == 0) {
+        EXH_CUDA_TRY(cudaMemcpyAsync(&hc, ctl, sizeof(SortCtl), cudaMemcpyDeviceToHost, st));
+        EXH_CUDA_TRY(cudaStreamSynchronize(st));
+        if (c.verbose) { printf("  sort level %d: %d large, %d small, %d single\n", level, hc.nseg, hc.nsmall, hc.nsingle); fflush(stdout); }
+        if (hc.err) {
+          exh_set_error_msg("peak sort: segment lists overflowed", __FILE__, __LINE__);
+          return EXH_E_RANGE;
+        }
+        if (hc.nseg == 0) break;
+      }
+      if (level > np) {
+        exh_set_error_msg("peak sort made no progress", __FILE__, __LINE__);
+        return EXH_E_TIMEOUT;
       }
     }
-    // a level holds segments from one buffer only: children all live in buf^1
-    large.swap(next);
-    if (c.verbose) { printf("  sort level: %zu large, %zu small, %zu single\n", large.size(), small.size(), single_pos.size()); fflush(stdout); }
   }
-  if (!single_pos.empty()) {
-    const int ns = (int)single_pos.size();
-    DevBuf& tmp = c.buf[B_HOSTIO2];
-    EXH_TRY(tmp.ensure(sizeof(int) * 2 * ns + sizeof(void*) * 4 + 64));
-    int* dpos = tmp.as<int>();
-    int* dbuf = dpos + ns;
-    void** dptr = reinterpret_cast<void**>(reinterpret_cast<char*>(tmp.p) + ((sizeof(int) * 2 * ns + 15) & ~size_t(15)));
-    void* hp[4] = {kb[0], kb[1], ib[0], ib[1]};
-    EXH_CUDA_TRY(cudaMemcpyAsync(dpos, single_pos.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
-    EXH_CUDA_TRY(cudaMemcpyAsync(dbuf, single_buf.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st));
-    EXH_CUDA_TRY(cudaMemcpyAsync(dptr, hp, sizeof(hp), cudaMemcpyHostToDevice, st));
-    k_qs_copy_single<<<exh_div_up(ns, 256), 256, 0, st>>>(dpos, dbuf, ns, reinterpret_cast<float* const*>(dptr),
-                                                          reinterpret_cast<unsigned* const*>(dptr + 2), fk, fi);
+  SortBufs sb{{kb[0], kb[1]}, {ib[0], ib[1]}};
+  if (hc.nsingle > 0) {
+    k_qs_copy_single<<<exh_div_up(hc.nsingle, 256), 256, 0, st>>>(d_single, ctl, sb, fk, fi);
     count_launch(1);
     EXH_CUDA_TRY(cudaGetLastError());
-    EXH_CUDA_TRY(cudaStreamSynchronize(st));
   }
-  if (!small.empty()) {
-    const int ns = (int)small.size();
-    EXH_CUDA_TRY(cudaMemcpyAsync(d_segs, small.data(), sizeof(Seg) * ns, cudaMemcpyHostToDevice, st));
-    EXH_TRY(c.buf[B_HOSTIO2].ensure(64));
-    int* d_err = c.buf[B_HOSTIO2].as<int>();
-    EXH_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+  if (hc.nsmall > 0) {
+    const int ns = hc.nsmall;
     const size_t sm = (size_t)SORT_SMALL * (4 * 4 + 2 * 4) + sizeof(int) * 3 * (size_t)SORT_SMALL;
     EXH_CUDA_TRY(set_smem(k_qs_small, sm));
-    SmallSortBuffers sb{{kb[0], kb[1]}, {ib[0], ib[1]}};
+    SmallSortBuffers smb{{kb[0], kb[1]}, {ib[0], ib[1]}};
     { KTimer kt(KC_SORT, st, 16.0 * np);
-    k_qs_small<<<ns, SORT_T, sm, st>>>(d_segs, ns, sb, fk, fi, d_err); }
+    k_qs_small<<<ns, SORT_T, sm, st>>>(d_small, ns, smb, fk, fi, &ctl->err); }
     count_launch(1);
     EXH_CUDA_TRY(cudaGetLastError());
     int herr = 0;
-    EXH_CUDA_TRY(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    EXH_CUDA_TRY(cudaMemcpyAsync(&herr, &ctl->err, sizeof(int), cudaMemcpyDeviceToHost, st));
     EXH_CUDA_TRY(cudaStreamSynchronize(st));
     if (herr) {
       exh_set_error_msg("peak sort: a block segment did not finish", __FILE__, __LINE__);
@@ -882,42 +984,46 @@ struct RoundArgs {
 
 __device__ __forceinline__ unsigned tentative_words(const GrowArgs& A, int ge) {
   // cells read by the growth (density + label) and reserved (read + atomic)
-  return 2u * (A.t.start_cap[min(ge, A.t.gmax) + 1] - A.t.start_cap[1]) + 2u * A.t.start_all[ge + 1] + 2u;
+  return 2u * (A.t.start_cap[min(ge, A.t.gmax) + 1] - A.t.start_cap[1]) + 2u * A.t.start_all[ge] + 2u;
 }
 
 // One round, part 1 (one thread per pending peak): every pending peak grows
-// with the flags committed so far (an upper bound of its final reads, since
-// flags are only ever added), keeps the result and reserves the cells up to
-// the shell it read last.  Peaks with larger spheres, or a comparison too
-// close to call in FP32, go to the warp pass.
+// with the flags committed so far and keeps the result.  Flags are only ever
+// added, and a claimed cell can only stop a growth earlier, so the last shell
+// read (gexit) is an upper bound of the final one, and the cells the peak
+// will flag (r^2 < final grows_tmp <= final gexit) lie inside r^2 < gexit:
+// the peak reserves those cells, its possible writes.  Peaks with larger
+// spheres, or a comparison too close to call in FP32, go to the warp pass.
 __global__ void __launch_bounds__(GROW_T)
-k_tentative(GrowArgs A, const int* __restrict__ list, int nlist, RoundArgs R) {
-  const int t = (int)(blockIdx.x * (size_t)blockDim.x + threadIdx.x);
-  if (t >= nlist) return;
-  const int r = list[t];
-  const int64_t l = A.np - 1 - r;
-  const unsigned cell0 = A.id[l];
-  if (R.flag[cell0] != FLAG_FREE) {        // find_halos.c:233: the peak is already inside a halo
-    R.state[r] = 1;
-    R.cnt[r] = 0;
-    return;
-  }
-  count_push(R.npend);
-  int x, y, z;
-  peak_coords(cell0, A.hs, x, y, z);
-  int count, gt, ge;
-  const int st = grow_lane_f32(A, R.flag, x, y, z, A.key[l], count, gt, ge);
-  if (st == 3) {
-    list_push(R.wlist, R.nw, r);
-    return;
-  }
-  R.cnt[r] = count; R.gtmp[r] = gt; R.gexit[r] = ge; R.gst[r] = st;
-  if (R.nwords) R.nwords[r] += tentative_words(A, ge);
-  const unsigned key = resv_key(R.tag, r);
-  const int e = A.t.start_all[ge + 1];
-  for (int q = 0; q < e; q++) {
-    unsigned* pr = &R.resv[cell_at(x, y, z, A.t.off_all[q], A.hs)];
-    if (*pr < key) atomicMax(pr, key);
+k_tentative(GrowArgs A, const int* __restrict__ list, const int* __restrict__ nlist, RoundArgs R) {
+  const int n = *nlist;
+  const int stride = (int)(gridDim.x * blockDim.x);
+  for (int t = (int)(blockIdx.x * (size_t)blockDim.x + threadIdx.x); t < n; t += stride) {
+    const int r = list[t];
+    const int64_t l = A.np - 1 - r;
+    const unsigned cell0 = A.id[l];
+    if (R.flag[cell0] != FLAG_FREE) {        // find_halos.c:233: the peak is already inside a halo
+      R.state[r] = 1;
+      R.cnt[r] = 0;
+      continue;
+    }
+    count_push(R.npend);
+    int x, y, z;
+    peak_coords(cell0, A.hs, x, y, z);
+    int count, gt, ge;
+    const int st = grow_lane_f32(A, R.flag, x, y, z, A.key[l], count, gt, ge);
+    if (st == 3) {
+      list_push(R.wlist, R.nw, r);
+      continue;
+    }
+    R.cnt[r] = count; R.gtmp[r] = gt; R.gexit[r] = ge; R.gst[r] = st;
+    if (R.nwords) R.nwords[r] += tentative_words(A, ge);
+    const unsigned key = resv_key(R.tag, r);
+    const int e = A.t.start_all[ge];          // cells it may flag: r^2 < gexit
+    for (int q = 0; q < e; q++) {
+      unsigned* pr = &R.resv[cell_at(x, y, z, A.t.off_all[q], A.hs)];
+      if (*pr < key) atomicMax(pr, key);
+    }
   }
 }
 
@@ -940,7 +1046,7 @@ k_tentative_warp(GrowArgs A, RoundArgs R) {
     if (lane == 0) { R.cnt[r] = count; R.gtmp[r] = gt; R.gexit[r] = ge; R.gst[r] = st; }
     if (lane == 0 && R.nwords) R.nwords[r] += tentative_words(A, ge);
     const unsigned key = resv_key(R.tag, r);
-    const int e = A.t.start_all[ge + 1];
+    const int e = A.t.start_all[ge];
     for (int q = lane; q < e; q += 32) {
       unsigned* pr = &R.resv[cell_at(x, y, z, A.t.off_all[q], A.hs)];
       if (*pr < key) atomicMax(pr, key);
@@ -962,35 +1068,41 @@ __device__ __forceinline__ bool commit_status(const RoundArgs& R, int r) {
   return R.cnt[r] != 0;                  // find_halos.c:339-340
 }
 
-// One round, part 2 (one thread per pending peak with at most
-// LANE_COMMIT_MAX reserved cells; the others go to the warp pass)
+// One round, part 2: a peak commits when no pending peak of higher rank
+// reserved (may flag) any cell it read (r^2 <= gexit): its tentative result
+// is then the sequential one.  Reservation keys order by round, then rank,
+// so a key above the peak's own is a higher-rank writer of this round.
+// One thread per pending peak with at most LANE_COMMIT_MAX cells read; the
+// others go to the warp pass.
 __global__ void __launch_bounds__(GROW_T)
-k_commit(GrowArgs A, const int* __restrict__ list, int nlist, RoundArgs R) {
-  const int t = (int)(blockIdx.x * (size_t)blockDim.x + threadIdx.x);
-  if (t >= nlist) return;
-  const int r = list[t];
-  if (R.state[r]) return;                // resolved by the centre test this round
-  const int e = A.t.start_all[R.gexit[r] + 1];
-  if (e > LANE_COMMIT_MAX) {
-    list_push(R.clist, R.nc, r);
-    return;
+k_commit(GrowArgs A, const int* __restrict__ list, const int* __restrict__ nlist, RoundArgs R) {
+  const int n = *nlist;
+  const int stride = (int)(gridDim.x * blockDim.x);
+  for (int t = (int)(blockIdx.x * (size_t)blockDim.x + threadIdx.x); t < n; t += stride) {
+    const int r = list[t];
+    if (R.state[r]) continue;              // resolved by the centre test this round
+    const int e = A.t.start_all[R.gexit[r] + 1];
+    if (e > LANE_COMMIT_MAX) {
+      list_push(R.clist, R.nc, r);
+      continue;
+    }
+    const unsigned cell0 = A.id[A.np - 1 - r];
+    int x, y, z;
+    peak_coords(cell0, A.hs, x, y, z);
+    const unsigned key = resv_key(R.tag, r);
+    bool mine = true;
+    for (int q = 0; q < e && mine; q++) mine = R.resv[cell_at(x, y, z, A.t.off_all[q], A.hs)] <= key;
+    if (R.nwords) R.nwords[r] += (unsigned)e;
+    if (!mine) {
+      list_push(R.next, R.nnext, r);
+      continue;
+    }
+    if (!commit_status(R, r)) continue;
+    const int we = A.t.start_all[R.gtmp[r]];     // cells with r^2 < grows_tmp
+    for (int q = 0; q < we; q++) R.flag[cell_at(x, y, z, A.t.off_all[q], A.hs)] = r;
+    if (R.nwords) R.nwords[r] += (unsigned)we;
+    R.flag[cell0] = -(r + 2);
   }
-  const unsigned cell0 = A.id[A.np - 1 - r];
-  int x, y, z;
-  peak_coords(cell0, A.hs, x, y, z);
-  const unsigned key = resv_key(R.tag, r);
-  bool mine = true;
-  for (int q = 0; q < e && mine; q++) mine = R.resv[cell_at(x, y, z, A.t.off_all[q], A.hs)] == key;
-  if (R.nwords) R.nwords[r] += (unsigned)e;
-  if (!mine) {
-    list_push(R.next, R.nnext, r);
-    return;
-  }
-  if (!commit_status(R, r)) return;
-  const int we = A.t.start_all[R.gtmp[r]];     // cells with r^2 < grows_tmp
-  for (int q = 0; q < we; q++) R.flag[cell_at(x, y, z, A.t.off_all[q], A.hs)] = r;
-  if (R.nwords) R.nwords[r] += (unsigned)we;
-  R.flag[cell0] = -(r + 2);
 }
 
 // part 2, warp pass (persistent) over the peaks handed on by k_commit
@@ -1007,7 +1119,7 @@ k_commit_warp(GrowArgs A, RoundArgs R) {
     const unsigned key = resv_key(R.tag, r);
     const int e = A.t.start_all[R.gexit[r] + 1];
     bool mine = true;
-    for (int q = lane; q < e && mine; q += 32) mine = R.resv[cell_at(x, y, z, A.t.off_all[q], A.hs)] == key;
+    for (int q = lane; q < e && mine; q += 32) mine = R.resv[cell_at(x, y, z, A.t.off_all[q], A.hs)] <= key;
     if (lane == 0 && R.nwords) R.nwords[r] += (unsigned)e;
     if (!__all_sync(0xffffffffu, mine)) {
       if (lane == 0) R.next[atomicAdd(R.nnext, 1)] = r;
@@ -1129,44 +1241,54 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   EXH_TRY(c.buf[B_HALO3].ensure(sizeof(int) * 2 * npr));
   int* wlist = c.buf[B_HALO3].as<int>();
   int* clist = wlist + npr;
+  // device counters: [0] grown this round, [1] error, [2] [3] the two list
+  // lengths, [4] warp growth list, [5] warp commit list, [6..7] byte total
   k_iota<<<nb, 128, 0, st>>>(lists[0], (int)nproc);
   count_launch(1);
-  int nlist = (int)nproc, cur = 0;
+  {
+    const int init[6] = {0, 0, (int)nproc, 0, 0, 0};
+    EXH_CUDA_TRY(cudaMemcpyAsync(dcnt, init, sizeof(init), cudaMemcpyHostToDevice, st));
+  }
   (void)nbw;
   if (timing_on()) EXH_CUDA_TRY(cudaMemsetAsync(h->words, 0, sizeof(unsigned) * npr, st));
   KTimer kt(KC_GROW, st, 0.0);   // the whole growth phase is one timed unit
-  int round = 0;
-  while (true) {
+  // the rounds run without host round trips: list lengths stay on the device
+  // and the persistent grids read them; the host checks every few rounds
+  const unsigned nbl = std::min<unsigned>(exh_div_up((size_t)nproc, GROW_T), GROW_PERSIST);
+  constexpr int ROUNDS_PER_CHECK = 3;
+  int cur = 0;
+  for (int round = 0;; round++) {
     const int tag = (round % 255) + 1;
     if (round > 0 && tag == 1) EXH_CUDA_TRY(cudaMemsetAsync(h->resv, 0, sizeof(unsigned) * ng, st));
-    EXH_CUDA_TRY(cudaMemsetAsync(dcnt, 0, sizeof(int) * 6, st));
+    EXH_CUDA_TRY(cudaMemsetAsync(dcnt + 3 - cur, 0, sizeof(int), st));      // next list
+    EXH_CUDA_TRY(cudaMemsetAsync(dcnt + 4, 0, sizeof(int) * 2, st));        // warp lists
     RoundArgs R;
     R.state = h->state; R.flag = h->flag; R.resv = h->resv; R.tag = tag;
     R.cnt = h->cnt; R.gtmp = h->gfin; R.gexit = gexit; R.gst = gst; R.gfin = h->gfin;
-    R.npend = dcnt; R.err = dcnt + 1; R.next = lists[cur ^ 1]; R.nnext = dcnt + 2;
-    R.wlist = wlist; R.nw = dcnt + 3; R.clist = clist; R.nc = dcnt + 4;
+    R.npend = dcnt; R.err = dcnt + 1; R.next = lists[cur ^ 1]; R.nnext = dcnt + 3 - cur;
+    R.wlist = wlist; R.nw = dcnt + 4; R.clist = clist; R.nc = dcnt + 5;
     R.nwords = timing_on() ? h->words : nullptr;
-    const unsigned nbl = exh_div_up((size_t)nlist, GROW_T);
-    k_tentative<<<nbl, GROW_T, 0, st>>>(A, lists[cur], nlist, R);
-    k_tentative_warp<<<std::min<unsigned>(GROW_PERSIST, exh_div_up((size_t)nlist * 32, GROW_T)), GROW_T, 0, st>>>(A, R);
-    k_commit<<<nbl, GROW_T, 0, st>>>(A, lists[cur], nlist, R);
-    k_commit_warp<<<std::min<unsigned>(GROW_PERSIST, exh_div_up((size_t)nlist * 32, GROW_T)), GROW_T, 0, st>>>(A, R);
+    const int* ncur = dcnt + 2 + cur;
+    k_tentative<<<nbl, GROW_T, 0, st>>>(A, lists[cur], ncur, R);
+    k_tentative_warp<<<nbl, GROW_T, 0, st>>>(A, R);
+    k_commit<<<nbl, GROW_T, 0, st>>>(A, lists[cur], ncur, R);
+    k_commit_warp<<<nbl, GROW_T, 0, st>>>(A, R);
     count_launch(4);
     EXH_CUDA_TRY(cudaGetLastError());
-    int hc[6];
-    EXH_CUDA_TRY(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
-    EXH_CUDA_TRY(cudaStreamSynchronize(st));
-    if (hc[1]) {
-      exh_set_error_msg(hc[1] == 1 ? "a halo grew past the sigma(M) table (find_halos.c:316 would read past Sig_Grid)"
-                                   : "a halo grew past every shell of the box",
-                        __FILE__, __LINE__);
-      return EXH_E_RANGE;
-    }
-    if (c.verbose > 1) { printf("  growth round %d: %d grown, %d left\n", round, hc[0], hc[2]); fflush(stdout); }
-    if (hc[2] == 0) break;
-    nlist = hc[2];
     cur ^= 1;
-    round++;
+    if ((round + 1) % ROUNDS_PER_CHECK == 0) {
+      int hc[6];
+      EXH_CUDA_TRY(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
+      EXH_CUDA_TRY(cudaStreamSynchronize(st));
+      if (hc[1]) {
+        exh_set_error_msg(hc[1] == 1 ? "a halo grew past the sigma(M) table (find_halos.c:316 would read past Sig_Grid)"
+                                     : "a halo grew past every shell of the box",
+                          __FILE__, __LINE__);
+        return EXH_E_RANGE;
+      }
+      if (c.verbose > 1) { printf("  growth round %d: %d left\n", round, hc[2 + cur]); fflush(stdout); }
+      if (hc[2 + cur] == 0) break;
+    }
     if (round > nproc + 2) {
       exh_set_error_msg("halo growth made no progress", __FILE__, __LINE__);
       return EXH_E_TIMEOUT;
@@ -1174,7 +1296,7 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   }
   if (timing_on()) {
     // algorithmic bytes of the growth rounds: one reduction over the peaks
-    unsigned long long* dsum = reinterpret_cast<unsigned long long*>(dcnt + 6);
+    unsigned long long* dsum = reinterpret_cast<unsigned long long*>(dcnt + 6);   // 8-byte aligned slot
     EXH_CUDA_TRY(cudaMemsetAsync(dsum, 0, sizeof(unsigned long long), st));
     k_sum_words<<<EXH_NUM_SMS, 256, 0, st>>>(h->words, (int)nproc, dsum);
     count_launch(1);
