@@ -238,10 +238,9 @@ int power_spectrum(Ctx& c, const float* grid_dev, int nd, float L, int window, i
 // ------------------------------------------------------------------------
 // Power spectrum that allocates nothing.
 //
-// Some callers cannot call cudaMalloc: code that runs while a stream is being
-// captured into a CUDA graph, real-time loops that must not touch the
-// allocator, and hosts whose device memory is handed out by a pool the
-// caller does not own.  exh_power_compute_noalloc gives them the power
+// Some callers cannot call cudaMalloc: real-time loops that must not stall
+// in the allocator (cudaMalloc/cudaFree can synchronise the device), and
+// hosts whose device memory is handed out by a pool the caller does not own.  exh_power_compute_noalloc gives them the power
 // spectrum of a small grid (nd <= 64, Nk <= 256) with every temporary -- the
 // half-complex work array, the twiddle tables and the per-block histograms --
 // in one file-scope device array below.  Every GPU that loads the library

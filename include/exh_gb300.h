@@ -73,9 +73,9 @@ int exh_power_compute(exh_ctx *ctx, const float *grid, int nd, float L, int wind
                       float k_min, float k_max, float *k_out, float *P_out, int64_t *count_out,
                       int mem, void *stream);
 
-/* Power spectrum for callers that cannot allocate device memory: code that
- * runs during CUDA-graph stream capture, real-time loops that must not touch
- * the allocator, or hosts whose device memory belongs to someone else's pool.
+/* Power spectrum for callers that cannot allocate device memory: real-time
+ * loops that must not stall in the allocator, and hosts whose device memory
+ * is handed out by a pool or framework that owns all of it.
  * No counterpart in the reference.  Same meaning as exh_power_compute, but
  * grid, k_out, P_out and count_out are all device pointers and nothing is
  * allocated: the work arrays live in one static device array of about

@@ -1,8 +1,8 @@
 """The allocation-free power spectrum (GPU).
 
 exh_power_compute_noalloc serves callers that cannot allocate device memory
-(code running under CUDA-graph stream capture, allocator-free real-time loops,
-hosts whose device memory belongs to another pool).  Its temporaries live in
+(real-time loops that must not stall in the allocator, hosts whose device
+memory belongs to a pool they do not own).  Its temporaries live in
 one static device array shared by every call.  This test calls it through
 the C ABI twice in a row, with different sizes so that the second call runs
 on what the first left behind, and checks both results against
