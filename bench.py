@@ -37,6 +37,13 @@ sys.path.insert(0, ROOT)
 
 ND, LC, NK_PK = 256, 2.0, 128
 BARRIER = dict(a=1.0, beta=0.12, alpha=0.0)
+# kernel classes whose time is set by dependent loads rather than bandwidth
+LATENCY_NOTES = {
+    "sort": "latency-bound: exact Lomuto order, dependent L2 loads along the > chains of each level",
+    "grow": "latency-bound: per-peak shell gathers and reservation rounds",
+    "mass": "FP64 spline evaluations",
+    "halo_disp": "per-halo gathers over member cells",
+}
 N_RADII, R_LADDER = 50, 30.0
 LADDER_SAMPLE = 5          # radii of the ladder timed on the host (each radius is the same work)
 METRIC = "256^3 realisations/s (halos+P(k))"
@@ -403,7 +410,8 @@ def run_ours(args, ws, rank, local):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_source": peak_kind,
-                     "traffic": traffic, "launches": nl, "ms_total": ms},
+                     "traffic": traffic, "launches": nl, "ms_total": ms,
+                     "note": LATENCY_NOTES.get(name, "streaming passes against the HBM copy peak")},
         "stage_ms_per_step": {kk: round(v[0] / args.steps, 4) for kk, v in rep.items() if v[1]},
         "roofline_by_class": by_class,
         "clocks": clk,

@@ -369,7 +369,8 @@ k_qs_place(const float* __restrict__ key, const unsigned* __restrict__ id, const
 
 // level bookkeeping on the device: counters of the level loop
 struct SortCtl {
-  int nseg, nch, nnext, nsmall, nsingle, err, pad0, pad1;
+  int nseg, nch, nnext, nsmall, nsingle, err;
+  unsigned long long elems;    // elements partitioned by the level kernels (timing)
 };
 
 struct SortBufs {
@@ -422,6 +423,7 @@ k_qs_chunks(SortCtl* ctl, const Seg* __restrict__ next, Seg* __restrict__ segs, 
       sg = next[i];
       n = (sg.hi - sg.lo + CH - 1) / CH;        // chunks over the elements before the pivot
       segs[i] = sg;
+      atomicAdd(&ctl->elems, (unsigned long long)(sg.hi - sg.lo + 1));
     }
     int tot;
     const int ex = block_exclusive_scan<int>(n, ws, tot) + carry;
@@ -607,10 +609,12 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
     k_qs_chunks<<<1, QS_CHUNK_T, 0, st>>>(ctl, d_next, d_segs, d_cfirst, d_cseg, d_coff, max_chunks);
     count_launch(1);
     constexpr int LEVELS_PER_CHECK = 4;
+    // the level loop is one timed unit; its algorithmic bytes are one read
+    // and one write of key and id (16 B) per element partitioned
+    KTimer kt(KC_SORT, st, 0.0);
     for (int level = 0;; level++) {
       const int buf = level & 1;       // every large segment of a level sits in the same buffer
       {
-        KTimer kt(KC_SORT, st, 0.0);
         k_qs_count<<<max_chunks, CH_T, 0, st>>>(kb[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL);
         k_qs_seg_scan<<<max_segs, 256, 0, st>>>(d_cfirst, &ctl->nseg, d_cL, d_nl);
         k_qs_place<1><<<max_chunks, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL, d_nl,
@@ -633,7 +637,10 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
           exh_set_error_msg("peak sort: segment lists overflowed", __FILE__, __LINE__);
           return EXH_E_RANGE;
         }
-        if (hc.nseg == 0) break;
+        if (hc.nseg == 0) {
+          kt.bytes = 16.0 * (double)hc.elems;
+          break;
+        }
       }
       if (level > np) {
         exh_set_error_msg("peak sort made no progress", __FILE__, __LINE__);

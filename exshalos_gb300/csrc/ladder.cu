@@ -89,6 +89,89 @@ struct CrossStore {
   }
 };
 
+// z pass of one radius with the barrier test, for boxes whose block tile of
+// the u8 map (R rows of 2M bytes) is a whole number of 16-byte chunks per
+// thread: the block's map bytes are loaded at the start, with the row data,
+// and written back once as 16-byte vectors after the transform.
+template <int N1, int N2>
+__global__ void __launch_bounds__(FS_THREADS)
+k_ladder_z(const float2* __restrict__ work, const float2* __restrict__ twM, const float2* __restrict__ twN,
+           unsigned char* __restrict__ cross, float normx, float B, int r) {
+  using S = FsShape<N1, N2>;
+  constexpr int M = S::n, R = S::R, LDA = FsRows<N1, N2>::LDA, nc = M + 1;
+  constexpr int CHUNKS = (R * 2 * M) / (16 * FS_THREADS);      // 16-byte chunks per thread
+  static_assert(CHUNKS >= 1 && (R * 2 * M) % (16 * FS_THREADS) == 0, "tile of whole 16-byte chunks");
+  extern __shared__ float2 x[];                    // 2 * R * LDA
+  float2* a = x + R * LDA;
+  const size_t r0 = (size_t)blockIdx.x * R;
+  uint4* tile = reinterpret_cast<uint4*>(cross + r0 * (2 * M));
+  uint4 cm[CHUNKS];
+#pragma unroll
+  for (int q = 0; q < CHUNKS; q++) cm[q] = tile[threadIdx.x + q * FS_THREADS];
+#pragma unroll
+  for (int t = threadIdx.x; t < R * nc; t += FS_THREADS) {
+    const int b = t / nc, k = t % nc;
+    float2 v = work[(r0 + b) * nc + k];
+    if (k == 0 || k == M) v.y = 0.f;
+    x[b * LDA + k] = v;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < R * M; t += FS_THREADS) {
+    const int b = t / M, k = t % M;
+    const float2 xk = x[b * LDA + k];
+    const float2 xm = cconj(x[b * LDA + (M - k)]);
+    const float2 d = cmul(tw_get(twN, k, 1.f), csub(xk, xm));
+    a[b * LDA + k] = make_float2(xk.x + xm.x - d.y, xk.y + xm.y + d.x);
+  }
+  __syncthreads();
+  fs_rows_smem<N1, N2>(a, LDA, twM, 1.f);
+  const unsigned char rb = (unsigned char)r;
+#pragma unroll
+  for (int q = 0; q < CHUNKS; q++) {
+    const int o = (threadIdx.x + q * FS_THREADS) * 16;          // byte offset in the tile
+    const int b = o / (2 * M), m0 = (o % (2 * M)) / 2;
+    unsigned w[4] = {cm[q].x, cm[q].y, cm[q].z, cm[q].w};
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      const float2 v = a[b * LDA + m0 + i];
+      const int s0 = (2 * i) & 3, wi = (2 * i) >> 2;             // bytes 2i and 2i+1 of the chunk
+      unsigned c0 = (w[wi] >> (8 * s0)) & 0xFFu, c1 = (w[wi] >> (8 * (s0 + 1))) & 0xFFu;
+      if (c0 == 255u && v.x * normx >= B) c0 = rb;
+      if (c1 == 255u && v.y * normx >= B) c1 = rb;
+      w[wi] = (w[wi] & ~(0xFFFFu << (8 * s0))) | (c0 << (8 * s0)) | (c1 << (8 * (s0 + 1)));
+    }
+    tile[threadIdx.x + q * FS_THREADS] = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
+// launches k_ladder_z when the box has a tile split for it; false otherwise
+static bool launch_ladder_z(const FFTPlan3D& p, const float2* work, unsigned char* cross, float normx, float B, int r,
+                            cudaStream_t st, cudaError_t* err) {
+  const size_t rows = (size_t)p.nx * p.ny;
+  if (reinterpret_cast<uintptr_t>(cross) % 16) return false;     // 16-byte vectors need an aligned map
+  switch (fs_split(p.M)) {
+#define X(A_, B_)                                                                                      \
+  case A_ * 1000 + B_: {                                                                               \
+    constexpr int R_ = FsShape<A_, B_>::R, M_ = A_ * B_;                                               \
+    if constexpr ((R_ * 2 * M_) % (16 * FS_THREADS) == 0) {                                            \
+      if (rows % R_) return false;                                                                     \
+      const size_t sm = 2 * sizeof(float2) * R_ * FsRows<A_, B_>::LDA;                                \
+      *err = set_smem(k_ladder_z<A_, B_>, sm);                                                         \
+      if (*err != cudaSuccess) return true;                                                            \
+      KTimer kt(KC_FFT_ROWS, st, (double)rows * ((M_ + 1) * 8.0 + M_ * 4.0));                          \
+      k_ladder_z<A_, B_><<<(unsigned)(rows / R_), FS_THREADS, sm, st>>>(work, p.twm, p.twn, cross, normx, B, r); \
+      count_launch(1);                                                                                 \
+      *err = cudaGetLastError();                                                                       \
+      return true;                                                                                     \
+    }                                                                                                  \
+    return false;                                                                                      \
+  }
+    EXH_FS_CASES(X)
+#undef X
+    default: return false;
+  }
+}
+
 int smoothing_ladder(Ctx& c, const BoxParams& b, const FieldModes& modes, int n_radii, const float* R,
                      const float* B, unsigned char* cross, cudaStream_t st) {
   FFTPlan3D* p;
@@ -127,7 +210,15 @@ int smoothing_ladder(Ctx& c, const BoxParams& b, const FieldModes& modes, int n_
   for (int i = n_radii - 1; i >= 0; i--) {       // large scales first
     LadderGen gen{dk, wtab + (size_t)i * nn, b.nd[0], p->nc, h};
     CrossStore cs{cross, b.nd[2], b.Normx, B[i], i};
-    EXH_CUDA_TRY(fft_c2r_3d(*p, gen, work, cs, st));
+    // x and y passes, then the z pass with the barrier test
+    EXH_CUDA_TRY(launch_strided(gen, CplxStore{work, p->nx, p->ny * p->nc}, p->px, p->twx, 1.f, 1, p->ny * p->nc,
+                                st));
+    EXH_CUDA_TRY(launch_strided(CplxLoad{work, p->ny, p->nc}, CplxStore{work, p->ny, p->nc}, p->py, p->twy, 1.f,
+                                p->nx, p->nc, st));
+    cudaError_t e = cudaSuccess;
+    if (!launch_ladder_z(*p, work, cross, b.Normx, B[i], i, st, &e))
+      e = launch_c2r_rows(HalfLoad{work, p->nc}, cs, *p, (size_t)p->nx * p->ny, st);
+    EXH_CUDA_TRY(e);
   }
   return EXH_OK;
 }
