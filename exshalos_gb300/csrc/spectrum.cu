@@ -105,6 +105,63 @@ int cic_assign(Ctx& c, const float* pos_dev, int64_t np, int nd, float L, float*
 // ------------------------------------------------------------------ P(k)
 __device__ __forceinline__ float sinc_f(float x) { return x != 0.f ? sinf(x) / x : 1.f; }
 
+// Binning of one transformed tile res[i * W + b] (x index i < n, column
+// b < nb of the tile starting at inner index i0) into the block's shared
+// histograms.
+__device__ __forceinline__ void bin_tile(const float2* res, int W, int n, int nb, int i0, int nd, int nc,
+                                         const BinParams& bp, double* hP, double* hK, unsigned* hN) {
+  // one thread per x row of the tile walks its W adjacent (y, kz)
+  // columns (cyclically, from a per-row start); neighbouring kz mostly share
+  // a shell, so the thread adds a run of same-bin modes in registers and
+  // touches the shared histogram once per run
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    int cur = -1;
+    double aP = 0.0, aK = 0.0;
+    unsigned aN = 0u;
+    for (int bb = 0; bb < nb; bb++) {
+      const int b = (bb + i) % nb;          // staggered start: rows of a warp hit different banks
+      const int col = i0 + b, j = col / nc, k = col % nc;
+      // mode-skip rule of powermodule.c:50-51 on the kz = 0 and kz = nd/2 planes
+      if ((k == 0 || k == nd / 2) &&
+          ((i > nd / 2 && j > nd / 2) || i == 0 || i == nd / 2 || j == 0 || j == nd / 2 || (i > nd / 2 && j < nd / 2)))
+        continue;
+      // wave numbers and bin index in the reference's float arithmetic
+      const float kx = (float)((2 * i < nd) ? i : i - nd) * bp.kn;
+      const float ky = (float)((2 * j < nd) ? j : j - nd) * bp.kn;
+      const float kz = (float)((2 * k < nd) ? k : k - nd) * bp.kn;
+      const float k2 = __fadd_rn(__fadd_rn(__fmul_rn(kx, kx), __fmul_rn(ky, ky)), __fmul_rn(kz, kz));
+      const float kmod = __fsqrt_rn(k2);
+      const int bin = (int)floorf(__fdiv_rn(__fsub_rn(kmod, bp.kmin), bp.dk));
+      if (bin < 0 || bin >= bp.Nk) continue;
+      float w = 1.f;
+      if (bp.window == 1 || bp.window == 2) {
+        w = sinc_f(kx * bp.Lb * 0.5f) * sinc_f(ky * bp.Lb * 0.5f) * sinc_f(kz * bp.Lb * 0.5f);
+        if (bp.window == 2) w = w * w;
+      }
+      const float2 v = res[i * W + b];
+      const double s = (double)bp.Normk / (double)w;
+      const double re = (double)v.x * s, im = (double)v.y * s;
+      if (bin != cur) {
+        if (cur >= 0) {
+          atomicAdd(&hP[cur], aP);
+          atomicAdd(&hK[cur], aK);
+          atomicAdd(&hN[cur], aN);
+        }
+        cur = bin;
+        aP = 0.0; aK = 0.0; aN = 0u;
+      }
+      aP += re * re + im * im;
+      aK += (double)kmod;
+      aN++;
+    }
+    if (cur >= 0) {
+      atomicAdd(&hP[cur], aP);
+      atomicAdd(&hK[cur], aK);
+      atomicAdd(&hN[cur], aN);
+    }
+  }
+}
+
 // x pass of the forward transform with the binning epilogue.
 // Tile: all nx modes of FFT_W adjacent (y, kz) columns.
 __global__ void __launch_bounds__(FFT_THREADS)
@@ -128,39 +185,92 @@ k_fft_x_bin(const float2* __restrict__ work, RadixPlan pl, const float2* __restr
   }
   __syncthreads();
   const float2* res = stockham_run(b0, b1, pl, FFT_W, FFT_W, tw, -1.f);
-  for (int t = threadIdx.x; t < n * FFT_W; t += blockDim.x) {
-    const int i = t / FFT_W, b = t % FFT_W;
-    if (b >= nb) continue;
-    const int col = i0 + b, j = col / nc, k = col % nc;
-    // mode-skip rule of powermodule.c:50-51 on the kz = 0 and kz = nd/2 planes
-    if ((k == 0 || k == nd / 2) &&
-        ((i > nd / 2 && j > nd / 2) || i == 0 || i == nd / 2 || j == 0 || j == nd / 2 || (i > nd / 2 && j < nd / 2)))
-      continue;
-    // wave numbers and bin index in the reference's float arithmetic
-    const float kx = (float)((2 * i < nd) ? i : i - nd) * bp.kn;
-    const float ky = (float)((2 * j < nd) ? j : j - nd) * bp.kn;
-    const float kz = (float)((2 * k < nd) ? k : k - nd) * bp.kn;
-    const float k2 = __fadd_rn(__fadd_rn(__fmul_rn(kx, kx), __fmul_rn(ky, ky)), __fmul_rn(kz, kz));
-    const float kmod = __fsqrt_rn(k2);
-    const int bin = (int)floorf(__fdiv_rn(__fsub_rn(kmod, bp.kmin), bp.dk));
-    if (bin < 0 || bin >= bp.Nk) continue;
-    float w = 1.f;
-    if (bp.window == 1 || bp.window == 2) {
-      w = sinc_f(kx * bp.Lb * 0.5f) * sinc_f(ky * bp.Lb * 0.5f) * sinc_f(kz * bp.Lb * 0.5f);
-      if (bp.window == 2) w = w * w;
-    }
-    const float2 v = res[i * FFT_W + b];
-    const double s = (double)bp.Normk / (double)w;
-    const double re = (double)v.x * s, im = (double)v.y * s;
-    atomicAdd(&hP[bin], re * re + im * im);
-    atomicAdd(&hK[bin], (double)kmod);
-    atomicAdd(&hN[bin], 1u);
-  }
+  bin_tile(res, FFT_W, n, nb, i0, nd, nc, bp, hP, hK, hN);
   __syncthreads();
   for (int b = threadIdx.x; b < bp.Nk; b += blockDim.x) {
     partP[(size_t)blockIdx.x * bp.Nk + b] = hP[b];
     partK[(size_t)blockIdx.x * bp.Nk + b] = hK[b];
     partN[(size_t)blockIdx.x * bp.Nk + b] = hN[b];
+  }
+}
+
+// The same x pass as a four-step register FFT (fft4.cuh) for the lengths it
+// covers: step 1 and the transpose as k_fft4_strided, then the results go
+// back to shared memory in natural order for bin_tile.
+template <int N1, int N2>
+__global__ void __launch_bounds__(FS_THREADS, 4)
+k_fft4_x_bin(const float2* __restrict__ work, const float2* __restrict__ tw, int nd, int nc, BinParams bp,
+             double* __restrict__ partP, double* __restrict__ partK, unsigned int* __restrict__ partN) {
+  using S = FsShape<N1, N2>;
+  constexpr int W = S::W, n = S::n;
+  extern __shared__ float2 dsm[];
+  float2* sm = dsm;
+  double* hP = reinterpret_cast<double*>(sm + n * W);
+  double* hK = hP + bp.Nk;
+  unsigned int* hN = reinterpret_cast<unsigned int*>(hK + bp.Nk);
+  const int inner = nd * nc;
+  const int i0 = blockIdx.x * W;
+  const int nb = min(W, inner - i0);
+  const int c = threadIdx.x % W, jj = threadIdx.x / W;
+  for (int b = threadIdx.x; b < bp.Nk; b += blockDim.x) { hP[b] = 0.0; hK[b] = 0.0; hN[b] = 0u; }
+  if (jj < N2) {
+    float2 v[N1];
+#pragma unroll
+    for (int j1 = 0; j1 < N1; j1++)
+      v[j1] = (c < nb) ? work[(size_t)(jj + N2 * j1) * inner + i0 + c] : make_float2(0.f, 0.f);
+    RDft<N1>::run(v, -1.f, [tw](int m) { return __ldg(&tw[m * N2]); });
+#pragma unroll
+    for (int k1 = 0; k1 < N1; k1++) {
+      float2 x = v[k1];
+      if (k1 != 0 && jj != 0) x = cmul(x, tw_get(tw, jj * k1, -1.f));
+      sm[(k1 * N2 + jj) * W + c] = x;
+    }
+  }
+  __syncthreads();
+  float2 u[N2];
+  if (jj < N1) {
+#pragma unroll
+    for (int j2 = 0; j2 < N2; j2++) u[j2] = sm[(jj * N2 + j2) * W + c];
+    RDft<N2>::run(u, -1.f, [tw](int m) { return __ldg(&tw[m * N1]); });
+  }
+  __syncthreads();
+  if (jj < N1) {
+#pragma unroll
+    for (int k2 = 0; k2 < N2; k2++) sm[(jj + N1 * k2) * W + c] = u[k2];
+  }
+  __syncthreads();
+  bin_tile(sm, W, n, nb, i0, nd, nc, bp, hP, hK, hN);
+  __syncthreads();
+  for (int b = threadIdx.x; b < bp.Nk; b += blockDim.x) {
+    partP[(size_t)blockIdx.x * bp.Nk + b] = hP[b];
+    partK[(size_t)blockIdx.x * bp.Nk + b] = hK[b];
+    partN[(size_t)blockIdx.x * bp.Nk + b] = hN[b];
+  }
+}
+
+// launches k_fft4_x_bin for the lengths with a four-step split; returns the
+// block count through nblk (0: not covered)
+static cudaError_t launch_fs_x_bin(const float2* work, const float2* tw, int nd, int nc, const BinParams& bp,
+                                   double* partP, double* partK, unsigned* partN, int nblk_cap, int* nblk,
+                                   cudaStream_t st) {
+  *nblk = 0;
+  const int inner = nd * nc;
+  switch (fs_split(nd)) {
+#define X(A_, B_)                                                                                        \
+  case A_ * 1000 + B_: {                                                                                 \
+    using S = FsShape<A_, B_>;                                                                           \
+    const int nb = (int)exh_div_up(inner, S::W);                                                         \
+    if (nb > nblk_cap) return cudaSuccess;                                                               \
+    const size_t sm = sizeof(float2) * S::n * S::W + (size_t)bp.Nk * (2 * sizeof(double) + sizeof(unsigned)) + 16; \
+    cudaError_t e = set_smem(k_fft4_x_bin<A_, B_>, sm);                                                  \
+    if (e != cudaSuccess) return e;                                                                      \
+    k_fft4_x_bin<A_, B_><<<nb, FS_THREADS, sm, st>>>(work, tw, nd, nc, bp, partP, partK, partN);          \
+    *nblk = nb;                                                                                          \
+    return cudaGetLastError();                                                                           \
+  }
+    EXH_FS_CASES(X)
+#undef X
+    default: return cudaSuccess;
   }
 }
 
@@ -218,17 +328,25 @@ int power_spectrum(Ctx& c, const float* grid_dev, int nd, float L, int window, i
   bp.Normk = (float)pow((double)(L / (float)(nd * nd)), 1.5);   // spectrum_h.c:90
   bp.window = window;
   const int inner = nd * p->nc;
-  const int nblk = (int)exh_div_up(inner, FFT_W);
-  EXH_TRY(c.buf[B_SCRATCH].ensure((sizeof(double) * 2 + sizeof(unsigned)) * (size_t)nblk * Nk));
+  // partial histograms: room for the smaller tile width of the two kernels
+  const int cap = (int)exh_div_up(inner, 4);
+  EXH_TRY(c.buf[B_SCRATCH].ensure((sizeof(double) * 2 + sizeof(unsigned)) * (size_t)cap * Nk));
   double* partP = c.buf[B_SCRATCH].as<double>();
-  double* partK = partP + (size_t)nblk * Nk;
-  unsigned* partN = reinterpret_cast<unsigned*>(partK + (size_t)nblk * Nk);
-  const size_t sm = smem_strided(nd) + (size_t)Nk * (2 * sizeof(double) + sizeof(unsigned)) + 16;
-  EXH_CUDA_TRY(set_smem(k_fft_x_bin, sm));
-  { KTimer kt(KC_BIN, st, 8.0 * nd * inner);
-  k_fft_x_bin<<<nblk, FFT_THREADS, sm, st>>>(work, p->px, p->twx, nd, p->nc, bp, partP, partK, partN); }
+  double* partK = partP + (size_t)cap * Nk;
+  unsigned* partN = reinterpret_cast<unsigned*>(partK + (size_t)cap * Nk);
+  int nblk = 0;
+  {
+    KTimer kt(KC_BIN, st, 8.0 * nd * inner);
+    EXH_CUDA_TRY(launch_fs_x_bin(work, p->twx, nd, p->nc, bp, partP, partK, partN, cap, &nblk, st));
+    if (nblk == 0) {
+      nblk = (int)exh_div_up(inner, FFT_W);
+      const size_t sm = smem_strided(nd) + (size_t)Nk * (2 * sizeof(double) + sizeof(unsigned)) + 16;
+      EXH_CUDA_TRY(set_smem(k_fft_x_bin, sm));
+      k_fft_x_bin<<<nblk, FFT_THREADS, sm, st>>>(work, p->px, p->twx, nd, p->nc, bp, partP, partK, partN);
+      EXH_CUDA_TRY(cudaGetLastError());
+    }
+  }
   count_launch(1);
-  EXH_CUDA_TRY(cudaGetLastError());
   k_bin_reduce<<<Nk, 256, 0, st>>>(partP, partK, partN, nblk, Nk, outP_dev, outK_dev, outN_dev);
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
