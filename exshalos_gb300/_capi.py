@@ -75,6 +75,10 @@ SIGNATURES = {
     "exh_diff_backward": (C.c_int, [_P, C.c_double, _P, _P, _P]),
     "exh_halos_box_from_grid": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, _P, _P, C.c_int, _P, _P,
                                           C.POINTER(HaloParams), C.c_int, C.POINTER(C.c_int64), _P]),
+    "exh_grid_compute_ex": (C.c_int, [_P, _P, _P, _P, _P, C.c_int64, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
+                                      C.c_int, C.c_int, C.c_float, C.c_float, C.c_int, C.c_int, _P, C.c_int, _P]),
+    "exh_power_compute_ex": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_float, C.c_int, C.c_float, C.c_int, C.c_int,
+                                       C.c_float, C.c_float, C.c_int, C.c_int, _P, _P, _P, C.c_int, _P]),
     "exh_smoothing_ladder": (C.c_int, [_P, _P, _P, C.c_int, C.POINTER(HaloParams), C.c_int, C.c_float, _P, _P, _P,
                                        C.c_int, _P]),
     "exh_fft_r2c_3d": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P]),

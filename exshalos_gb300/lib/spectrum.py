@@ -1,10 +1,7 @@
 """Mirror of the reference extension pyexshalos.lib.spectrum
 (src/spectrum/spectrum.c) for the functions on the mock path.
 
-Arguments keep the reference's positional order and meaning.  Options the
-GPU path does not build (other windows, several tracer types, interlacing,
-redshift-space shifts, multipoles, folding) raise NotImplementedError instead
-of silently changing the result.
+Arguments keep the reference's positional order and meaning.
 """
 import numpy as np
 
@@ -18,37 +15,62 @@ def check_precision():
 
 def grid_compute(pos, vel, mass, nmass, type, ntype, nd, L, Om0, z, direction, window, R, R_times,
                  interlacing, folds, verbose, nthreads):
-    """Density contrast grid [ntype, interlacing+1, nd, nd, nd] (spectrum.c:46-108)."""
-    if int(nmass) != 0 or mass is not None:
-        raise NotImplementedError("weighted tracers are not built")
-    if int(ntype) != 1 or int(interlacing) != 0:
-        raise NotImplementedError("one tracer type without interlacing is built")
-    if int(direction) != -1:
-        raise NotImplementedError("redshift-space shifts are not built")
+    """Density contrast grid [ntype, interlacing+1, nd, nd, nd] (spectrum.c:46-108).
+
+    One unit-mass tracer type with CIC, no interlacing and no redshift-space
+    shift runs the dedicated CIC kernel; every other combination (NGP, CIC,
+    Sphere, Exp windows, masses, several types, interlacing, a shift along
+    x/y/z, folds) runs the general assignment.  The positions passed in are
+    not modified (the reference shifts them in place for redshift space)."""
     pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
-    nd = int(nd)
-    grid = np.empty((1, 1, nd, nd, nd), dtype=np.float32)
+    npart = pos.shape[0]
+    nd, ntype, interlacing, direction = int(nd), int(ntype), int(interlacing), int(direction)
+    window, folds = int(window), int(folds)
+    weighted = int(nmass) != 0 and mass is not None
+    if window not in (1, 2, 3, 4):
+        raise ValueError("window must be 1 (NGP), 2 (CIC), 3 (Sphere) or 4 (Exp)")
     L_ = _capi.load()
-    _capi.check(L_.exh_grid_compute(_capi.context(), _capi.ptr(pos), pos.shape[0], nd, float(L), int(window),
-                                    int(folds), _capi.ptr(grid), _capi.EXH_MEM_HOST, None))
+    grid = np.empty((ntype, interlacing + 1, nd, nd, nd), dtype=np.float32)
+    if ntype == 1 and interlacing == 0 and direction == -1 and window == 2 and not weighted:
+        _capi.check(L_.exh_grid_compute(_capi.context(), _capi.ptr(pos), npart, nd, float(L) / folds, 2, 1,
+                                        _capi.ptr(grid), _capi.EXH_MEM_HOST, None))
+        return grid
+    v = np.ascontiguousarray(vel, dtype=np.float32).reshape(-1, 3) if direction != -1 else None
+    if direction != -1 and (v is None or v.shape[0] != npart):
+        raise ValueError("a redshift-space shift needs one velocity per tracer")
+    m = np.ascontiguousarray(mass, dtype=np.float32).reshape(-1) if weighted else None
+    t = np.ascontiguousarray(type, dtype=np.int32).reshape(-1) if ntype > 1 else None
+    if (m is not None and m.size != npart) or (t is not None and t.size != npart):
+        raise ValueError("mass and type need one entry per tracer")
+    _capi.check(L_.exh_grid_compute_ex(_capi.context(), _capi.ptr(pos), _capi.ptr(v), _capi.ptr(m), _capi.ptr(t),
+                                       npart, ntype, nd, float(L), float(Om0), float(z), direction, window, float(R),
+                                       float(R_times), interlacing, folds, _capi.ptr(grid), _capi.EXH_MEM_HOST,
+                                       None))
     return grid
 
 
 def power_compute(grid, ntype, nd, L, window, R, interlacing, Nk, k_min, k_max, l_max, direction, verbose,
                   nthreads):
-    """{"k", "Pk", "Nk"} of one grid (spectrum.c:111-197); Pk shaped [1, 1, Nk]."""
-    if int(ntype) != 1 or int(interlacing) != 0 or int(l_max) != 0:
-        raise NotImplementedError("one tracer type, no interlacing and l_max = 0 are built")
+    """{"k", "Pk", "Nk"} (spectrum.c:111-197); Pk shaped [ntype (ntype + 1) / 2, l_max / 2 + 1, Nk]
+    (auto and cross spectra in the order (0,0), (1,0), (1,1), ...; even
+    multipoles).  One grid, l_max = 0, no interlacing and windows 0-2 run
+    the fused single-spectrum kernel; other options the general one."""
     g = np.ascontiguousarray(grid, dtype=np.float32)
-    nd = int(nd)
-    if g.size != nd ** 3:
-        raise ValueError("grid size does not match nd")
-    Nk = int(Nk)
+    nd, ntype, interlacing, l_max = int(nd), int(ntype), int(interlacing), int(l_max)
+    window, direction, Nk = int(window), int(direction), int(Nk)
+    if g.size != ntype * (interlacing + 1) * nd ** 3:
+        raise ValueError("grid size does not match ntype, interlacing and nd")
+    nps, ls = ntype * (ntype + 1) // 2, l_max // 2 + 1
     k = np.zeros(Nk, dtype=np.float32)
-    P = np.zeros((1, 1, Nk), dtype=np.float32)
+    P = np.zeros((nps, ls, Nk), dtype=np.float32)
     cnt = np.zeros(Nk, dtype=np.int64)
     L_ = _capi.load()
-    _capi.check(L_.exh_power_compute(_capi.context(), _capi.ptr(g), nd, float(L), int(window), Nk, float(k_min),
-                                     float(k_max), _capi.ptr(k), _capi.ptr(P), _capi.ptr(cnt),
-                                     _capi.EXH_MEM_HOST, None))
+    if ntype == 1 and interlacing == 0 and l_max == 0 and window in (0, 1, 2):
+        _capi.check(L_.exh_power_compute(_capi.context(), _capi.ptr(g), nd, float(L), window, Nk, float(k_min),
+                                         float(k_max), _capi.ptr(k), _capi.ptr(P), _capi.ptr(cnt),
+                                         _capi.EXH_MEM_HOST, None))
+    else:
+        _capi.check(L_.exh_power_compute_ex(_capi.context(), _capi.ptr(g), ntype, nd, float(L), window, float(R),
+                                            interlacing, Nk, float(k_min), float(k_max), l_max, direction,
+                                            _capi.ptr(k), _capi.ptr(P), _capi.ptr(cnt), _capi.EXH_MEM_HOST, None))
     return {"k": k, "Pk": P, "Nk": cnt}

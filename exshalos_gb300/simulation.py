@@ -53,8 +53,10 @@ def Compute_Density_Grid(
 ) -> np.ndarray:
     """Density contrast of a tracer set on an nd^3 grid (simulation.py:9-166).
 
-    Built: CIC, one tracer type, no interlacing, real space, folds = 1; other
-    options raise NotImplementedError.  Returns [nd, nd, nd] float32."""
+    Windows NGP, CIC, SPHERICAL (R), EXPONENTIAL (R, R_times); masses;
+    several tracer types; interlacing; redshift-space shifts along x/y/z;
+    folds.  Returns [nd, nd, nd] float32 for one type without interlacing,
+    else [ntypes, interlacing + 1, nd, nd, nd]."""
     pos = np.asarray(pos).astype("float32")
     L, R, R_times = np.float32(L), np.float32(R), np.float32(R_times)
     Om0, z = np.float32(Om0), np.float32(z)
@@ -64,9 +66,9 @@ def Compute_Density_Grid(
         nmass = 1
     ntypes = 1
     if types is not None:
-        t = np.fabs(types)
-        t = (t - np.min(t)).astype("int32")
-        ntypes = len(np.unique(t))
+        types = np.fabs(types)
+        types = (types - np.min(types)).astype("int32")
+        ntypes = len(np.unique(types))
     direction = _direction_code(direction)
     window = _window_code(window, allow_none=False)
     if window is None:

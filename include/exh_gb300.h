@@ -73,6 +73,32 @@ int exh_power_compute(exh_ctx *ctx, const float *grid, int nd, float L, int wind
                       float k_min, float k_max, float *k_out, float *P_out, int64_t *count_out,
                       int mem, void *stream);
 
+/* grid_compute with every option of Tracer_Grid (src/spectrum/spectrum.c:46-108,
+ * src/spectrum/gridmodule.c:146-376): window 1 NGP, 2 CIC, 3 Sphere(R),
+ * 4 Exp(R, R_times) (gridmodule.c:7-140); mass[np] (NULL: unit masses);
+ * type[np] in 0..ntype-1 (NULL when ntype == 1); interlacing (a second grid
+ * of the positions shifted by -L/nd/2); direction 0..2 shifts that
+ * coordinate by vel (1+z)^3 / H(Om0, z) (redshift space; the caller's
+ * positions are not modified, unlike the reference); folds >= 1.
+ * grid[ntype][interlacing + 1][nd^3] holds rho / (M / nd^3) - 1 per grid.
+ * pos/vel/mass/type and grid are in `mem`.  Masses must sum to a positive
+ * total. */
+int exh_grid_compute_ex(exh_ctx *ctx, const float *pos, const float *vel, const float *mass,
+                        const int32_t *type, int64_t np, int ntype, int nd, float L, float Om0, float z,
+                        int direction, int window, float R, float R_times, int interlacing, int folds,
+                        float *grid, int mem, void *stream);
+
+/* power_compute with every option of Power_Spectrum (src/spectrum/spectrum.c:111-197,
+ * src/spectrum/powermodule.c:4-108, Compute_gridk src/spectrum/spectrum_h.c:83-167):
+ * grid[ntype][interlacing + 1][nd^3] (in `mem`), window 0..4 deconvolved,
+ * every auto and cross spectrum (ntype (ntype + 1) / 2 pairs, l >= m order)
+ * and the even Legendre multipoles up to l_max about `direction` (-1: mu = 0).
+ * P_out[pair][l / 2][Nk], k_out[Nk], count_out[Nk] on the host; bin sums
+ * in FP64. */
+int exh_power_compute_ex(exh_ctx *ctx, const float *grid, int ntype, int nd, float L, int window, float R,
+                         int interlacing, int Nk, float k_min, float k_max, int l_max, int direction,
+                         float *k_out, float *P_out, int64_t *count_out, int mem, void *stream);
+
 /* Power spectrum for callers that cannot allocate device memory: real-time
  * loops that must not stall in the allocator, and hosts whose device memory
  * is handed out by a pool or framework that owns all of it.
