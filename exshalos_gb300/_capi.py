@@ -79,6 +79,8 @@ SIGNATURES = {
                                       C.c_int, C.c_int, C.c_float, C.c_float, C.c_int, C.c_int, _P, C.c_int, _P]),
     "exh_power_compute_ex": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_float, C.c_int, C.c_float, C.c_int, C.c_int,
                                        C.c_float, C.c_float, C.c_int, C.c_int, _P, _P, _P, C.c_int, _P]),
+    "exh_abundance_compute": (C.c_int, [_P, _P, C.c_int64, C.c_float, C.c_float, C.c_int, C.c_float, C.c_int, C.c_int,
+                                        C.c_int, _P, _P, _P, C.c_int, _P]),
     "exh_smoothing_ladder": (C.c_int, [_P, _P, _P, C.c_int, C.POINTER(HaloParams), C.c_int, C.c_float, _P, _P, _P,
                                        C.c_int, _P]),
     "exh_fft_r2c_3d": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P]),

@@ -102,6 +102,12 @@ struct Ctx {
   size_t shell_ncap = 0, shell_nall = 0;
   std::string mass_key;                 // mass-function splines (B_WORK2)
   std::string ladder_key;               // ladder window table (B_LADDERW)
+  // sorted peaks of the last grid given to exh_find_halos (B_PEAKS2), by digest
+  unsigned long long peak_hash = 0;
+  int peak_nd[3] = {0, 0, 0};
+  int64_t peak_np = 0;
+  float* peak_key = nullptr;
+  unsigned* peak_id = nullptr;
   DiffState* diff = nullptr;
   // lanes of the batched runner: contexts with their own streams
   std::vector<exh_ctx*> lane_ctx;

@@ -44,8 +44,41 @@ static int check_common(const exh_halo_params* p, const float* k, const float* P
 namespace {
 
 // Find_Halos (find_halos.c:479-563) on the device field `delta`
+// order-independent 64-bit digest of a grid (sum of splitmix64 of value bits
+// and index): a repeated grid is recognised without a host copy
+__global__ void k_grid_hash(const float* __restrict__ d, size_t n, unsigned long long* __restrict__ out) {
+  unsigned long long s = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    unsigned long long x = ((unsigned long long)__float_as_uint(d[i]) << 32) ^ (unsigned long long)i;
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    s += x ^ (x >> 31);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+
+int grid_digest(Ctx& c, const float* d, size_t n, cudaStream_t st, unsigned long long* out) {
+  EXH_TRY(c.buf[B_HOSTIO2].ensure(64));
+  unsigned long long* dh = reinterpret_cast<unsigned long long*>(c.buf[B_HOSTIO2].as<char>() + 32);
+  EXH_CUDA_TRY(cudaMemsetAsync(dh, 0, sizeof(unsigned long long), st));
+  k_grid_hash<<<EXH_NUM_SMS * 8, 256, 0, st>>>(d, n, dh);
+  count_launch(1);
+  EXH_CUDA_TRY(cudaGetLastError());
+  EXH_CUDA_TRY(cudaMemcpyAsync(out, dh, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  EXH_CUDA_TRY(cudaStreamSynchronize(st));
+  *out |= 1ull;       // 0 stays "no digest"
+  return EXH_OK;
+}
+
+// grid_hash != 0: the peaks and their sorted order of a grid with that
+// digest are reused from the previous call (they do not depend on the
+// barrier, the cosmology or Nmin), so repeated halo finding on one grid --
+// barrier fits -- skips peak finding and the sort
 int run_halo_finder(Ctx& c, const BoxParams& b, const float* k, const float* P, int Nk, int setup_fp64,
-                    const float* delta, HaloDev* h, ShellTable* t, cudaStream_t st) {
+                    const float* delta, HaloDev* h, ShellTable* t, cudaStream_t st, unsigned long long grid_hash = 0) {
   HostTables& tab = c.halos.tab;
   // the tables depend on P(k), the cosmology, the cell and the barrier only:
   // reuse them across realisations (the key holds every input bit)
@@ -70,10 +103,26 @@ int run_halo_finder(Ctx& c, const BoxParams& b, const float* k, const float* P, 
   EXH_TRY(c.buf[B_HOSTIO].ensure(sizeof(float) * tab.Ncells));
   float* Btab_dev = c.buf[B_HOSTIO].as<float>();
   EXH_CUDA_TRY(cudaMemcpyAsync(Btab_dev, tab.Btab.data(), sizeof(float) * tab.Ncells, cudaMemcpyHostToDevice, st));
-  EXH_TRY(find_peaks(c, delta, b, h, st));
-  if (c.verbose) { printf("There are %lld peaks\n", (long long)h->np); fflush(stdout); }
-  EXH_TRY(sort_peaks(c, h, st));
-  if (c.verbose) { printf("peaks sorted\n"); fflush(stdout); }
+  const bool reuse = grid_hash != 0 && grid_hash == c.peak_hash && c.peak_nd[0] == b.nd[0] &&
+                     c.peak_nd[1] == b.nd[1] && c.peak_nd[2] == b.nd[2];
+  if (reuse) {
+    h->np = c.peak_np;
+    h->key = c.peak_key;
+    h->id = c.peak_id;
+  } else {
+    c.peak_hash = 0;
+    EXH_TRY(find_peaks(c, delta, b, h, st));
+    if (c.verbose) { printf("There are %lld peaks\n", (long long)h->np); fflush(stdout); }
+    EXH_TRY(sort_peaks(c, h, st));
+    if (c.verbose) { printf("peaks sorted\n"); fflush(stdout); }
+    if (grid_hash != 0) {
+      c.peak_hash = grid_hash;
+      c.peak_nd[0] = b.nd[0]; c.peak_nd[1] = b.nd[1]; c.peak_nd[2] = b.nd[2];
+      c.peak_np = h->np;
+      c.peak_key = h->key;
+      c.peak_id = h->id;
+    }
+  }
   HaloScalars hs;
   hs.Bmin = tab.Btab[tab.Ncells - 1];
   hs.Mtot = b.Mtot;
@@ -244,7 +293,9 @@ int exh_find_halos(exh_ctx* ctx, const float* delta, int ndx, int ndy, int ndz, 
   }
   HaloDev h;
   ShellTable t;
-  EXH_TRY(run_halo_finder(c, b, k, P, Nk, prm->setup_fp64, d, &h, &t, st));
+  unsigned long long digest = 0;
+  EXH_TRY(grid_digest(c, d, b.ng, st, &digest));
+  EXH_TRY(run_halo_finder(c, b, k, P, Nk, prm->setup_fp64, d, &h, &t, st, digest));
   const size_t nh = std::max<int64_t>(h.nh, 1);
   EXH_TRY(c.buf[B_POSH].ensure(sizeof(float) * 6 * nh));
   float* posh = c.buf[B_POSH].as<float>();

@@ -74,3 +74,18 @@ def power_compute(grid, ntype, nd, L, window, R, interlacing, Nk, k_min, k_max, 
                                             interlacing, Nk, float(k_min), float(k_max), l_max, direction,
                                             _capi.ptr(k), _capi.ptr(P), _capi.ptr(cnt), _capi.EXH_MEM_HOST, None))
     return {"k": k, "Pk": P, "Nk": cnt}
+
+
+def abundance_compute(Mh_array, Mmin, Mmax, Nm, Lc, ndx, ndy, ndz, verbose):
+    """{"Mh", "dn", "dn_err"}: differential abundance of a halo catalogue
+    (spectrum.c:535-600, abundance.c:4-36) in Nm log-mass bins; Mmin or
+    Mmax < 0 take the catalogue's range widened by 1e-4."""
+    M = np.ascontiguousarray(Mh_array, dtype=np.float32).reshape(-1)
+    Nm = int(Nm)
+    out = {"Mh": np.zeros(Nm, dtype=np.float32), "dn": np.zeros(Nm, dtype=np.float32),
+           "dn_err": np.zeros(Nm, dtype=np.float32)}
+    _capi.check(_capi.load().exh_abundance_compute(_capi.context(), _capi.ptr(M), M.size, float(Mmin), float(Mmax),
+                                                   Nm, float(Lc), int(ndx), int(ndy), int(ndz),
+                                                   _capi.ptr(out["Mh"]), _capi.ptr(out["dn"]),
+                                                   _capi.ptr(out["dn_err"]), _capi.EXH_MEM_HOST, None))
+    return out

@@ -124,3 +124,26 @@ def Compute_Power_Spectrum(
     if ntypes == 1 and l_max == 0:
         x["Pk"] = x["Pk"].reshape([Nk])
     return x
+
+
+def Compute_Abundance(
+    Mh: np.ndarray,
+    Mmin: Optional[float] = None,
+    Mmax: Optional[float] = None,
+    Nm: int = 25,
+    Lc: float = 2.0,
+    nd: int = 256,
+    ndx: Optional[int] = None,
+    ndy: Optional[int] = None,
+    ndz: Optional[int] = None,
+    verbose: bool = False,
+) -> Dict[str, np.ndarray]:
+    """Differential abundance of a halo catalogue (simulation.py:719-806):
+    {"Mh": mean mass per bin, "dn": dn/dlnM, "dn_err": Poisson error}."""
+    Mmin = -1.0 if Mmin is None else Mmin
+    Mmax = -1.0 if Mmax is None else Mmax
+    ndx = nd if ndx is None else ndx
+    ndy = nd if ndy is None else ndy
+    ndz = nd if ndz is None else ndz
+    return _spec.abundance_compute(np.asarray(Mh).astype("float32"), np.float32(Mmin), np.float32(Mmax), np.int32(Nm),
+                                   np.float32(Lc), np.int32(ndx), np.int32(ndy), np.int32(ndz), np.int32(verbose))

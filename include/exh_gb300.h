@@ -99,6 +99,16 @@ int exh_power_compute_ex(exh_ctx *ctx, const float *grid, int ntype, int nd, flo
                          int interlacing, int Nk, float k_min, float k_max, int l_max, int direction,
                          float *k_out, float *P_out, int64_t *count_out, int mem, void *stream);
 
+/* abundance_compute (src/spectrum/spectrum.c:535-600 -> Measure_Abundance,
+ * src/spectrum/abundance.c:4-36): differential mass function of nh halo
+ * masses (in `mem`) in Nm log bins between Mmin and Mmax (negative: from the
+ * masses, widened by 1e-4 as the reference does) in a box of
+ * (Lc ndx) (Lc ndy) (Lc ndz).  Mmean, dn, dn_err: Nm floats on the host.  As in
+ * the reference, the first bin is never filled. */
+int exh_abundance_compute(exh_ctx *ctx, const float *Mh, int64_t nh, float Mmin, float Mmax, int Nm, float Lc,
+                          int ndx, int ndy, int ndz, float *Mmean, float *dn, float *dn_err, int mem,
+                          void *stream);
+
 /* Power spectrum for callers that cannot allocate device memory: real-time
  * loops that must not stall in the allocator, and hosts whose device memory
  * is handed out by a pool or framework that owns all of it.

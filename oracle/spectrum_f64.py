@@ -187,3 +187,25 @@ def power(grid, L, ntype=1, window=2, R=4.0, interlacing=0, Nk=25, kmin=None, km
     for s in range(ls):
         P[:, s] = np.where(n > 0, (4 * s + 1) * P[:, s] / np.maximum(n, 1), 0.0)
     return {"k": np.where(n > 0, kmean / np.maximum(n, 1), 0.0), "Pk": P, "Nk": n.astype(np.int64)}
+
+
+def abundance(Mh, Mmin, Mmax, Nm, Lc, ndx, ndy, ndz):
+    """Measure_Abundance (src/spectrum/abundance.c:4-36) with the range rule
+    of abundance_compute (src/spectrum/spectrum.c:566-578); the mean masses in
+    FP64"""
+    f32 = np.float32
+    M = np.asarray(Mh, dtype=f32).reshape(-1)
+    if Mmin < 0:
+        Mmin = f32(min(float(M.min()) if M.size else 1e20, 1e20) * 0.9999)
+    if Mmax < 0:
+        Mmax = f32(float(M.max()) * 1.0001)
+    dlnM = f32((np.log(float(Mmax)) - np.log(float(Mmin))) / Nm)
+    ind = np.floor((np.log(M.astype(np.float64)) - np.log(float(Mmin))) / float(dlnM)).astype(np.int64)
+    ok = (ind > 0) & (ind < Nm)
+    N = np.bincount(ind[ok], minlength=Nm)[:Nm]
+    S = np.bincount(ind[ok], weights=M[ok].astype(np.float64), minlength=Nm)[:Nm]
+    V = f32(f32(f32(Lc) * f32(ndx)) * f32(f32(Lc) * f32(ndy))) * f32(f32(Lc) * f32(ndz))
+    dn = (N.astype(f32) / V / dlnM).astype(f32)
+    err = (np.sqrt(N.astype(np.float64)) / float(V) / float(dlnM)).astype(f32)
+    Mm = np.where(N > 0, S / np.maximum(N, 1), 0.0).astype(f32)
+    return {"Mh": Mm, "dn": dn, "dn_err": err}
