@@ -74,6 +74,24 @@ struct LadderGen {
   __device__ __forceinline__ size_t inner_size() const { return (size_t)n0 * nc; }
 };
 
+// y-pass source (the y transform runs first): stored modes times W(|k| R);
+// its tiles read runs of kz within one x plane, a better DRAM pattern than
+// the x pass's planes 2 nd nc bytes apart
+struct LadderGenY {
+  static constexpr int io_bytes = 8;
+  const float2* __restrict__ dk;
+  const float* __restrict__ w;
+  int n0, nc, h;
+  __device__ __forceinline__ float2 operator()(int o, int e, int k) const {
+    const int ii = (2 * o < n0) ? o : o - n0;
+    const int jj = (2 * e < n0) ? e : e - n0;
+    const int kk = (k == h) ? -h : k;
+    const float wv = __ldg(&w[ii * ii + jj * jj + kk * kk]);
+    const float2 v = dk[((size_t)o * n0 + e) * nc + k];
+    return make_float2(v.x * wv, v.y * wv);
+  }
+};
+
 // z-pass destination: barrier test, first crossing kept
 struct CrossStore {
   static constexpr int io_bytes = 4;     // two u8 reads and writes per pair
@@ -210,11 +228,13 @@ int smoothing_ladder(Ctx& c, const BoxParams& b, const FieldModes& modes, int n_
   for (int i = n_radii - 1; i >= 0; i--) {       // large scales first
     LadderGen gen{dk, wtab + (size_t)i * nn, b.nd[0], p->nc, h};
     CrossStore cs{cross, b.nd[2], b.Normx, B[i], i};
-    // x and y passes, then the z pass with the barrier test
-    EXH_CUDA_TRY(launch_strided(gen, CplxStore{work, p->nx, p->ny * p->nc}, p->px, p->twx, 1.f, 1, p->ny * p->nc,
-                                st));
-    EXH_CUDA_TRY(launch_strided(CplxLoad{work, p->ny, p->nc}, CplxStore{work, p->ny, p->nc}, p->py, p->twy, 1.f,
-                                p->nx, p->nc, st));
+    // y then x (both complex, in either order), then the z pass with the
+    // barrier test; the mode read and the window sit in the y pass
+    (void)gen;
+    EXH_CUDA_TRY(launch_strided(LadderGenY{dk, wtab + (size_t)i * nn, b.nd[0], p->nc, h},
+                                CplxStore{work, p->ny, p->nc}, p->py, p->twy, 1.f, p->nx, p->nc, st));
+    EXH_CUDA_TRY(launch_strided(CplxLoad{work, p->nx, p->ny * p->nc}, CplxStore{work, p->nx, p->ny * p->nc}, p->px,
+                                p->twx, 1.f, 1, p->ny * p->nc, st));
     cudaError_t e = cudaSuccess;
     if (!launch_ladder_z(*p, work, cross, b.Normx, B[i], i, st, &e))
       e = launch_c2r_rows(HalfLoad{work, p->nc}, cs, *p, (size_t)p->nx * p->ny, st);
