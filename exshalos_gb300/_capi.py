@@ -49,6 +49,13 @@ class DiffParams(C.Structure):
                 ("k_max", C.c_float)]
 
 
+class HodParams(C.Structure):
+    _fields_ = [("Lc", C.c_float), ("Om0", C.c_float), ("redshift", C.c_float),
+                ("ndx", C.c_int32), ("ndy", C.c_int32), ("ndz", C.c_int32),
+                ("logMmin", C.c_float), ("siglogM", C.c_float), ("logM0", C.c_float), ("logM1", C.c_float),
+                ("alpha", C.c_float), ("sigma", C.c_float), ("Deltah", C.c_float), ("seed", C.c_int32)]
+
+
 # every symbol the header declares, with its argument and result types
 _P = C.c_void_p
 SIGNATURES = {
@@ -79,6 +86,11 @@ SIGNATURES = {
                                       C.c_int, C.c_int, C.c_float, C.c_float, C.c_int, C.c_int, _P, C.c_int, _P]),
     "exh_power_compute_ex": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_float, C.c_int, C.c_float, C.c_int, C.c_int,
                                        C.c_float, C.c_float, C.c_int, C.c_int, _P, _P, _P, C.c_int, _P]),
+    "exh_hod_populate": (C.c_int, [_P, _P, _P, _P, _P, C.c_int64, C.POINTER(HodParams), C.c_int,
+                                   C.POINTER(C.c_int64), C.c_int, _P]),
+    "exh_hod_fetch": (C.c_int, [_P, _P, _P, _P, C.c_int, _P]),
+    "exh_hod_split": (C.c_int, [_P, _P, C.c_int64, _P, C.c_int64, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, _P,
+                                C.c_int, _P]),
     "exh_abundance_compute": (C.c_int, [_P, _P, C.c_int64, C.c_float, C.c_float, C.c_int, C.c_float, C.c_int, C.c_int,
                                         C.c_int, _P, _P, _P, C.c_int, _P]),
     "exh_smoothing_ladder": (C.c_int, [_P, _P, _P, C.c_int, C.POINTER(HaloParams), C.c_int, C.c_float, _P, _P, _P,

@@ -78,6 +78,9 @@ enum BufId {
   B_POSH,         // halo positions / velocities
   B_MH,
   B_TAB,          // device copies of tables
+  B_HODIN,        // galaxy population: staged halo inputs
+  B_HOD,          // galaxy population: per-halo work, stream, tables
+  B_HODG,         // galaxy population: the galaxies of the last call
   B_SCRATCH,      // per-block partials, counters
   B_HOSTIO,       // staging for host pointers
   B_HOSTIO2,
@@ -109,6 +112,10 @@ struct Ctx {
   float* peak_key = nullptr;
   unsigned* peak_id = nullptr;
   DiffState* diff = nullptr;
+  // galaxies of the last exh_hod_populate (B_HODG)
+  int64_t hod_ng = -1;
+  int hod_vel = 0;
+  size_t hod_off = 0;                   // galaxies start after the random stream
   // lanes of the batched runner: contexts with their own streams
   std::vector<exh_ctx*> lane_ctx;
   std::vector<cudaStream_t> lane_st;

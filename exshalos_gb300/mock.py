@@ -126,3 +126,84 @@ def Generate_Halos_Box_from_Grid(
         k, P, grid, S, V, Lc, k_smooth, Om0, z, delta_c, np.int32(Nmin), a, beta, alpha, np.int32(OUT_LPT),
         np.int32(OUT_VEL), np.int32(DO_2LPT), np.int32(OUT_FLAG), np.int32(In_disp), np.int32(OUT_PROF),
         np.int32(verbose), np.int32(nthreads))
+
+
+def Generate_Galaxies_from_Halos(
+    posh: np.ndarray,
+    Mh: np.ndarray,
+    velh: Optional[np.ndarray] = None,
+    Ch: Optional[np.ndarray] = None,
+    nd: int = 256,
+    ndx: int = 0,
+    ndy: int = 0,
+    ndz: int = 0,
+    Lc: float = 2.0,
+    Om0: float = 0.31,
+    z: float = 0.0,
+    logMmin: float = 13.25424743,
+    siglogM: float = 0.26461332,
+    logM0: float = 13.28383025,
+    logM1: float = 14.32465146,
+    alpha: float = 1.00811277,
+    sigma: float = 0.5,
+    Deltah: float = -1.0,
+    seed: int = 12345,
+    OUT_VEL: bool = False,
+    OUT_FLAG: bool = False,
+    verbose: bool = False,
+) -> Dict[str, np.ndarray]:
+    """Galaxy catalogue of a halo catalogue (mock.py:357-507): Zheng (2005)
+    occupations, centrals at the halo centres, satellites around them.
+
+    Returns {"posg"[, "velg" with OUT_VEL][, "flag" with OUT_FLAG]}; flag is
+    -i for the central of halo i and i for its satellites.  As in the
+    reference, ndx/ndy/ndz fall back to nd only when None: with the default 0
+    the box length along that axis is 0 and satellite positions are not
+    wrapped into the box.
+    """
+    from .lib import hod as _hod
+
+    In_C = Ch is not None
+    posh = np.asarray(posh).astype("float32")
+    if velh is not None:
+        velh = np.asarray(velh).astype("float32")
+    Mh = np.asarray(Mh).astype("float32")
+    if In_C:
+        Ch = np.asarray(Ch).astype("float32")
+    if ndx is None:
+        ndx = nd
+    if ndy is None:
+        ndy = nd
+    if ndz is None:
+        ndz = nd
+    return _hod.populate_halos(
+        posh, velh, Mh, Ch, np.float32(Lc), np.float32(Om0), np.float32(z), np.int32(ndx), np.int32(ndy),
+        np.int32(ndz), np.float32(logMmin), np.float32(siglogM), np.float32(logM0), np.float32(logM1),
+        np.float32(alpha), np.float32(sigma), np.float32(Deltah), np.int32(seed), np.int32(OUT_VEL),
+        np.int32(OUT_FLAG), np.int32(In_C), np.int32(verbose))
+
+
+def Split_Galaxies(
+    Mh: np.ndarray,
+    Flag: np.ndarray,
+    params_cen: np.ndarray = np.array([37.10265321, -5.07596644, 0.17497771]),
+    params_sat: np.ndarray = np.array([19.84341938, -2.8352781, 0.10443049]),
+    seed: int = 12345,
+    verbose: bool = False,
+) -> np.ndarray:
+    """Type of each galaxy from polynomial occupations in log10(Mh)
+    (mock.py:519-576): int32, +-(1..ntypes), negative for centrals."""
+    from .lib import hod as _hod
+
+    Mh = np.asarray(Mh).astype("float32")
+    params_cen = np.asarray(params_cen).astype("float32")
+    params_sat = np.asarray(params_sat).astype("float32")
+    if len(params_cen.shape) == 1:
+        params_cen = params_cen.reshape([1, len(params_cen)])
+    if len(params_sat.shape) == 1:
+        params_sat = params_sat.reshape([1, len(params_sat)])
+    if params_cen.shape[0] != params_sat.shape[0]:
+        raise ValueError(
+            "Different number of types of galaxies for the centrals and satellites! %d != %d!"
+            % (params_cen.shape[0], params_sat.shape[0]))
+    return _hod.split_galaxies(Mh, Flag, params_cen, params_sat, np.int32(seed), np.int32(verbose))

@@ -257,6 +257,40 @@ int exh_diff_forward(exh_ctx *ctx, const exh_diff_params *prm, const float *nois
                      float *P_out, float *k_out, int64_t *count_out, void *stream);
 int exh_diff_backward(exh_ctx *ctx, double grad_loss, float *grad_noise, double *grad_knots, void *stream);
 
+/* Galaxy population of a halo catalogue: populate_halos (src/hod/hod.c:31-160
+ * -> Populate_total, src/hod/populate_halos.c:120-217).  Arguments as the
+ * reference's keyword list; Om0 and Deltah only enter the virial radius,
+ * which the reference computes and does not use.  The galaxies (centrals at
+ * the halo centre with flag -i, satellites with flag i, halo by halo) follow
+ * the reference's gsl_rng_taus stream seeded with `seed`. */
+typedef struct {
+  float Lc, Om0, redshift;
+  int32_t ndx, ndy, ndz;   /* box side Lc * nd per axis; 0 leaves that axis unwrapped */
+  float logMmin, siglogM, logM0, logM1, alpha, sigma, Deltah;
+  int32_t seed;
+} exh_hod_params;
+
+/* posh[nh][3], velh[nh][3] (read when out_vel), Mh[nh], Ch[nh] (NULL: the
+ * concentration f_c(M) of populate_halos.c:21-27) in `mem`.  Writes the
+ * number of galaxies to *ng_out; the catalogue stays in the context until
+ * the next call.  EXH_E_INVALID for non-positive or non-finite masses or
+ * concentrations, or a mean satellite number above 1e6. */
+int exh_hod_populate(exh_ctx *ctx, const float *posh, const float *velh, const float *Mh, const float *Ch,
+                     int64_t nh, const exh_hod_params *p, int out_vel, int64_t *ng_out, int mem, void *stream);
+/* Copies the last catalogue: posg[ng][3], velg[ng][3], flag[ng]; any may be
+ * NULL (velg must be NULL when populated without velocities). */
+int exh_hod_fetch(exh_ctx *ctx, float *posg, float *velg, int64_t *flag, int mem, void *stream);
+
+/* Colour split, split_galaxies (src/hod/hod.c:163-211 -> Galaxy_Types,
+ * src/hod/split_galaxies.c:37-72): type_out[ng] = +-(1..ntypes) from halo
+ * masses Mh[nh], galaxy flags flag[ng] and the occupation polynomials
+ * params_cen[(ntypes-1) * order_cen], params_sat[(ntypes-1) * order_sat],
+ * one uniform of a taus stream seeded with `seed` per galaxy.  EXH_E_INVALID
+ * when a flag names a halo outside [0, nh). */
+int exh_hod_split(exh_ctx *ctx, const float *Mh, int64_t nh, const int64_t *flag, int64_t ng,
+                  const float *params_cen, const float *params_sat, int ntypes, int order_cen, int order_sat,
+                  int seed, int32_t *type_out, int mem, void *stream);
+
 /* 3-D FFTs with FFTW conventions (unnormalised, half-complex last axis,
  * interleaved float2) — the transforms fftwf_plan_dft_r2c_3d /
  * fftwf_plan_dft_c2r_3d perform at src/spectrum/spectrum_h.c:103-107 and

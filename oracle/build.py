@@ -12,7 +12,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRCS = ["orc_rng.c", "orc_spline.c", "orc_setup.c", "orc_fft.c", "orc_field.c",
-        "orc_halos.c", "orc_lpt.c", "orc_spectrum.c", "orc_pipeline.c"]
+        "orc_halos.c", "orc_lpt.c", "orc_spectrum.c", "orc_pipeline.c", "orc_hod.c"]
 OUT = os.path.join(HERE, "_build")
 
 

@@ -181,6 +181,18 @@ int  orc_halos_box_from_pk(const float *K, const float *P, int Nk, int nd, float
 void orc_free(void *ptr);
 void orc_result_free(orc_result *r);
 
+/* --------------------------------------------------------------- hod */
+/* populate_halos (src/hod/hod.c:31-160, populate_halos.c:120-217); Ch may be
+ * NULL.  Returns the galaxy count, -1 beyond cap, -2 on a table error. */
+long long orc_populate_halos(const real *posh, const real *velh, const real *Mh, const real *Ch, long long nh,
+                             real Lc, real redshift, int ndx, int ndy, int ndz, real logMmin, real siglogM,
+                             real logM0, real logM1, real alpha, real sigma, int seed, int out_vel,
+                             long long cap, real *posg, real *velg, int64_t *gal_type, int *nsat_out,
+                             int *ncen_out);
+/* split_galaxies (hod.c:163-211, split_galaxies.c:37-72); 1 on a bad flag */
+int orc_split_galaxies(long long ng, const real *Mh, long long nh, const int64_t *flag, const real *params_cen,
+                       const real *params_sat, int ntypes, int order_cen, int order_sat, int seed, int *type);
+
 #ifdef __cplusplus
 }
 #endif

@@ -279,3 +279,55 @@ def ladder(p, modes, R, B, prec="f64"):
     if lib(prec).orc_ladder(C.byref(p), _ptr(np.ascontiguousarray(modes)), R.size, _ptr(R), _ptr(B), _ptr(out)):
         raise RuntimeError("oracle ladder failed")
     return out
+
+
+def populate_halos(posh, Mh, velh=None, Ch=None, Lc=2.0, z=0.0, nd=(0, 0, 0), logMmin=13.25424743,
+                   siglogM=0.26461332, logM0=13.28383025, logM1=14.32465146, alpha=1.00811277, sigma=0.5,
+                   seed=12345, out_vel=False, prec="f32"):
+    """Galaxies of a halo catalogue on the reference's sequential taus stream:
+    {"posg", "velg", "flag", "nsat", "ncen"} (nsat, ncen per halo)."""
+    rt = real_dtype(prec)
+    cr = C.c_float if prec == "f32" else C.c_double
+    L = lib(prec)
+    L.orc_populate_halos.restype = C.c_longlong
+    posh = np.ascontiguousarray(posh, dtype=rt).reshape(-1, 3)
+    Mh = np.ascontiguousarray(Mh, dtype=rt).reshape(-1)
+    nh = Mh.size
+    v = np.ascontiguousarray(velh, dtype=rt).reshape(-1, 3) if out_vel else None
+    c = np.ascontiguousarray(Ch, dtype=rt).reshape(-1) if Ch is not None else None
+    cap = 64 * max(nh, 1) + 1024
+    while True:
+        posg = np.zeros((cap, 3), dtype=rt)
+        velg = np.zeros((cap, 3), dtype=rt) if out_vel else None
+        flag = np.zeros(cap, dtype=np.int64)
+        nsat = np.zeros(max(nh, 1), dtype=np.int32)
+        ncen = np.zeros(max(nh, 1), dtype=np.int32)
+        ng = L.orc_populate_halos(_ptr(posh), _ptr(v) if v is not None else None, _ptr(Mh),
+                                  _ptr(c) if c is not None else None, C.c_longlong(nh), cr(Lc), cr(z),
+                                  int(nd[0]), int(nd[1]), int(nd[2]), cr(logMmin), cr(siglogM), cr(logM0),
+                                  cr(logM1), cr(alpha), cr(sigma), int(seed), int(bool(out_vel)),
+                                  C.c_longlong(cap), _ptr(posg), _ptr(velg) if velg is not None else None,
+                                  _ptr(flag), _ptr(nsat), _ptr(ncen))
+        if ng == -1:
+            cap *= 4
+            continue
+        if ng < 0:
+            raise RuntimeError("oracle r(Eps) tables failed")
+        out = {"posg": posg[:ng], "flag": flag[:ng], "nsat": nsat[:nh], "ncen": ncen[:nh]}
+        if out_vel:
+            out["velg"] = velg[:ng]
+        return out
+
+
+def split_galaxies(Mh, flag, params_cen, params_sat, seed=12345, prec="f32"):
+    """Galaxy types (signed, as split_galaxies.c) on the reference's taus stream."""
+    rt = real_dtype(prec)
+    Mh = np.ascontiguousarray(Mh, dtype=rt).reshape(-1)
+    flag = np.ascontiguousarray(flag, dtype=np.int64).reshape(-1)
+    pc = np.ascontiguousarray(np.atleast_2d(params_cen), dtype=rt)
+    ps = np.ascontiguousarray(np.atleast_2d(params_sat), dtype=rt)
+    out = np.zeros(flag.size, dtype=np.int32)
+    if lib(prec).orc_split_galaxies(C.c_longlong(flag.size), _ptr(Mh), C.c_longlong(Mh.size), _ptr(flag), _ptr(pc),
+                                    _ptr(ps), pc.shape[0] + 1, pc.shape[1], ps.shape[1], int(seed), _ptr(out)):
+        raise ValueError("a flag names a halo outside the catalogue")
+    return out
