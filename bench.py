@@ -288,6 +288,79 @@ def diff_summary(k, P, reps=3):
             "loss": loss}
 
 
+def galaxies_summary(k, P, reps=3, cpu=True):
+    """Galaxy population of one 256^3 halo catalogue (seed 1, 2LPT, barrier
+    a=1 beta=0.12, Lc=2; about 1e6 halos) with the reference's default HOD
+    (Zheng 2005 parameters, sigma=0.5, taus seed 12345, nd=256 so satellites
+    wrap): the device-resident C-ABI call timed with CUDA events (median of
+    reps), the public host-array call and the colour split by wall clock, and
+    the sequential oracle (the reference's algorithm, one thread) on the same
+    catalogue."""
+    import ctypes as C
+
+    import torch
+    from exshalos_gb300 import _capi, mock
+    r = mock.Generate_Halos_Box_from_Pk(k, P, nd=ND, Lc=LC, seed=1, DO_2LPT=True, OUT_VEL=True, **BARRIER)
+    posh, velh, Mh = r["posh"], r["velh"], r["Mh"]
+    nh = Mh.size
+    L_ = _capi.load()
+    ctx = _capi.context()
+    dpos, dvel, dM = (torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (posh, velh, Mh))
+    prm = _capi.HodParams(LC, 0.31, 0.0, ND, ND, ND, 13.25424743, 0.26461332, 13.28383025, 14.32465146,
+                          1.00811277, 0.5, -1.0, 12345)
+    ng = C.c_int64(0)
+    out_pos = out_vel = out_flag = None
+    times = []
+    for rep in range(reps + 1):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _capi.check(L_.exh_hod_populate(ctx, dpos.data_ptr(), dvel.data_ptr(), dM.data_ptr(), None, nh,
+                                        C.byref(prm), 1, C.byref(ng), _capi.EXH_MEM_DEVICE, None))
+        if out_pos is None:
+            n = int(ng.value)
+            out_pos = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+            out_vel = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+            out_flag = torch.empty(n, dtype=torch.int64, device="cuda")
+        _capi.check(L_.exh_hod_fetch(ctx, out_pos.data_ptr(), out_vel.data_ptr(), out_flag.data_ptr(),
+                                     _capi.EXH_MEM_DEVICE, None))
+        e1.record()
+        torch.cuda.synchronize()
+        if rep:
+            times.append(e0.elapsed_time(e1))
+    t_dev = float(np.median(times))
+    n = int(ng.value)
+    kw = dict(ndx=ND, ndy=ND, ndz=ND, Lc=LC, OUT_VEL=True, OUT_FLAG=True)
+    mock.Generate_Galaxies_from_Halos(posh, Mh, velh=velh, **kw)
+    t0 = time.perf_counter()
+    g = mock.Generate_Galaxies_from_Halos(posh, Mh, velh=velh, **kw)
+    t_e2e = time.perf_counter() - t0
+    mock.Split_Galaxies(Mh, g["flag"])
+    t0 = time.perf_counter()
+    mock.Split_Galaxies(Mh, g["flag"])
+    t_split = time.perf_counter() - t0
+    base = None
+    if cpu:
+        from oracle import orc
+        t0 = time.perf_counter()
+        want = orc.populate_halos(posh, Mh, velh=velh, Lc=LC, nd=(ND, ND, ND), out_vel=True)
+        t_cpu = time.perf_counter() - t0
+        same = bool(np.array_equal(want["flag"], g["flag"]) and
+                    np.max(np.abs(want["posg"] - g["posg"]), initial=0.0) < 1e-4)
+        base = {"value": want["posg"].shape[0] / t_cpu, "unit": "galaxies/s", "cores": 1, "kind": "port",
+                "ms": round(1000.0 * t_cpu, 3), "sample": "the whole catalogue, the reference's sequential algorithm",
+                "speedup_device": round(t_cpu / (t_dev / 1000.0), 2), "speedup_e2e": round(t_cpu / t_e2e, 2),
+                "identical_catalogue": same}
+    return {"workload": "galaxies_256: halos of one 256^3 box (seed 1) populated with the default HOD, "
+                        "positions + velocities + flags",
+            "halos": int(nh), "galaxies": n, "random_satellite_draws": int(np.sum(Mh >= 10 ** 13.28383025)),
+            "device_ms": round(t_dev, 3), "galaxies_per_s": n / (t_dev / 1000.0),
+            "e2e_ms": round(1000.0 * t_e2e, 3), "split_e2e_ms": round(1000.0 * t_split, 3),
+            "cpu_baseline": base,
+            "timing": "device: CUDA events around exh_hod_populate + exh_hod_fetch on device arrays; "
+                      "e2e/split/cpu: host wall clock"}
+
+
 def run_ours(args, ws, rank, local):
     os.environ["EXH_DEVICE"] = str(local)
     import ctypes as C
@@ -386,6 +459,7 @@ def run_ours(args, ws, rank, local):
     traffic = committed_traffic().get(name)
     batched = None if args.no_batched else batched_summary(k, P, args.lanes, seed0=1000 * rank)
     differentiable = None if args.no_batched else diff_summary(k, P)
+    galaxies = None if args.no_batched else galaxies_summary(k, P, reps=5, cpu=not args.no_cpu_baseline)
     if rank != 0:
         return
     cpu = None
@@ -418,6 +492,7 @@ def run_ours(args, ws, rank, local):
         "cpu_baseline": cpu,
         "batched": batched,
         "differentiable": differentiable,
+        "galaxies": galaxies,
     }
     print(json.dumps(line), flush=True)
 
@@ -506,14 +581,24 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-workload summary")
     ap.add_argument("--lanes", type=int, default=12, help="lanes of the batched runner")
-    ap.add_argument("--workload", default="box_256", choices=["box_256", "box_512"],
-                    help="box_256: the headline line; box_512: the large-box kernel-class report")
+    ap.add_argument("--workload", default="box_256", choices=["box_256", "box_512", "galaxies_256"],
+                    help="box_256: the headline line; box_512: the large-box kernel-class report; "
+                         "galaxies_256: the galaxy-population summary alone")
     args = ap.parse_args()
     ws, rank, local = dist_init()
     if args.impl == "reference":
         run_reference(args, ws, rank)
     elif args.workload == "box_512":
         run_box512(args, ws, rank, local)
+    elif args.workload == "galaxies_256":
+        if rank == 0:
+            os.environ["EXH_DEVICE"] = str(local)
+            import torch
+            torch.cuda.set_device(local)
+            from exshalos_gb300.workloads import synthetic_pk
+            k, P = synthetic_pk()
+            print(json.dumps(galaxies_summary(k.astype(np.float32), P.astype(np.float32), reps=5,
+                                              cpu=not args.no_cpu_baseline)), flush=True)
     else:
         run_ours(args, ws, rank, local)
     if ws > 1:

@@ -10,12 +10,12 @@
 //                      concentration range, and whether the satellite draw is
 //                      random (<Nsat> > 0: its uniform count depends on the draw)
 //   2. k_taus_stream   the stream itself, 64 values per thread from a jump-ahead
-//   3. k_hod_parse     one warp walks the halos with <Nsat> > 0 in order and
+//   3. k_hod_parse     one block walks the halos with <Nsat> > 0 in order and
 //                      fixes each one's satellite count; a halo with <Nsat> = 0
 //                      always takes two uniforms, so only the random ones need
-//                      the walk.  The 32 lanes draw the next 32 halos at the
-//                      current offset; every lane up to the first one with
-//                      satellites drew from its true offset and commits.
+//                      the walk.  Each round draws the next 64 halos at 64
+//                      candidate stream offsets in parallel and then follows
+//                      the chain of true offsets through shared memory.
 //   4. scans           stream offset of every halo (2 i + extra uniforms before
 //                      it), galaxies per halo, galaxy offsets
 //   5. k_hod_write     central and satellites of every halo, in the reference's
@@ -127,11 +127,36 @@ k_hod_prep(const float* __restrict__ Mh, const float* __restrict__ Ch_in, int64_
   }
 }
 
-// list[pos[i]] = i for the halos whose satellite draw is random
-__global__ void k_hod_compact(const int* __restrict__ rnd, const int* __restrict__ pos, int64_t nh,
-                              int* __restrict__ list) {
+// one halo whose satellite draw is random: the multiplicative draw stops
+// at the first uniform u = x / 2^32 with u <= exp(-mu), i.e. x <= thr
+struct __align__(8) HodDraw {
+  int h;
+  unsigned thr;        // floor(exp(-mu) 2^32)
+  double emu;          // exp(-mu)
+  float emuf;          // exp(-mu) rounded to float
+  int mode;            // 0: float test with a certified band, 1: double products, 2: pieces (mu > 500)
+};
+
+__global__ void k_hod_compact(const int* __restrict__ rnd, const int* __restrict__ pos, const float* __restrict__ mu,
+                              int64_t nh, HodDraw* __restrict__ hm) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nh; i += (int64_t)gridDim.x * blockDim.x)
-    if (rnd[i]) list[pos[i]] = (int)i;
+    if (rnd[i]) {
+      const double m = (double)mu[i];
+      HodDraw d;
+      d.h = (int)i;
+      if (m <= 500.0) {
+        d.emu = exp(-m);
+        d.thr = (unsigned)floor(__dmul_rn(d.emu, 4294967296.0));   // exact scaling; emu < 1
+        d.emuf = (float)d.emu;
+        d.mode = m <= 60.0 ? 0 : 1;            // exp(-60) ~ 1e-26 stays a normal float
+      } else {
+        d.emu = 0.0;
+        d.thr = 0u;
+        d.emuf = 0.f;
+        d.mode = 2;
+      }
+      hm[pos[i]] = d;
+    }
 }
 
 // stream values [t*CHUNK, (t+1)*CHUNK): value p is the (p+1)-th draw after seeding
@@ -179,35 +204,177 @@ __device__ __forceinline__ bool hod_poisson(double mu, const unsigned* __restric
   return true;
 }
 
-// one warp: satellite counts of the halos with a random draw, in order
-__global__ void __launch_bounds__(32)
-k_hod_parse(const int* __restrict__ list, int K, const float* __restrict__ mu, const unsigned* __restrict__ st,
-            int64_t Ls, int* __restrict__ nsat, long long* __restrict__ extra, HodCtl* __restrict__ ctl) {
-  const int lane = threadIdx.x;
-  long long E = 0;        // uniforms beyond two per halo, over the halos already fixed
-  for (int k = 0; k < K;) {
-    const int idx = k + lane;
-    int h = -1, ns = 0, used = 0;
-    long long ex = 0;
-    bool ok = true;
-    if (idx < K) {
-      h = list[idx];
-      const int64_t o = 2 * (int64_t)h + E;           // this halo's central draw
-      ok = hod_poisson((double)mu[h], st, Ls, o + 1, &ns, &used);
-      ex = (long long)used + 3LL * ns - 1;             // 1 + used + 3 ns uniforms in all, minus 2
+// Satellite counts of the halos with a random draw, in halo order, by one
+// block.  A round takes the next PARSE_H halos and draws each of them at
+// PARSE_C candidate offsets E, E+4, ..., E+4(PARSE_C-1) (E: uniforms beyond
+// two per halo so far; a halo with ns satellites from the multiplicative
+// draw takes 4 ns more, so E moves in steps of 4).  Thread 0 then follows
+// the chain through shared memory: halo q reads its result at the offset
+// the halos before it left, while that offset is a candidate.  At least one
+// halo commits per round (the first one's candidate 0 is exact).
+constexpr int PARSE_H = 64;
+constexpr int PARSE_C = 64;
+constexpr int PARSE_T = 512;
+constexpr int PARSE_HPW = PARSE_H / (PARSE_T / 32);       // halos per warp
+constexpr int PARSE_PER = PARSE_H * PARSE_C / PARSE_T;    // candidates per thread
+
+constexpr int PARSE_PRE = 3;     // stream values fetched ahead per candidate
+
+// the double product u_p u_{p+1} ... u_{p+n-1} in the draw's order
+__device__ __noinline__ double hod_prod(const unsigned* __restrict__ st, int64_t p, int n) {
+  double pr = taus_u01(st[p]);
+  for (int j = 1; j < n; j++) pr = __dmul_rn(pr, taus_u01(st[p + j]));
+  return pr;
+}
+
+// stream value p + u: from the prefetched ones when u < PARSE_PRE
+__device__ __forceinline__ unsigned hod_value(const unsigned (&x)[PARSE_PRE], const unsigned* __restrict__ st,
+                                              int64_t p, int u) {
+  unsigned v = 0u;
+  bool hit = false;
+#pragma unroll
+  for (int j = 1; j < PARSE_PRE; j++)
+    if (u == j) { v = x[j]; hit = true; }
+  return hit ? v : st[p + u];
+}
+
+// The draw of one halo from stream position p; x[] holds the values at
+// p .. p + PARSE_PRE - 1 (those below Ls).  The multiplicative draw goes on
+// while the double product exceeds exp(-mu).  In mode 0 the product is
+// carried in float: after n factors its relative distance to the double
+// product is below n 2^-23 (n roundings of the factors and n - 1 of the
+// products, each 2^-24) and exp(-mu) in float is within 2^-24, so a float
+// product outside emuf (1 +- (n + 3) 2^-22) decides the comparison; inside
+// that band the double product is formed and compared as the reference does.
+__device__ __forceinline__ bool hod_draw(const HodDraw& d, const unsigned (&x)[PARSE_PRE],
+                                         const float* __restrict__ mu, const unsigned* __restrict__ st, int64_t Ls,
+                                         int64_t p, int* ns, int* used) {
+  if (d.mode == 2) return hod_poisson((double)mu[d.h], st, Ls, p, ns, used);
+  if (p >= Ls) return false;
+  if (x[0] <= d.thr) { *ns = 0; *used = 1; return true; }
+  constexpr float TWO_M32 = 2.3283064365386963e-10f;
+  constexpr float TWO_M22 = 2.384185791015625e-07f;
+  if (d.mode == 0) {
+    float pf = __fmul_rn((float)x[0], TWO_M32);
+    int u = 1;
+    for (;;) {
+      if (p + u >= Ls) return false;
+      const unsigned v = hod_value(x, st, p, u);
+      pf = __fmul_rn(pf, __fmul_rn((float)v, TWO_M32));
+      u++;
+      const float tol = __fmul_rn((float)(u + 3), TWO_M22);
+      bool more;
+      if (pf > __fmul_rn(d.emuf, __fadd_rn(1.f, tol))) more = true;
+      else if (pf < __fmul_rn(d.emuf, __fsub_rn(1.f, tol))) more = false;
+      else more = hod_prod(st, p, u) > d.emu;
+      if (!more) break;
     }
-    if (__any_sync(0xffffffffu, !ok)) {
-      if (lane == 0) ctl->overflow = 1;
+    *ns = u - 1;
+    *used = u;
+    return true;
+  }
+  double prod = taus_u01(x[0]);
+  int u = 1;
+  do {
+    if (p + u >= Ls) return false;
+    const unsigned v = hod_value(x, st, p, u);
+    prod = __dmul_rn(prod, taus_u01(v));
+    u++;
+  } while (prod > d.emu);
+  *ns = u - 1;
+  *used = u;
+  return true;
+}
+
+__global__ void __launch_bounds__(PARSE_T)
+k_hod_parse(const HodDraw* __restrict__ hm, int K, const float* __restrict__ mu, const unsigned* __restrict__ st,
+            int64_t Ls, int* __restrict__ nsat, long long* __restrict__ extra, HodCtl* __restrict__ ctl) {
+  __shared__ int s_ns[PARSE_H][PARSE_C];     // [halo][candidate]: a warp writes consecutive words
+  __shared__ int s_ex[PARSE_H][PARSE_C];      // -1: stream ended first
+  __shared__ unsigned long long s_Z[PARSE_C];  // bit q: halo q moves the offset (or ran out) at candidate c
+  __shared__ int s_cs[PARSE_H];                 // candidate of the run starting at halo q
+  __shared__ unsigned long long s_B;            // bit q: a run starts at halo q
+  __shared__ long long s_E;
+  __shared__ int s_k, s_adv, s_ovf;
+  if (threadIdx.x == 0) { s_E = 0; s_k = 0; s_ovf = 0; s_adv = 0; }
+  if (threadIdx.x < PARSE_C) s_Z[threadIdx.x] = 0ull;
+  __syncthreads();
+  // warp w: halos PARSE_HPW w .. + PARSE_HPW - 1 of the round; lane l:
+  // candidates l and l + 32, so a warp's loads cover one halo's consecutive
+  // candidate offsets
+  const int lane = threadIdx.x & 31, wq = (threadIdx.x >> 5) * PARSE_HPW;
+  static_assert(PARSE_PER == 2 * PARSE_HPW && PARSE_C == 64, "round shape");
+  for (;;) {
+    const int k = s_k;
+    const long long E = s_E;
+    if (k >= K) break;
+    HodDraw d[PARSE_HPW];
+    bool valid[PARSE_HPW];
+#pragma unroll
+    for (int a = 0; a < PARSE_HPW; a++) {
+      valid[a] = k + wq + a < K;
+      d[a] = valid[a] ? hm[k + wq + a] : HodDraw{0, 0u, 0.0, 0.f, 0};
+    }
+    unsigned x[PARSE_PER][PARSE_PRE];
+#pragma unroll
+    for (int i = 0; i < PARSE_PER; i++) {
+      const int a = i >> 1, c = lane + 32 * (i & 1);
+      const int64_t pp = 2 * (int64_t)d[a].h + E + 4 * c + 1;
+#pragma unroll
+      for (int j = 0; j < PARSE_PRE; j++) x[i][j] = valid[a] && pp + j < Ls ? st[pp + j] : 0u;
+    }
+#pragma unroll
+    for (int i = 0; i < PARSE_PER; i++) {
+      const int a = i >> 1, c = lane + 32 * (i & 1);
+      const int64_t pp = 2 * (int64_t)d[a].h + E + 4 * c + 1;
+      int ns = 0, used = 0, ex = -1;
+      if (valid[a] && hod_draw(d[a], x[i], mu, st, Ls, pp, &ns, &used)) ex = used + 3 * ns - 1;
+      s_ns[wq + a][c] = ns;
+      s_ex[wq + a][c] = ex;
+      if (ex != 0) atomicOr(&s_Z[c], 1ull << (wq + a));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      // follow the offsets from candidate 0, jumping over the halos that
+      // leave the offset where it is
+      const int lim = min(PARSE_H, K - k);
+      const unsigned long long live = lim >= 64 ? ~0ull : ((1ull << lim) - 1ull);
+      int c = 0, adv = lim, rel = 0;
+      unsigned long long B = 1ull, from = live;      // halos not yet passed
+      s_cs[0] = 0;
+      for (;;) {
+        const unsigned long long z = s_Z[c] & from;
+        if (z == 0ull) { rel = 4 * c; break; }
+        const int qq = __ffsll((long long)z) - 1;
+        const int ex = s_ex[qq][c];
+        if (ex < 0) { s_ovf = 1; break; }
+        rel = 4 * c + ex;
+        if (qq + 1 >= lim || (rel & 3) || rel >= 4 * PARSE_C) { adv = qq + 1; break; }
+        c = rel >> 2;
+        from = live & (~1ull << qq);                  // halos qq + 1 ..
+        B |= 1ull << (qq + 1);
+        s_cs[qq + 1] = c;
+      }
+      s_B = B;
+      s_adv = adv;
+      s_E = E + rel;
+      s_k = k + adv;
+    }
+    __syncthreads();
+    if (s_ovf) {
+      if (threadIdx.x == 0) ctl->overflow = 1;
       return;
     }
-    const unsigned nz = __ballot_sync(0xffffffffu, idx < K && ex != 0);
-    const int last = nz ? __ffs(nz) - 1 : 31;
-    if (idx < K && lane <= last) {
-      nsat[h] = ns;
-      extra[h] = ex;
+    if (threadIdx.x < s_adv) {
+      const int qq = threadIdx.x;
+      const unsigned long long upto = qq == 63 ? ~0ull : ((2ull << qq) - 1ull);
+      const int c = s_cs[63 - __clzll((long long)(s_B & upto))];    // the run holding halo qq
+      const int h = hm[k + qq].h;
+      nsat[h] = s_ns[qq][c];
+      extra[h] = s_ex[qq][c];
     }
-    E += __shfl_sync(0xffffffffu, ex, last);
-    k += last + 1;
+    if (threadIdx.x < PARSE_C) s_Z[threadIdx.x] = 0ull;
+    __syncthreads();
   }
 }
 
@@ -309,7 +476,7 @@ __global__ void __launch_bounds__(HOD_T) k_hod_write(HodWriteArgs a) {
 }
 
 // Galaxy_Types (split_galaxies.c:37-72): one uniform per galaxy, in order
-constexpr int SPLIT_CHUNK = 32;
+constexpr int SPLIT_CHUNK = 8;
 
 __global__ void __launch_bounds__(128)
 k_hod_split(const TausJump* __restrict__ J, TausState s0, const float* __restrict__ Mh, int64_t nh,
@@ -458,7 +625,7 @@ extern "C" int exh_hod_populate(exh_ctx* ctx, const float* posh, const float* ve
   }
   // per-halo work
   const size_t nscan = n / SCAN_TILE + 2;
-  const size_t work_bytes = n * (4 * 7 + 8 * 4) + nscan * 16 + sizeof(TausJump) + 8 * HOD_NEPS * (1 + 2 * HOD_NB) +
+  const size_t work_bytes = n * (4 * 6 + 8 * 4 + sizeof(HodDraw)) + nscan * 16 + sizeof(TausJump) + 8 * HOD_NEPS * (1 + 2 * HOD_NB) +
                             32 * 256;
   EXH_TRY(c.buf[B_HOD].ensure(work_bytes));
   Bump w{c.buf[B_HOD].as<char>()};
@@ -467,7 +634,7 @@ extern "C" int exh_hod_populate(exh_ctx* ctx, const float* posh, const float* ve
   float* mu = w.take<float>(n);
   int* rnd = w.take<int>(n);
   int* rpos = w.take<int>(n);
-  int* list = w.take<int>(n);
+  HodDraw* hm = w.take<HodDraw>(n);
   int* nsat = w.take<int>(n);
   long long* extra = w.take<long long>(n);
   long long* E = w.take<long long>(n);
@@ -500,7 +667,7 @@ extern "C" int exh_hod_populate(exh_ctx* ctx, const float* posh, const float* ve
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   EXH_CUDA_TRY(exclusive_scan<int>(rnd, rpos, n, isc, K_dev, st));
-  k_hod_compact<<<nb, HOD_T, 0, st>>>(rnd, rpos, nh, list);
+  k_hod_compact<<<nb, HOD_T, 0, st>>>(rnd, rpos, mu, nh, hm);
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   HodCtl hctl;
@@ -545,7 +712,7 @@ extern "C" int exh_hod_populate(exh_ctx* ctx, const float* posh, const float* ve
     EXH_CUDA_TRY(cudaGetLastError());
     EXH_CUDA_TRY(cudaMemsetAsync(&ctl->overflow, 0, sizeof(int), st));
     if (K > 0) {
-      k_hod_parse<<<1, 32, 0, st>>>(list, K, mu, dst, Ls, nsat, extra, ctl);
+      k_hod_parse<<<1, PARSE_T, 0, st>>>(hm, K, mu, dst, Ls, nsat, extra, ctl);
       count_launch(1);
       EXH_CUDA_TRY(cudaGetLastError());
     }
