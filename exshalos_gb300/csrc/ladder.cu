@@ -92,6 +92,84 @@ struct LadderGenY {
   }
 };
 
+// y pass of one radius for boxes with a four-step split of ny: the block's
+// tile (x row o, W columns k0..k0+W-1, all n rows j) is multiplied by the
+// window before the transform.  The W(|k| R) values it needs, one per
+// (|j|, column), are gathered once from the |n|^2 table into shared memory
+// (n/2 + 1 rows of W floats); a gather per element costs the pass about as
+// much again as its loads of the modes.  The transform is the one of
+// k_fft4_strided, so results equal the generic pass with LadderGenY.
+template <int N1, int N2>
+__global__ void __launch_bounds__(FS_THREADS, 4)
+k_ladder_y(const float2* __restrict__ dk, const float* __restrict__ w, int h, float2* __restrict__ out,
+           const float2* __restrict__ tw, int nc) {
+  using S = FsShape<N1, N2>;
+  constexpr int W = S::W, n = S::n, HJ = n / 2 + 1;
+  __shared__ float2 sm[n * W];
+  __shared__ float slab[HJ * W];
+  const int o = blockIdx.y, i0 = blockIdx.x * W;
+  const int nb = min(W, nc - i0);
+  const int c = threadIdx.x % W, jj = threadIdx.x / W;
+  const int ai = (2 * o < n) ? o : n - o;              // |i| of this x row (cubic box)
+  for (int t = threadIdx.x; t < HJ * W; t += FS_THREADS) {
+    const int aj = t / W, k = min(i0 + t % W, h);     // k <= h is |k|
+    slab[t] = __ldg(&w[ai * ai + aj * aj + k * k]);
+  }
+  float2 v[N1];
+  if (jj < N2) {
+#pragma unroll
+    for (int j1 = 0; j1 < N1; j1++)
+      v[j1] = (c < nb) ? dk[((size_t)o * n + jj + N2 * j1) * nc + i0 + c] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  if (jj < N2) {
+#pragma unroll
+    for (int j1 = 0; j1 < N1; j1++) {
+      const int e = jj + N2 * j1, aj = (2 * e < n) ? e : n - e;
+      const float wv = slab[aj * W + c];
+      v[j1] = make_float2(v[j1].x * wv, v[j1].y * wv);
+    }
+    RDft<N1>::run(v, 1.f, [tw](int m) { return __ldg(&tw[m * N2]); });
+#pragma unroll
+    for (int k1 = 0; k1 < N1; k1++) {
+      float2 x = v[k1];
+      if (k1 != 0 && jj != 0) x = cmul(x, tw_get(tw, jj * k1, 1.f));
+      sm[(k1 * N2 + jj) * W + c] = x;
+    }
+  }
+  __syncthreads();
+  if (jj < N1) {
+    float2 u[N2];
+#pragma unroll
+    for (int j2 = 0; j2 < N2; j2++) u[j2] = sm[(jj * N2 + j2) * W + c];
+    RDft<N2>::run(u, 1.f, [tw](int m) { return __ldg(&tw[m * N1]); });
+    if (c < nb) {
+#pragma unroll
+      for (int k2 = 0; k2 < N2; k2++) out[((size_t)o * n + jj + N1 * k2) * nc + i0 + c] = u[k2];
+    }
+  }
+}
+
+// launches k_ladder_y when ny has a four-step split; false otherwise
+static bool launch_ladder_y(const FFTPlan3D& p, const float2* dk, const float* w, int h, float2* out,
+                            cudaStream_t st, cudaError_t* err) {
+  if (p.nx != p.ny || p.ny != p.nz) return false;     // the slab indexes x, y and z alike
+  switch (fs_split(p.ny)) {
+#define X(A_, B_)                                                                                      \
+  case A_ * 1000 + B_: {                                                                               \
+    constexpr int W_ = FsShape<A_, B_>::W;                                                             \
+    KTimer kt(KC_FFT_STRIDED, st, (double)p.ny * p.nc * p.nx * 16.0);                                  \
+    k_ladder_y<A_, B_><<<dim3(exh_div_up(p.nc, W_), p.nx), FS_THREADS, 0, st>>>(dk, w, h, out, p.twy, p.nc); \
+    count_launch(1);                                                                                   \
+    *err = cudaGetLastError();                                                                         \
+    return true;                                                                                       \
+  }
+    EXH_FS_CASES(X)
+#undef X
+    default: return false;
+  }
+}
+
 // z-pass destination: barrier test, first crossing kept
 struct CrossStore {
   static constexpr int io_bytes = 4;     // two u8 reads and writes per pair
@@ -231,8 +309,11 @@ int smoothing_ladder(Ctx& c, const BoxParams& b, const FieldModes& modes, int n_
     // y then x (both complex, in either order), then the z pass with the
     // barrier test; the mode read and the window sit in the y pass
     (void)gen;
-    EXH_CUDA_TRY(launch_strided(LadderGenY{dk, wtab + (size_t)i * nn, b.nd[0], p->nc, h},
-                                CplxStore{work, p->ny, p->nc}, p->py, p->twy, 1.f, p->nx, p->nc, st));
+    cudaError_t ey = cudaSuccess;
+    if (!launch_ladder_y(*p, dk, wtab + (size_t)i * nn, h, work, st, &ey))
+      ey = launch_strided(LadderGenY{dk, wtab + (size_t)i * nn, b.nd[0], p->nc, h}, CplxStore{work, p->ny, p->nc},
+                          p->py, p->twy, 1.f, p->nx, p->nc, st);
+    EXH_CUDA_TRY(ey);
     EXH_CUDA_TRY(launch_strided(CplxLoad{work, p->nx, p->ny * p->nc}, CplxStore{work, p->nx, p->ny * p->nc}, p->px,
                                 p->twx, 1.f, 1, p->ny * p->nc, st));
     cudaError_t e = cudaSuccess;
