@@ -240,11 +240,109 @@ k_ladder_z(const float2* __restrict__ work, const float2* __restrict__ twM, cons
   }
 }
 
+// z pass of one radius for nz = 256 (M = 128 packed complex values per row),
+// one warp per row and no shared memory.  Lane l holds the half-complex
+// values k = l + 32 j (j < 4); the c2r pre-processing pairs k with M - k,
+// which sits in lane (32 - l) mod 32, register 3 - j (lane 0 keeps its own).
+// The inverse 128-point DFT of the packed rows is a 4-point DFT in registers
+// (n = l + 32 n1), the twiddles w_128^(l m1), then a 32-point DFT across the
+// lanes by five radix-2 decimation-in-frequency stages with shfl_xor.  Lane l
+// then holds outputs m1 + 4 bitrev5(l), i.e. the eight consecutive reals
+// 8 bitrev5(l) .. + 7 of the row, whose eight crossing-map bytes it updates
+// with one 8-byte load and store.  Two rows per warp for more loads in flight.
+__device__ __forceinline__ float2 shfl_c(float2 v, int src) {
+  return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+__device__ __forceinline__ float2 shfl_xor_c(float2 v, int m) {
+  return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+
+constexpr int LZ_ROWS = 2;      // rows per warp
+
+__global__ void __launch_bounds__(256)
+k_ladder_z128(const float2* __restrict__ work, const float2* __restrict__ twM, const float2* __restrict__ twN,
+              unsigned char* __restrict__ cross, size_t rows, float normx, float B, int r) {
+  constexpr int nc = 129, RW = LZ_ROWS;
+  const int lane = threadIdx.x & 31;
+  const size_t row0 = ((size_t)blockIdx.x * 8 + (threadIdx.x >> 5)) * RW;
+  if (row0 >= rows) return;                           // rows % RW == 0: whole warps leave
+  float2 X[RW][4], XM[RW];
+#pragma unroll
+  for (int q = 0; q < RW; q++) {
+    const float2* x = work + (row0 + q) * nc;
+#pragma unroll
+    for (int j = 0; j < 4; j++) X[q][j] = x[lane + 32 * j];
+    XM[q] = lane == 0 ? x[128] : make_float2(0.f, 0.f);
+    if (lane == 0) { X[q][0].y = 0.f; XM[q].y = 0.f; }   // k = 0 and k = M are real
+  }
+  const int pl = (32 - lane) & 31;
+  float2 tN[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) tN[j] = tw_get(twN, lane + 32 * j, 1.f);
+  float2 Y[RW][4];
+#pragma unroll
+  for (int q = 0; q < RW; q++) {
+    float2 a[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      float2 xm = shfl_c(X[q][3 - j], pl);
+      if (lane == 0) xm = (j == 0) ? XM[q] : X[q][(4 - j) & 3];
+      xm = cconj(xm);
+      const float2 d = cmul(tN[j], csub(X[q][j], xm));
+      a[j] = make_float2(X[q][j].x + xm.x - d.y, X[q][j].y + xm.y + d.x);
+    }
+    const float2 s02 = cadd(a[0], a[2]), d02 = csub(a[0], a[2]), s13 = cadd(a[1], a[3]), d13 = csub(a[1], a[3]);
+    Y[q][0] = cadd(s02, s13);
+    Y[q][2] = csub(s02, s13);
+    Y[q][1] = make_float2(d02.x - d13.y, d02.y + d13.x);     // d02 + i d13
+    Y[q][3] = make_float2(d02.x + d13.y, d02.y - d13.x);     // d02 - i d13
+  }
+#pragma unroll
+  for (int m1 = 1; m1 < 4; m1++) {
+    const float2 w = tw_get(twM, lane * m1, 1.f);
+#pragma unroll
+    for (int q = 0; q < RW; q++) Y[q][m1] = cmul(Y[q][m1], w);
+  }
+#pragma unroll
+  for (int h = 16; h >= 1; h >>= 1) {
+    const bool hi = (lane & h) != 0;
+    const float2 w = tw_get(twM, (lane & (h - 1)) * (64 / h), 1.f);    // w_(2h)^(l mod h)
+#pragma unroll
+    for (int q = 0; q < RW; q++)
+#pragma unroll
+      for (int m1 = 0; m1 < 4; m1++) {
+        const float2 pv = shfl_xor_c(Y[q][m1], h);
+        Y[q][m1] = hi ? cmul(csub(pv, Y[q][m1]), w) : cadd(Y[q][m1], pv);
+      }
+  }
+  const int br = (int)(__brev((unsigned)lane) >> 27);
+  const unsigned long long rb = (unsigned long long)(unsigned char)r;
+#pragma unroll
+  for (int q = 0; q < RW; q++) {
+    unsigned long long* cp = reinterpret_cast<unsigned long long*>(cross + (row0 + q) * 256 + 8 * br);
+    unsigned long long mw = *cp;
+    const float v[8] = {Y[q][0].x, Y[q][0].y, Y[q][1].x, Y[q][1].y, Y[q][2].x, Y[q][2].y, Y[q][3].x, Y[q][3].y};
+#pragma unroll
+    for (int b = 0; b < 8; b++) {
+      const unsigned c = (unsigned)(mw >> (8 * b)) & 0xFFu;
+      if (c == 255u && v[b] * normx >= B) mw = (mw & ~(0xFFull << (8 * b))) | (rb << (8 * b));
+    }
+    *cp = mw;
+  }
+}
+
 // launches k_ladder_z when the box has a tile split for it; false otherwise
 static bool launch_ladder_z(const FFTPlan3D& p, const float2* work, unsigned char* cross, float normx, float B, int r,
                             cudaStream_t st, cudaError_t* err) {
   const size_t rows = (size_t)p.nx * p.ny;
   if (reinterpret_cast<uintptr_t>(cross) % 16) return false;     // 16-byte vectors need an aligned map
+  if (p.M == 128 && rows % (8 * LZ_ROWS) == 0) {
+    KTimer kt(KC_FFT_ROWS, st, (double)rows * (129 * 8.0 + 256 * 2.0));
+    k_ladder_z128<<<(unsigned)(rows / (8 * LZ_ROWS)), 256, 0, st>>>(work, p.twm, p.twn, cross, rows, normx, B, r);
+    count_launch(1);
+    *err = cudaGetLastError();
+    return true;
+  }
   switch (fs_split(p.M)) {
 #define X(A_, B_)                                                                                      \
   case A_ * 1000 + B_: {                                                                               \

@@ -5,7 +5,8 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("nd,Lc,n_radii,R_max", [(64, 4.0, 50, 40.0), (48, 2.0, 12, 30.0), (32, 8.0, 1, 8.0)])
+@pytest.mark.parametrize("nd,Lc,n_radii,R_max", [(64, 4.0, 50, 40.0), (48, 2.0, 12, 30.0), (32, 8.0, 1, 8.0),
+                                                 (256, 2.0, 4, 30.0)])
 def test_ladder_matches_fp64_oracle(orc, pk, nd, Lc, n_radii, R_max):
     from exshalos_gb300.lib import exshalos as ex
     k, P = pk
