@@ -5,6 +5,7 @@ fallback: if the shared library or a CUDA device is missing, the calls raise.
 """
 import ctypes as C
 import os
+import sys
 import threading
 
 import numpy as np
@@ -176,6 +177,36 @@ def context():
         _tls.ctx = h
         ctx = h
     return ctx
+
+
+_POOL_MIN_BYTES = 1 << 20
+_POOL_PER_SHAPE = 2
+
+
+def host_empty(shape, dtype):
+    """An uninitialised host array for a large output that the library fills
+    completely.  Arrays of 1 MB or more come from a per-thread pool of up to
+    two buffers per shape: a buffer is handed out again only once the pool
+    holds the last reference to it (the caller has dropped it), so a result
+    never shares memory with a live array; the pool saves the page faults and
+    zero-fill of a fresh allocation on every call in a loop."""
+    dt = np.dtype(dtype)
+    shape = tuple(int(x) for x in (shape if isinstance(shape, (tuple, list)) else (shape,)))
+    nbytes = int(np.prod(shape, dtype=np.int64)) * dt.itemsize
+    if nbytes < _POOL_MIN_BYTES:
+        return np.empty(shape, dtype=dt)
+    pool = getattr(_tls, "pool", None)
+    if pool is None:
+        pool = _tls.pool = {}
+    bufs = pool.setdefault((shape, dt.str), [])
+    for i in range(len(bufs)):
+        if sys.getrefcount(bufs[i]) <= 2:        # the list entry and getrefcount's argument
+            return bufs[i]
+    a = np.empty(shape, dtype=dt)
+    bufs.append(a)
+    if len(bufs) > _POOL_PER_SHAPE:
+        bufs.pop(0)
+    return a
 
 
 def ptr(a):

@@ -24,17 +24,19 @@ def _params(**kw):
 
 def _fetch_catalogue(nh, ng, want_vel=False, want_grid=False, want_pos=False, want_flag=False, nd=None):
     L = _capi.load()
+    # every array is filled completely by exh_halos_fetch
+    he = _capi.host_empty
     out = {
-        "posh": np.zeros((nh, 3), dtype=np.float32),
-        "Mh": np.zeros(nh, dtype=np.float32),
-        "x": np.zeros((nh, 3), dtype=np.int32),
-        "count": np.zeros(nh, dtype=np.int32),
+        "posh": he((nh, 3), np.float32),
+        "Mh": he(nh, np.float32),
+        "x": he((nh, 3), np.int32),
+        "count": he(nh, np.int32),
     }
-    velh = np.zeros((nh, 3), dtype=np.float32) if want_vel else None
-    grid = np.zeros(nd, dtype=np.float32) if want_grid else None
-    pos = np.zeros((ng, 3), dtype=np.float32) if want_pos else None
-    vel = np.zeros((ng, 3), dtype=np.float32) if (want_pos and want_vel) else None
-    flag = np.zeros(nd, dtype=np.int64) if want_flag else None
+    velh = he((nh, 3), np.float32) if want_vel else None
+    grid = he(nd, np.float32) if want_grid else None
+    pos = he((ng, 3), np.float32) if want_pos else None
+    vel = he((ng, 3), np.float32) if (want_pos and want_vel) else None
+    flag = he(nd, np.int64) if want_flag else None
     _capi.check(L.exh_halos_fetch(_capi.context(), _capi.ptr(out["posh"]), _capi.ptr(velh), _capi.ptr(out["Mh"]),
                                   _capi.ptr(out["x"]), _capi.ptr(out["count"]), _capi.ptr(grid), _capi.ptr(pos),
                                   _capi.ptr(vel), _capi.ptr(flag), _capi.EXH_MEM_HOST, None))
@@ -162,7 +164,7 @@ def density_grid_compute(k, P, R_max, Ndx, Ndy, Ndz, Lc, outk, seed, fixed, phas
     P = np.ascontiguousarray(P, dtype=np.float32)
     prm = _params(R_max=float(R_max), ndx=int(Ndx), ndy=int(Ndy), ndz=int(Ndz), Lc=float(Lc), seed=int(seed),
                   fixed=int(fixed), phase=float(phase), k_smooth=float(k_smooth))
-    grid = np.empty((int(Ndx), int(Ndy), int(Ndz)), dtype=np.float32)
+    grid = _capi.host_empty((int(Ndx), int(Ndy), int(Ndz)), np.float32)
     _capi.check(_capi.load().exh_density_grid_compute(_capi.context(), _capi.ptr(k), _capi.ptr(P), k.size, prm,
                                                       _capi.ptr(grid), _capi.EXH_MEM_HOST, None))
     return {"grid": grid}
@@ -185,7 +187,7 @@ def smoothing_ladder(k, P, R_max, Ndx, Ndy, Ndz, Lc, seed=12345, n_radii=50, Om0
     R = np.zeros(int(n_radii), dtype=np.float32)
     B = np.zeros(int(n_radii), dtype=np.float32)
     if out is None:
-        cross = np.empty((int(Ndx), int(Ndy), int(Ndz)), dtype=np.uint8)
+        cross = _capi.host_empty((int(Ndx), int(Ndy), int(Ndz)), np.uint8)
         dst, mem = _capi.ptr(cross), _capi.EXH_MEM_HOST
     else:
         cross, dst, mem = out, out.data_ptr(), _capi.EXH_MEM_DEVICE

@@ -30,7 +30,7 @@ def grid_compute(pos, vel, mass, nmass, type, ntype, nd, L, Om0, z, direction, w
     if window not in (1, 2, 3, 4):
         raise ValueError("window must be 1 (NGP), 2 (CIC), 3 (Sphere) or 4 (Exp)")
     L_ = _capi.load()
-    grid = np.empty((ntype, interlacing + 1, nd, nd, nd), dtype=np.float32)
+    grid = _capi.host_empty((ntype, interlacing + 1, nd, nd, nd), np.float32)
     if ntype == 1 and interlacing == 0 and direction == -1 and window == 2 and not weighted:
         _capi.check(L_.exh_grid_compute(_capi.context(), _capi.ptr(pos), npart, nd, float(L) / folds, 2, 1,
                                         _capi.ptr(grid), _capi.EXH_MEM_HOST, None))

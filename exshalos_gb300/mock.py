@@ -50,8 +50,8 @@ def Generate_Halos_Box_from_Pk(
     """
     precision = _ext.check_precision()
     if precision == 4:
-        k = np.asarray(k).astype("float32")
-        P = np.asarray(P).astype("float32")
+        k = np.asarray(k, dtype=np.float32)
+        P = np.asarray(P, dtype=np.float32)
         R_max, Lc, Om0, z = np.float32(R_max), np.float32(Lc), np.float32(Om0), np.float32(z)
         k_smooth, delta_c = np.float32(k_smooth), np.float32(delta_c)
         a, beta, alpha, phase = np.float32(a), np.float32(beta), np.float32(alpha), np.float32(phase)
@@ -112,16 +112,16 @@ def Generate_Halos_Box_from_Grid(
                 raise ValueError("The number of components of V is different from 3!")
     precision = _ext.check_precision()
     if precision == 4:
-        grid = np.asarray(grid).astype("float32")
-        k = np.asarray(k).astype("float32")
-        P = np.asarray(P).astype("float32")
+        grid = np.asarray(grid, dtype=np.float32)
+        k = np.asarray(k, dtype=np.float32)
+        P = np.asarray(P, dtype=np.float32)
         Lc, Om0, z = np.float32(Lc), np.float32(Om0), np.float32(z)
         k_smooth, delta_c = np.float32(k_smooth), np.float32(delta_c)
         a, beta, alpha = np.float32(a), np.float32(beta), np.float32(alpha)
         if S is not None:
-            S = np.asarray(S).astype("float32")
+            S = np.asarray(S, dtype=np.float32)
         if V is not None:
-            V = np.asarray(V).astype("float32")
+            V = np.asarray(V, dtype=np.float32)
     return _ext.halos_box_from_grid(
         k, P, grid, S, V, Lc, k_smooth, Om0, z, delta_c, np.int32(Nmin), a, beta, alpha, np.int32(OUT_LPT),
         np.int32(OUT_VEL), np.int32(DO_2LPT), np.int32(OUT_FLAG), np.int32(In_disp), np.int32(OUT_PROF),
@@ -164,12 +164,12 @@ def Generate_Galaxies_from_Halos(
     from .lib import hod as _hod
 
     In_C = Ch is not None
-    posh = np.asarray(posh).astype("float32")
+    posh = np.asarray(posh, dtype=np.float32)
     if velh is not None:
-        velh = np.asarray(velh).astype("float32")
-    Mh = np.asarray(Mh).astype("float32")
+        velh = np.asarray(velh, dtype=np.float32)
+    Mh = np.asarray(Mh, dtype=np.float32)
     if In_C:
-        Ch = np.asarray(Ch).astype("float32")
+        Ch = np.asarray(Ch, dtype=np.float32)
     if ndx is None:
         ndx = nd
     if ndy is None:
@@ -195,9 +195,9 @@ def Split_Galaxies(
     (mock.py:519-576): int32, +-(1..ntypes), negative for centrals."""
     from .lib import hod as _hod
 
-    Mh = np.asarray(Mh).astype("float32")
-    params_cen = np.asarray(params_cen).astype("float32")
-    params_sat = np.asarray(params_sat).astype("float32")
+    Mh = np.asarray(Mh, dtype=np.float32)
+    params_cen = np.asarray(params_cen, dtype=np.float32)
+    params_sat = np.asarray(params_sat, dtype=np.float32)
     if len(params_cen.shape) == 1:
         params_cen = params_cen.reshape([1, len(params_cen)])
     if len(params_sat.shape) == 1:

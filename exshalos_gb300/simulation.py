@@ -57,12 +57,12 @@ def Compute_Density_Grid(
     several tracer types; interlacing; redshift-space shifts along x/y/z;
     folds.  Returns [nd, nd, nd] float32 for one type without interlacing,
     else [ntypes, interlacing + 1, nd, nd, nd]."""
-    pos = np.asarray(pos).astype("float32")
+    pos = np.asarray(pos, dtype=np.float32)
     L, R, R_times = np.float32(L), np.float32(R), np.float32(R_times)
     Om0, z = np.float32(Om0), np.float32(z)
     nmass = 0
     if mass is not None:
-        mass = np.asarray(mass).astype("float32")
+        mass = np.asarray(mass, dtype=np.float32)
         nmass = 1
     ntypes = 1
     if types is not None:
@@ -113,7 +113,7 @@ def Compute_Power_Spectrum(
         k_min = 2.0 * np.pi / L
     if k_max is None:
         k_max = np.pi / L * nd
-    grid = np.asarray(grid).astype("float32")
+    grid = np.asarray(grid, dtype=np.float32)
     L, R = np.float32(L), np.float32(R)
     k_min, k_max = np.float32(k_min), np.float32(k_max)
     window = _window_code(window, allow_none=True)
@@ -145,5 +145,5 @@ def Compute_Abundance(
     ndx = nd if ndx is None else ndx
     ndy = nd if ndy is None else ndy
     ndz = nd if ndz is None else ndz
-    return _spec.abundance_compute(np.asarray(Mh).astype("float32"), np.float32(Mmin), np.float32(Mmax), np.int32(Nm),
+    return _spec.abundance_compute(np.asarray(Mh, dtype=np.float32), np.float32(Mmin), np.float32(Mmax), np.int32(Nm),
                                    np.float32(Lc), np.int32(ndx), np.int32(ndy), np.int32(ndz), np.int32(verbose))

@@ -37,3 +37,24 @@ def test_no_device_raises_instead_of_falling_back():
     from exshalos_gb300 import _capi
     with pytest.raises(_capi.ExhError):
         _capi.context()
+
+
+def test_host_output_pool_never_aliases_live_arrays():
+    """Large outputs come from a per-thread pool; a buffer returns only after
+    every reference to it (views included) is gone."""
+    import numpy as np
+    from exshalos_gb300 import _capi
+    shape = (64, 64, 64)
+    a = _capi.host_empty(shape, np.float32)
+    b = _capi.host_empty(shape, np.float32)
+    assert a.ctypes.data != b.ctypes.data
+    pa = a.ctypes.data
+    v = a.reshape(-1)
+    del a
+    c = _capi.host_empty(shape, np.float32)          # a is still alive through v
+    assert c.ctypes.data not in (pa, b.ctypes.data)
+    del v, c
+    d = _capi.host_empty(shape, np.float32)
+    assert d.ctypes.data != b.ctypes.data
+    small = _capi.host_empty(10, np.float32)
+    assert small.shape == (10,) and small.dtype == np.float32
