@@ -108,8 +108,7 @@ extern "C" int exh_abundance_compute(exh_ctx* ctx, const float* Mh, int64_t nh, 
   EXH_CUDA_TRY(cudaMemsetAsync(cnt, 0, (sizeof(unsigned long long) + sizeof(double)) * (size_t)Nm, st));
   if (nh > 0) {
     const size_t sm = (sizeof(double) + sizeof(unsigned)) * (size_t)Nm + 16;
-    if (sm > 48 * 1024) EXH_CUDA_TRY(cudaFuncSetAttribute(k_abundance, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                          (int)sm));
+    if (sm > 48 * 1024) EXH_CUDA_TRY(set_smem(k_abundance, sm));
     k_abundance<<<nb, AB_T, sm, st>>>(d, nh, std::log((double)Mmin), (double)dlnM, Nm, cnt, msum);
     count_launch(1);
     EXH_CUDA_TRY(cudaGetLastError());

@@ -1,11 +1,28 @@
 // FFT plans and the plain 3-D transforms of the C ABI.
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "ctx.cuh"
 #include "fft4.cuh"
 
 namespace exh {
+
+cudaError_t smem_raise(const void* kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, size_t> limit;     // (device, kernel) -> limit set
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = limit[std::make_pair(dev, kernel)];
+  if (bytes <= cur) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
+}
 
 RadixPlan make_radix_plan(int n) {
   RadixPlan p{};

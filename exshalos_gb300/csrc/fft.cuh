@@ -270,9 +270,16 @@ inline size_t smem_strided(int n) { return sizeof(float2) * 2 * (size_t)n * FFT_
 inline size_t smem_r2c(int M) { return sizeof(float2) * 2 * (size_t)M * FFT_LDB; }
 inline size_t smem_c2r(int M) { return sizeof(float2) * (3 * (size_t)M + 1) * FFT_LDB; }
 
+// Raise a kernel's dynamic shared-memory limit to at least `bytes`.  The
+// attribute is process-wide while contexts on several host threads launch
+// the same kernel with different sizes, so it only ever grows (under a lock,
+// per device): lowering it for a small box could make another thread's
+// launch for a larger one fail between its own call and its launch.
+cudaError_t smem_raise(const void* kernel, size_t bytes);     // fft.cu
+
 template <class K>
 inline cudaError_t set_smem(K kernel, size_t bytes) {
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  return smem_raise(reinterpret_cast<const void*>(kernel), bytes);
 }
 
 // Strided pass launcher: data [outer][n][inner].

@@ -66,3 +66,18 @@ def test_batch_rejects_bad_items(pk):
         ex.batch_run(k, P, [64], [1], lanes=0)
     r = ex.batch_run(k, P, [], [])
     assert r["nh"].size == 0
+
+
+def test_many_lanes_mixed_sizes_match_one_lane(pk):
+    """More lanes than items of one size, sizes interleaved, 2LPT on: every
+    lane thread launches the same kernels with different shared-memory sizes,
+    and the results equal the one-lane loop."""
+    from exshalos_gb300.lib import exshalos as ex
+    k, P = pk
+    nds = np.array([32, 96, 64, 128, 48, 96, 32, 128, 64, 48, 96, 32] * 4)
+    seeds = np.arange(100, 100 + nds.size)
+    kw = dict(Lc=2.0, Nk_pk=32, DO_2LPT=1, beta=0.12)
+    one = ex.batch_run(k, P, nds, seeds, lanes=1, **kw)
+    many = ex.batch_run(k, P, nds, seeds, lanes=32, **kw)
+    for key in ("nh", "k", "Pk", "Nk", "status"):
+        assert np.array_equal(many[key], one[key]), key
