@@ -386,19 +386,29 @@ def run_ours(args, ws, rank, local):
     cross_dev = torch.empty(ng, dtype=torch.uint8, device="cuda")
     nh = C.c_int64(0)
     nh_seen = []
+    # the ladder does not depend on the halo chain: it runs on its own library
+    # context (own buffers) and stream, beside the halo finder, whose sort and
+    # growth are latency-bound
+    ctx_lad = C.c_void_p()
+    _capi.check(L_.exh_ctx_create(local, C.byref(ctx_lad)))
+    s_lad = torch.cuda.Stream()
+    # the halo chain is the critical path: its stream gets the higher priority
+    s_halo = torch.cuda.Stream(priority=-1)
+    hs = C.c_void_p(s_halo.cuda_stream)
 
     def step(seed):
         prm = _capi.default_params(ndx=ND, ndy=ND, ndz=ND, Lc=LC, seed=seed, DO_2LPT=1, **BARRIER)
-        _capi.check(L_.exh_smoothing_ladder(ctx, _capi.ptr(k), _capi.ptr(P), k.size, prm, N_RADII, R_LADDER,
-                                            _capi.ptr(cross_dev), None, None, _capi.EXH_MEM_DEVICE, None))
-        _capi.check(L_.exh_halos_box_from_pk(ctx, _capi.ptr(k), _capi.ptr(P), k.size, prm, C.byref(nh), None))
+        _capi.check(L_.exh_smoothing_ladder(ctx_lad, _capi.ptr(k), _capi.ptr(P), k.size, prm, N_RADII, R_LADDER,
+                                            _capi.ptr(cross_dev), None, None, _capi.EXH_MEM_DEVICE,
+                                            C.c_void_p(s_lad.cuda_stream)))
+        _capi.check(L_.exh_halos_box_from_pk(ctx, _capi.ptr(k), _capi.ptr(P), k.size, prm, C.byref(nh), hs))
         _capi.check(L_.exh_halos_fetch(ctx, _capi.ptr(posh_dev), None, None, None, None, None, None, None, None,
-                                       _capi.EXH_MEM_DEVICE, None))
+                                       _capi.EXH_MEM_DEVICE, hs))
         _capi.check(L_.exh_grid_compute(ctx, _capi.ptr(posh_dev), nh.value, ND, float(Lbox), 2, 1,
-                                        _capi.ptr(grid_dev), _capi.EXH_MEM_DEVICE, None))
+                                        _capi.ptr(grid_dev), _capi.EXH_MEM_DEVICE, hs))
         _capi.check(L_.exh_power_compute(ctx, _capi.ptr(grid_dev), ND, float(Lbox), 2, NK_PK, float(kmin),
                                          float(kmax), _capi.ptr(k_out), _capi.ptr(P_out), _capi.ptr(c_out),
-                                         _capi.EXH_MEM_DEVICE, None))
+                                         _capi.EXH_MEM_DEVICE, hs))
         nh_seen.append(nh.value)
 
     seed0 = 1000 * rank + 1
@@ -413,8 +423,12 @@ def run_ours(args, ws, rank, local):
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record()
+    s_lad.wait_stream(torch.cuda.current_stream())
+    s_halo.wait_stream(torch.cuda.current_stream())
     for s in range(args.steps):
         step(seed0 + s)
+    torch.cuda.current_stream().wait_stream(s_lad)
+    torch.cuda.current_stream().wait_stream(s_halo)
     ev1.record()
     torch.cuda.synchronize()
     barrier(ws)

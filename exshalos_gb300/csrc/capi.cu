@@ -83,6 +83,11 @@ int exh_ctx_destroy(exh_ctx* ctx) {
     cudaStreamDestroy(ctx->c.lane_st[i]);
   }
   for (auto& kv : ctx->c.plans) fft_plan_destroy(&kv.second);
+  if (ctx->c.side) {
+    cudaEventDestroy(ctx->c.ev_fork);
+    cudaEventDestroy(ctx->c.ev_join);
+    cudaStreamDestroy(ctx->c.side);
+  }
   for (int i = 0; i < B_COUNT; i++) ctx->c.buf[i].release();
   diff_state_release(ctx->c);
   halo_state_release(ctx->c);

@@ -112,6 +112,11 @@ struct Ctx {
   float* peak_key = nullptr;
   unsigned* peak_id = nullptr;
   DiffState* diff = nullptr;
+  // second stream for work that runs beside the halo finder (LPT), created
+  // on first use; fork/join events
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  int side_stream(cudaStream_t* out);
   // galaxies of the last exh_hod_populate (B_HODG)
   int64_t hod_ng = -1;
   int hod_vel = 0;

@@ -77,6 +77,16 @@ void fft_plan_destroy(FFTPlan3D* p) {
   p->twx = p->twy = p->twm = p->twn = nullptr;
 }
 
+int Ctx::side_stream(cudaStream_t* out) {
+  if (!side) {
+    EXH_CUDA_TRY(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    EXH_CUDA_TRY(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    EXH_CUDA_TRY(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+  }
+  *out = side;
+  return EXH_OK;
+}
+
 int Ctx::get_plan(int nx, int ny, int nz, FFTPlan3D** out) {
   auto key = std::make_tuple(nx, ny, nz);
   auto it = plans.find(key);

@@ -453,8 +453,11 @@ extern "C" int exh_smoothing_ladder(exh_ctx* ctx, const float* k, const float* P
     out = c.buf[B_CROSS].as<unsigned char>();
   }
   EXH_TRY(smoothing_ladder(c, b, modes, n_radii, R.data(), B.data(), out, st));
-  if (mem == EXH_MEM_HOST) EXH_CUDA_TRY(cudaMemcpyAsync(cross, out, b.ng, cudaMemcpyDeviceToHost, st));
-  EXH_CUDA_TRY(cudaStreamSynchronize(st));
+  if (mem == EXH_MEM_HOST) {
+    EXH_CUDA_TRY(cudaMemcpyAsync(cross, out, b.ng, cudaMemcpyDeviceToHost, st));
+    EXH_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  // a device map is complete when `stream` reaches this point (no host wait)
   for (int i = 0; i < n_radii; i++) {
     if (radii_out) radii_out[i] = R[i];
     if (barrier_out) barrier_out[i] = B[i];

@@ -225,12 +225,12 @@ int exh_halos_box_from_pk(exh_ctx* ctx, const float* k, const float* P, int Nk, 
     FieldGen gen{make_modes(b, A_dev, prm->fixed, prm->phase)};
     EXH_CUDA_TRY(fft_c2r_3d(*p, gen, c.buf[B_WORK].as<float2>(), RealPairStore{delta, b.nd[2], b.Normx}, st));
   }
-  // halos (box.c:21)
-  HaloDev h;
-  ShellTable t;
-  EXH_TRY(run_halo_finder(c, b, k, P, Nk, prm->setup_fp64, delta, &h, &t, st));
-  // LPT (box.c:38-58): the amplitude table is re-uploaded (the mass step reused the buffer)
-  EXH_TRY(upload_amplitudes(c, b, k, P, Nk, &A_dev, st));
+  // LPT (box.c:38-58) depends on the field's modes only: it is enqueued on the
+  // context's side stream, after the field, and runs beside the halo finder
+  // (whose sort and growth are latency-bound and leave most SMs idle); the
+  // halo sums wait for it.  The two share no buffer.
+  cudaStream_t side;
+  EXH_TRY(c.side_stream(&side));
   FieldModes modes = make_modes(b, A_dev, prm->fixed, prm->phase);
   EXH_TRY(c.buf[B_S].ensure(sizeof(float) * 3 * ng));
   EXH_TRY(c.buf[B_PHI1].ensure(sizeof(float) * ng));
@@ -246,7 +246,19 @@ int exh_halos_box_from_pk(exh_ctx* ctx, const float* k, const float* P, int Nk, 
     EXH_TRY(c.buf[B_VEL].ensure(sizeof(float) * 3 * ng));
     V = c.buf[B_VEL].as<float>();
   }
-  EXH_TRY(lpt_run(c, b, modes, prm->k_smooth, prm->DO_2LPT != 0, S, V, phi1, phi2, st));
+  EXH_CUDA_TRY(cudaEventRecord(c.ev_fork, st));
+  EXH_CUDA_TRY(cudaStreamWaitEvent(side, c.ev_fork, 0));
+  EXH_TRY(lpt_run(c, b, modes, prm->k_smooth, prm->DO_2LPT != 0, S, V, phi1, phi2, side));
+  EXH_CUDA_TRY(cudaEventRecord(c.ev_join, side));
+  // halos (box.c:21)
+  HaloDev h;
+  ShellTable t;
+  const int hs = run_halo_finder(c, b, k, P, Nk, prm->setup_fp64, delta, &h, &t, st);
+  EXH_CUDA_TRY(cudaStreamWaitEvent(st, c.ev_join, 0));
+  if (hs != EXH_OK) {
+    EXH_CUDA_TRY(cudaStreamSynchronize(side));      // nothing of this call left running on return
+    return hs;
+  }
   const size_t nh = std::max<int64_t>(h.nh, 1);
   EXH_TRY(c.buf[B_POSH].ensure(sizeof(float) * 6 * nh));
   float* posh = c.buf[B_POSH].as<float>();
@@ -333,15 +345,37 @@ int exh_halos_box_from_grid(exh_ctx* ctx, const float* delta, int ndx, int ndy, 
     EXH_CUDA_TRY(cudaMemcpyAsync(c.buf[B_DELTA].p, delta, sizeof(float) * ng, cudaMemcpyHostToDevice, st));
     d = c.buf[B_DELTA].as<float>();
   }
-  HaloDev h;
-  ShellTable t;
-  EXH_TRY(run_halo_finder(c, b, k, P, Nk, prm->setup_fp64, d, &h, &t, st));
   EXH_TRY(c.buf[B_S].ensure(sizeof(float) * 3 * ng));
   float* S = c.buf[B_S].as<float>();
   float* V = nullptr;
   if (prm->OUT_VEL) {
     EXH_TRY(c.buf[B_VEL].ensure(sizeof(float) * 3 * ng));
     V = c.buf[B_VEL].as<float>();
+  }
+  cudaStream_t side = nullptr;
+  if (!S_in) {
+    // box.c:108-143: delta_k = Normk r2c(delta), then 1LPT (and 2LPT), on the
+    // side stream beside the halo finder (both only read the grid)
+    EXH_TRY(c.buf[B_PHI1].ensure(sizeof(float) * ng));
+    float* phi1 = c.buf[B_PHI1].as<float>();
+    float* phi2 = nullptr;
+    if (prm->DO_2LPT) {
+      EXH_TRY(c.buf[B_PHI2].ensure(sizeof(float) * ng));
+      phi2 = c.buf[B_PHI2].as<float>();
+    }
+    EXH_TRY(c.side_stream(&side));
+    EXH_CUDA_TRY(cudaEventRecord(c.ev_fork, st));
+    EXH_CUDA_TRY(cudaStreamWaitEvent(side, c.ev_fork, 0));
+    EXH_TRY(lpt_run_grid(c, b, d, prm->k_smooth, prm->DO_2LPT != 0, S, V, phi1, phi2, side));
+    EXH_CUDA_TRY(cudaEventRecord(c.ev_join, side));
+  }
+  HaloDev h;
+  ShellTable t;
+  const int hs = run_halo_finder(c, b, k, P, Nk, prm->setup_fp64, d, &h, &t, st);
+  if (side) EXH_CUDA_TRY(cudaStreamWaitEvent(st, c.ev_join, 0));
+  if (hs != EXH_OK) {
+    if (side) EXH_CUDA_TRY(cudaStreamSynchronize(side));
+    return hs;
   }
   if (S_in) {
     // box.c:89-105: the given displacements (and velocities), [ng][3]
@@ -359,16 +393,6 @@ int exh_halos_box_from_grid(exh_ctx* ctx, const float* delta, int ndx, int ndy, 
     }
     EXH_TRY(aos_to_planes(Sd, ng, S, st));
     if (V) EXH_TRY(aos_to_planes(Vd, ng, V, st));
-  } else {
-    // box.c:108-143: delta_k = Normk r2c(delta), then 1LPT (and 2LPT)
-    EXH_TRY(c.buf[B_PHI1].ensure(sizeof(float) * ng));
-    float* phi1 = c.buf[B_PHI1].as<float>();
-    float* phi2 = nullptr;
-    if (prm->DO_2LPT) {
-      EXH_TRY(c.buf[B_PHI2].ensure(sizeof(float) * ng));
-      phi2 = c.buf[B_PHI2].as<float>();
-    }
-    EXH_TRY(lpt_run_grid(c, b, d, prm->k_smooth, prm->DO_2LPT != 0, S, V, phi1, phi2, st));
   }
   const size_t nh = std::max<int64_t>(h.nh, 1);
   EXH_TRY(c.buf[B_POSH].ensure(sizeof(float) * 6 * nh));

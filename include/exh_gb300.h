@@ -200,7 +200,10 @@ int exh_density_grid_compute(exh_ctx *ctx, const float *k, const float *P, int N
  * prm; sigma^2(R) by the top-hat integral of src/exshalos/find_halos.c:4-14,
  * in FP64); 255 where no
  * radius crosses.  cross[ng] is u8 (host or device per mem); radii_out and
- * barrier_out (host, n_radii floats each) may be NULL. */
+ * barrier_out (host, n_radii floats each) may be NULL.  With a device map
+ * the call returns without waiting for the GPU: the map is complete when
+ * `stream` reaches the end of the call's work (the context's buffers stay in
+ * use until then, so a context serves one stream at a time). */
 int exh_smoothing_ladder(exh_ctx *ctx, const float *k, const float *P, int Nk, const exh_halo_params *prm,
                          int n_radii, float R_max, uint8_t *cross, float *radii_out, float *barrier_out,
                          int mem, void *stream);
