@@ -503,6 +503,90 @@ __device__ __forceinline__ void warp_partition(float* ka, unsigned* ia, float* k
   nL_out = nL;
 }
 
+// The same partition of one sub-segment [lo, hi] by the whole block (for
+// the first levels, where a block has one or two sub-segments): each thread
+// classifies SORT_SMALL / SORT_T consecutive elements, a block scan gives the
+// L ranks, and the > elements follow their chains.  Returns nL.
+__device__ __forceinline__ int block_partition(float* ka, unsigned* ia, float* kb, unsigned* ib, int* lam, int* posl,
+                                               int lo, int hi, int* ws) {
+  constexpr int IT = SORT_SMALL / SORT_T;
+  const float pv = ka[hi];
+  const int n = hi - lo;                     // elements before the pivot, <= SORT_SMALL - 1
+  const int base = lo + threadIdx.x * IT;
+  bool isL[IT];
+  int c = 0;
+#pragma unroll
+  for (int q = 0; q < IT; q++) {
+    const int p = base + q;
+    isL[q] = p < hi && ka[p] <= pv;
+    c += isL[q];
+  }
+  int nL;
+  int r = block_exclusive_scan<int>(c, ws, nL);
+#pragma unroll
+  for (int q = 0; q < IT; q++) {
+    const int p = base + q;
+    if (p >= hi) break;
+    if (isL[q]) { kb[lo + r] = ka[p]; ib[lo + r] = ia[p]; posl[lo + r] = p - lo; r++; }
+    else lam[lo + (p - lo - r)] = r;
+  }
+  __syncthreads();
+  const int m = n - nL;
+  const int* ls = lam + lo;
+  const int* ps = posl + lo;
+#pragma unroll
+  for (int q = 0; q < IT; q++) {
+    const int p = base + q;
+    if (p < hi && !isL[q]) {
+      const int a = lomuto_g_dest(p - lo, nL, m, [ls](int i) { return ls[i]; }, [ps](int i) { return ps[i]; });
+      const int dest = (a == nL) ? n : a;
+      kb[lo + dest] = ka[p];
+      ib[lo + dest] = ia[p];
+    }
+  }
+  if (threadIdx.x == 0) { kb[lo + nL] = ka[hi]; ib[lo + nL] = ia[hi]; }
+  __syncthreads();
+  for (int p = lo + threadIdx.x; p <= hi; p += blockDim.x) { ka[p] = kb[p]; ia[p] = ib[p]; }
+  __syncthreads();
+  return nL;
+}
+
+// Sub-segments of at most SORT_TINY elements are finished by one thread with
+// the literal Lomuto quicksort (find_halos.c:175-197: pivot at hi, keys
+// <= pivot to the front, then both sides), an explicit stack instead of the
+// recursion (the order in which independent sides are sorted does not change
+// the result; pushing the larger side keeps the depth below log2 n).
+constexpr int SORT_TINY = 32;
+
+__device__ __forceinline__ void tiny_quicksort(float* k, unsigned* id, int lo, int hi) {
+  int stk[16];
+  int sp = 0;
+  for (;;) {
+    while (lo < hi) {
+      const float pv = k[hi];
+      int i = lo - 1;
+      for (int j = lo; j < hi; j++) {
+        const float kj = k[j];
+        if (kj <= pv) {
+          i++;
+          const float tk = k[i]; k[i] = kj; k[j] = tk;
+          const unsigned ti = id[i]; id[i] = id[j]; id[j] = ti;
+        }
+      }
+      {
+        const float tk = k[i + 1]; k[i + 1] = k[hi]; k[hi] = tk;
+        const unsigned ti = id[i + 1]; id[i + 1] = id[hi]; id[hi] = ti;
+      }
+      const int pi = i + 1;
+      if (pi - lo < hi - pi) { stk[sp++] = pi + 1; stk[sp++] = hi; hi = pi - 1; }
+      else { stk[sp++] = lo; stk[sp++] = pi - 1; lo = pi + 1; }
+    }
+    if (sp == 0) break;
+    hi = stk[--sp];
+    lo = stk[--sp];
+  }
+}
+
 __global__ void __launch_bounds__(SORT_T)
 k_qs_small(const Seg* __restrict__ segs, int nseg, SmallSortBuffers bufs, float* __restrict__ fkey,
            unsigned* __restrict__ fid, int* __restrict__ err) {
@@ -513,9 +597,14 @@ k_qs_small(const Seg* __restrict__ segs, int nseg, SmallSortBuffers bufs, float*
   unsigned* ib = reinterpret_cast<unsigned*>(kb + SORT_SMALL);
   int* lam = reinterpret_cast<int*>(ib + SORT_SMALL);
   int* posl = lam + SORT_SMALL;
+  // pending sub-segments have more than SORT_TINY elements: at most
+  // SORT_SMALL / (SORT_TINY + 1) of them; tiny ones at most SORT_SMALL / 2
+  constexpr int PEND = 2 * (SORT_SMALL / (SORT_TINY + 1) + 1);
+  static_assert(2 * PEND + 4 * PEND + SORT_SMALL <= 3 * SORT_SMALL, "lists fit the allocation");
   int* cur = posl + SORT_SMALL;             // pending (lo, hi) pairs of this level
-  int* nxt = cur + SORT_SMALL;              // two child slots per pending segment
-  __shared__ int ncur;
+  int* nxt = cur + 2 * PEND;                // two child slots per pending segment
+  int* tiny = nxt + 4 * PEND;               // (lo, hi) pairs finished by one thread each
+  __shared__ int ncur, ntiny;
   if (blockIdx.x >= nseg) return;
   const Seg sg = segs[blockIdx.x];
   const int n = sg.hi - sg.lo + 1;
@@ -524,12 +613,28 @@ k_qs_small(const Seg* __restrict__ segs, int nseg, SmallSortBuffers bufs, float*
   for (int t = threadIdx.x; t < n; t += blockDim.x) { ka[t] = sk[t]; ia[t] = si[t]; }
   if (threadIdx.x == 0) {
     ncur = 0;
-    if (n >= 2) { cur[0] = 0; cur[1] = n - 1; ncur = 1; }
+    ntiny = 0;
+    if (n > SORT_TINY) { cur[0] = 0; cur[1] = n - 1; ncur = 1; }
+    else if (n >= 2) { tiny[0] = 0; tiny[1] = n - 1; ntiny = 1; }
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __shared__ int ws[32];
   for (int level = 0; level <= n && ncur > 0; level++) {
     const int nc = ncur;
+    if (nc <= 2) {                           // few large sub-segments: the whole block on each
+      for (int q = 0; q < nc; q++) {
+        const int lo = cur[2 * q], hi = cur[2 * q + 1];
+        const int nL = block_partition(ka, ia, kb, ib, lam, posl, lo, hi, ws);
+        if (threadIdx.x == 0) {
+          const int m = hi - lo - nL;
+          nxt[4 * q + 0] = nL >= 2 ? lo : -1;
+          nxt[4 * q + 1] = lo + nL - 1;
+          nxt[4 * q + 2] = m >= 2 ? lo + nL + 1 : -1;
+          nxt[4 * q + 3] = hi;
+        }
+      }
+    } else
     for (int q = w; q < nc; q += nw) {
       const int lo = cur[2 * q], hi = cur[2 * q + 1];
       int nL;
@@ -544,14 +649,21 @@ k_qs_small(const Seg* __restrict__ segs, int nseg, SmallSortBuffers bufs, float*
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-      int k = 0;
-      for (int q = 0; q < 2 * nc; q++)
-        if (nxt[2 * q] >= 0) { cur[2 * k] = nxt[2 * q]; cur[2 * k + 1] = nxt[2 * q + 1]; k++; }
+      int k = 0, t = ntiny;
+      for (int q = 0; q < 2 * nc; q++) {
+        const int clo = nxt[2 * q], chi = nxt[2 * q + 1];
+        if (clo < 0) continue;
+        if (chi - clo + 1 > SORT_TINY) { cur[2 * k] = clo; cur[2 * k + 1] = chi; k++; }
+        else { tiny[2 * t] = clo; tiny[2 * t + 1] = chi; t++; }
+      }
       ncur = k;
+      ntiny = t;
     }
     __syncthreads();
   }
   if (ncur > 0 && threadIdx.x == 0) atomicExch(err, 1);
+  for (int q = threadIdx.x; q < ntiny; q += blockDim.x) tiny_quicksort(ka, ia, tiny[2 * q], tiny[2 * q + 1]);
+  __syncthreads();
   for (int t = threadIdx.x; t < n; t += blockDim.x) { fkey[sg.lo + t] = ka[t]; fid[sg.lo + t] = ia[t]; }
 }
 int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
