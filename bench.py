@@ -454,14 +454,21 @@ def run_ours(args, ws, rank, local):
     # end to end through the public API with host arrays
     e2e_steps = max(1, min(args.steps, 5))
     h2d = d2h = 0
+
+    def e2e_step(s):
+        cr = exl.smoothing_ladder(k, P, R_LADDER, ND, ND, ND, LC, seed=s, n_radii=N_RADII, **BARRIER)
+        r = mock.Generate_Halos_Box_from_Pk(k, P, nd=ND, Lc=LC, seed=s, DO_2LPT=True, **BARRIER)
+        grid = simulation.Compute_Density_Grid(r["posh"], nd=ND, L=float(Lbox), window="CIC")
+        pk = simulation.Compute_Power_Spectrum(grid, L=float(Lbox), window="CIC", Nk=NK_PK)
+        return cr, r, grid, pk
+
+    for w in range(min(args.warmup, 2)):               # untimed: the public API's host buffers settle
+        e2e_step(seed0 + 150 + w)
     barrier(ws)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for s in range(e2e_steps):
-        cr = exl.smoothing_ladder(k, P, R_LADDER, ND, ND, ND, LC, seed=seed0 + 200 + s, n_radii=N_RADII, **BARRIER)
-        r = mock.Generate_Halos_Box_from_Pk(k, P, nd=ND, Lc=LC, seed=seed0 + 200 + s, DO_2LPT=True, **BARRIER)
-        grid = simulation.Compute_Density_Grid(r["posh"], nd=ND, L=float(Lbox), window="CIC")
-        pk = simulation.Compute_Power_Spectrum(grid, L=float(Lbox), window="CIC", Nk=NK_PK)
+        cr, r, grid, pk = e2e_step(seed0 + 200 + s)
         n = r["posh"].shape[0]
         h2d += k.nbytes + P.nbytes + 12 * n + 4 * ng
         d2h += cr["cross"].nbytes + 16 * n + 4 * ng + pk["k"].nbytes + pk["Pk"].nbytes + pk["Nk"].nbytes

@@ -105,6 +105,8 @@ struct Ctx {
   size_t shell_ncap = 0, shell_nall = 0;
   std::string mass_key;                 // mass-function splines (B_WORK2)
   std::string ladder_key;               // ladder window table (B_LADDERW)
+  std::string ladder_tab_key;           // ladder radii and barriers (host)
+  std::vector<float> ladder_R, ladder_B;
   // sorted peaks of the last grid given to exh_find_halos (B_PEAKS2), by digest
   unsigned long long peak_hash = 0;
   int peak_nd[3] = {0, 0, 0};

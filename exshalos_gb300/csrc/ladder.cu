@@ -439,11 +439,21 @@ extern "C" int exh_smoothing_ladder(exh_ctx* ctx, const float* k, const float* P
   BoxParams b;
   EXH_TRY(setup_box(&b, prm->ndx, prm->ndy, prm->ndz, prm->Lc, prm->Om0, prm->redshift, prm->dc, prm->Nmin, prm->a,
                     prm->beta, prm->alpha, prm->seed));
-  std::vector<float> R, B;
-  if (ladder_tables(b, k, P, Nk, n_radii, R_max, R, B) != EXH_OK) {
-    exh_set_error_msg("ladder needs 1..255 radii and R_max >= Lc", __FILE__, __LINE__);
-    return EXH_E_INVALID;
+  // radii and barriers, reused while every input they depend on repeats
+  std::string key(reinterpret_cast<const char*>(k), sizeof(float) * (size_t)std::max(Nk, 0));
+  key.append(reinterpret_cast<const char*>(P), sizeof(float) * (size_t)std::max(Nk, 0));
+  const float kf[9] = {R_max, b.Lc, b.dc, b.Omz, b.a, b.beta, b.alpha, (float)n_radii, (float)b.DO_EB};
+  key.append(reinterpret_cast<const char*>(kf), sizeof(kf));
+  if (key != c.ladder_tab_key) {
+    c.ladder_tab_key.clear();
+    if (ladder_tables(b, k, P, Nk, n_radii, R_max, c.ladder_R, c.ladder_B) != EXH_OK) {
+      exh_set_error_msg("ladder needs 1..255 radii and R_max >= Lc", __FILE__, __LINE__);
+      return EXH_E_INVALID;
+    }
+    c.ladder_tab_key = key;
   }
+  const std::vector<float>& R = c.ladder_R;
+  const std::vector<float>& B = c.ladder_B;
   float* A_dev = nullptr;
   EXH_TRY(upload_amplitudes(c, b, k, P, Nk, &A_dev, st));
   const FieldModes modes = make_modes(b, A_dev, prm->fixed, prm->phase);
