@@ -83,6 +83,7 @@ int exh_ctx_destroy(exh_ctx* ctx) {
     cudaStreamDestroy(ctx->c.lane_st[i]);
   }
   for (auto& kv : ctx->c.plans) fft_plan_destroy(&kv.second);
+  if (ctx->c.ladder_graph) cudaGraphExecDestroy(ctx->c.ladder_graph);
   if (ctx->c.side) {
     cudaEventDestroy(ctx->c.ev_fork);
     cudaEventDestroy(ctx->c.ev_join);

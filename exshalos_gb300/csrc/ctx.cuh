@@ -106,6 +106,8 @@ struct Ctx {
   std::string mass_key;                 // mass-function splines (B_WORK2)
   std::string ladder_key;               // ladder window table (B_LADDERW)
   std::string ladder_tab_key;           // ladder radii and barriers (host)
+  std::string ladder_seen_key, ladder_graph_key;
+  cudaGraphExec_t ladder_graph = nullptr;   // captured radius loop
   std::vector<float> ladder_R, ladder_B;
   // sorted peaks of the last grid given to exh_find_halos (B_PEAKS2), by digest
   unsigned long long peak_hash = 0;

@@ -56,23 +56,6 @@ __global__ void k_ladder_wtab(const float* __restrict__ R, int nr, int nn, doubl
   }
 }
 
-// x-pass source: stored modes times W(|k| R), W from the table row of R
-struct LadderGen {
-  static constexpr int io_bytes = 8;
-  const float2* __restrict__ dk;
-  const float* __restrict__ w;
-  int n0, nc, h;
-  __device__ __forceinline__ float2 operator()(int, int e, int inner) const {
-    const int j = inner / nc, k = inner % nc;
-    const int ii = (2 * e < n0) ? e : e - n0;
-    const int jj = (2 * j < n0) ? j : j - n0;
-    const int kk = (k == h) ? -h : k;
-    const float wv = __ldg(&w[ii * ii + jj * jj + kk * kk]);
-    const float2 v = dk[(size_t)e * inner_size() + inner];
-    return make_float2(v.x * wv, v.y * wv);
-  }
-  __device__ __forceinline__ size_t inner_size() const { return (size_t)n0 * nc; }
-};
 
 // y-pass source (the y transform runs first): stored modes times W(|k| R);
 // its tiles read runs of kz within one x plane, a better DRAM pattern than
@@ -401,25 +384,67 @@ int smoothing_ladder(Ctx& c, const BoxParams& b, const FieldModes& modes, int n_
     c.ladder_key = key;
   }
   EXH_CUDA_TRY(cudaMemsetAsync(cross, 255, b.ng, st));
-  for (int i = n_radii - 1; i >= 0; i--) {       // large scales first
-    LadderGen gen{dk, wtab + (size_t)i * nn, b.nd[0], p->nc, h};
-    CrossStore cs{cross, b.nd[2], b.Normx, B[i], i};
-    // y then x (both complex, in either order), then the z pass with the
-    // barrier test; the mode read and the window sit in the y pass
-    (void)gen;
-    cudaError_t ey = cudaSuccess;
-    if (!launch_ladder_y(*p, dk, wtab + (size_t)i * nn, h, work, st, &ey))
-      ey = launch_strided(LadderGenY{dk, wtab + (size_t)i * nn, b.nd[0], p->nc, h}, CplxStore{work, p->ny, p->nc},
-                          p->py, p->twy, 1.f, p->nx, p->nc, st);
-    EXH_CUDA_TRY(ey);
-    EXH_CUDA_TRY(launch_strided(CplxLoad{work, p->nx, p->ny * p->nc}, CplxStore{work, p->nx, p->ny * p->nc}, p->px,
-                                p->twx, 1.f, 1, p->ny * p->nc, st));
-    cudaError_t e = cudaSuccess;
-    if (!launch_ladder_z(*p, work, cross, b.Normx, B[i], i, st, &e))
-      e = launch_c2r_rows(HalfLoad{work, p->nc}, cs, *p, (size_t)p->nx * p->ny, st);
-    EXH_CUDA_TRY(e);
+  // the radius loop: y then x (both complex, in either order), then the z
+  // pass with the barrier test; the mode read and the window sit in the y
+  // pass.  Three kernels per radius, the same sequence whenever the buffers,
+  // tables and map repeat.
+  auto radii = [&](cudaStream_t s) -> int {
+    for (int i = n_radii - 1; i >= 0; i--) {       // large scales first
+      CrossStore cs{cross, b.nd[2], b.Normx, B[i], i};
+      cudaError_t ey = cudaSuccess;
+      if (!launch_ladder_y(*p, dk, wtab + (size_t)i * nn, h, work, s, &ey))
+        ey = launch_strided(LadderGenY{dk, wtab + (size_t)i * nn, b.nd[0], p->nc, h}, CplxStore{work, p->ny, p->nc},
+                            p->py, p->twy, 1.f, p->nx, p->nc, s);
+      EXH_CUDA_TRY(ey);
+      EXH_CUDA_TRY(launch_strided(CplxLoad{work, p->nx, p->ny * p->nc}, CplxStore{work, p->nx, p->ny * p->nc},
+                                  p->px, p->twx, 1.f, 1, p->ny * p->nc, s));
+      cudaError_t e = cudaSuccess;
+      if (!launch_ladder_z(*p, work, cross, b.Normx, B[i], i, s, &e))
+        e = launch_c2r_rows(HalfLoad{work, p->nc}, cs, *p, (size_t)p->nx * p->ny, s);
+      EXH_CUDA_TRY(e);
+    }
+    return EXH_OK;
+  };
+  // With per-kernel timing on, the kernels are launched one by one.  Else
+  // the loop is captured into a CUDA graph on the second call with the same
+  // arguments (the first one settles buffers and kernel attributes) and
+  // replayed with one launch from then on.
+  if (timing_on()) return radii(st);
+  std::string gk;
+  const void* ptrs[5] = {p, dk, work, wtab, cross};
+  gk.append(reinterpret_cast<const char*>(ptrs), sizeof(ptrs));
+  gk.append(reinterpret_cast<const char*>(B), sizeof(float) * n_radii);
+  gk.append(reinterpret_cast<const char*>(&b.Normx), sizeof(float));
+  gk.append(reinterpret_cast<const char*>(b.nd), sizeof(b.nd));
+  gk.append(c.ladder_key);
+  if (c.ladder_graph && gk == c.ladder_graph_key) {
+    EXH_CUDA_TRY(cudaGraphLaunch(c.ladder_graph, st));
+    count_launch(3 * n_radii);
+    return EXH_OK;
   }
-  return EXH_OK;
+  if (gk != c.ladder_seen_key) {
+    c.ladder_seen_key = gk;
+    return radii(st);
+  }
+  cudaStream_t cap;
+  EXH_TRY(c.side_stream(&cap));
+  EXH_CUDA_TRY(cudaStreamSynchronize(cap));
+  EXH_CUDA_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+  const int rs = radii(cap);
+  cudaGraph_t g = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(cap, &g);
+  cudaGraphExec_t ex = nullptr;
+  if (rs == EXH_OK && ec == cudaSuccess && g && cudaGraphInstantiate(&ex, g, 0) == cudaSuccess) {
+    cudaGraphDestroy(g);
+    if (c.ladder_graph) cudaGraphExecDestroy(c.ladder_graph);
+    c.ladder_graph = ex;
+    c.ladder_graph_key = gk;
+    EXH_CUDA_TRY(cudaGraphLaunch(ex, st));        // the captured kernels were counted once when captured
+    return EXH_OK;
+  }
+  if (g) cudaGraphDestroy(g);
+  cudaGetLastError();                              // capture not possible: launch directly
+  return radii(st);
 }
 
 }  // namespace exh
