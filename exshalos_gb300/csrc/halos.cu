@@ -283,7 +283,7 @@ k_qs_place(const float* __restrict__ key, const unsigned* __restrict__ id, const
            const int* __restrict__ cseg, const int* __restrict__ coff, const int* __restrict__ nchunks,
            const int* __restrict__ cLoff, const int* __restrict__ segNL, int* __restrict__ lam,
            int2* __restrict__ chain, float* __restrict__ okey, unsigned* __restrict__ oid, float* __restrict__ fkey,
-           unsigned* __restrict__ fid) {
+           unsigned* __restrict__ fid, const int* __restrict__ j4) {
   const int ch = blockIdx.x;
   if (ch >= *nchunks) return;
   const int sidx = cseg[ch];
@@ -312,17 +312,16 @@ k_qs_place(const float* __restrict__ key, const unsigned* __restrict__ id, const
       act[q] = p < end && !isL[q];
       a[q] = p - s.lo;
     }
-    const int2* cs = chain + s.lo;
-    for (int it = 0; it <= s.hi - s.lo; it++) {      // each step moves a chain forward
+    // a chain position a < nL is an L rank, so every load of the four-step
+    // table moves a chain four steps or to its end
+    const int* js = j4 + s.lo;
+    for (int it = 0; it <= s.hi - s.lo; it++) {      // each load moves a chain up to four steps
       bool any = false;
 #pragma unroll
       for (int q = 0; q < CH_ITEMS; q++) {
         if (act[q] && a[q] < nL) {
-          const int2 v = __ldg(&cs[a[q]]);
-          const int c = v.x - a[q];
-          if (c <= 0) { a[q] = nL; continue; }          // never loop on inconsistent input
-          const int steps = (v.y - a[q] + c - 1) / c;
-          a[q] += c * max(steps, 1);
+          const int nx = __ldg(&js[a[q]]);
+          a[q] = nx > a[q] ? nx : nL;                   // never loop on inconsistent input
           any = true;
         }
       }
@@ -365,6 +364,43 @@ k_qs_place(const float* __restrict__ key, const unsigned* __restrict__ id, const
     oid[s.lo + nL] = id[s.hi];
     fkey[s.lo + nL] = key[s.hi];
     fid[s.lo + nL] = id[s.hi];
+  }
+}
+
+// One step of a > chain from relative position a < nL, from its chain entry.
+__device__ __forceinline__ int chain_next(int a, int2 v, int nL) {
+  const int c = v.x - a;
+  if (c <= 0) return nL;                           // never loop on inconsistent input
+  const int steps = (v.y - a + c - 1) / c;
+  return a + c * max(steps, 1);
+}
+
+// Jump tables over the L ranks of every segment of the level (chains never
+// share a position, and the step depends on the position only):
+// DOUBLE == false: jt[r] = position two steps after r, or the chain's end
+// (>= nL) if it comes first; DOUBLE == true: jo[r] = jt applied twice (four
+// steps).  Phase 2 then walks four steps per load.
+template <bool DOUBLE>
+__global__ void __launch_bounds__(CH_T)
+k_qs_jump(const Seg* __restrict__ segs, const int* __restrict__ cseg, const int* __restrict__ coff,
+          const int* __restrict__ nchunks, const int* __restrict__ segNL, const int2* __restrict__ chain,
+          const int* __restrict__ jt, int* __restrict__ jo) {
+  const int ch = blockIdx.x;
+  if (ch >= *nchunks) return;
+  const int sidx = cseg[ch];
+  const Seg s = segs[sidx];
+  const int nL = segNL[sidx];
+  const int r0 = coff[ch], r1 = min(min(r0 + CH, s.hi - s.lo), nL);
+  for (int r = r0 + threadIdx.x; r < r1; r += CH_T) {
+    int a;
+    if (!DOUBLE) {
+      a = chain_next(r, __ldg(&chain[s.lo + r]), nL);
+      if (a < nL) a = chain_next(a, __ldg(&chain[s.lo + a]), nL);
+    } else {
+      a = __ldg(&jt[s.lo + r]);
+      if (a < nL) a = __ldg(&jt[s.lo + a]);
+    }
+    jo[s.lo + r] = a;
   }
 }
 
@@ -676,11 +712,13 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
   float* fk = reinterpret_cast<float*>(i1 + cap);
   // final arrays live in B_PEAKS2
   EXH_TRY(c.buf[B_PEAKS2].ensure((sizeof(float) + sizeof(unsigned)) * cap + sizeof(int) * (cap + 1) +
-                                  sizeof(int2) * cap));
+                                  sizeof(int2) * cap + 2 * sizeof(int) * cap));
   fk = c.buf[B_PEAKS2].as<float>();
   unsigned* fi = reinterpret_cast<unsigned*>(fk + cap);
   int* lam = reinterpret_cast<int*>(fi + cap);
   int2* chain = reinterpret_cast<int2*>(lam + cap + (cap & 1));     // 8-byte aligned
+  int* j2 = reinterpret_cast<int*>(chain + cap);                   // jump tables of the > chains
+  int* j4 = j2 + cap;
   if (np <= 1) {
     if (np == 1) {
       EXH_CUDA_TRY(cudaMemcpyAsync(fk, k0, sizeof(float), cudaMemcpyDeviceToDevice, st));
@@ -731,15 +769,17 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
         k_qs_count<<<max_chunks, CH_T, 0, st>>>(kb[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL);
         k_qs_seg_scan<<<max_segs, 256, 0, st>>>(d_cfirst, &ctl->nseg, d_cL, d_nl);
         k_qs_place<1><<<max_chunks, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL, d_nl,
-                                                   lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi);
+                                                   lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi, j4);
         k_qs_place<3><<<max_chunks, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL, d_nl,
-                                                   lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi);
+                                                   lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi, j4);
+        k_qs_jump<false><<<max_chunks, CH_T, 0, st>>>(d_segs, d_cseg, d_coff, &ctl->nch, d_nl, chain, nullptr, j2);
+        k_qs_jump<true><<<max_chunks, CH_T, 0, st>>>(d_segs, d_cseg, d_coff, &ctl->nch, d_nl, chain, j2, j4);
         k_qs_place<2><<<max_chunks, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL, d_nl,
-                                                   lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi);
+                                                   lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi, j4);
         k_qs_children<<<exh_div_up(max_segs, 128), 128, 0, st>>>(d_segs, d_nl, ctl, d_next, d_small, d_single,
                                                                  max_segs, cap_small);
         k_qs_chunks<<<1, QS_CHUNK_T, 0, st>>>(ctl, d_next, d_segs, d_cfirst, d_cseg, d_coff, max_chunks);
-        count_launch(7);
+        count_launch(9);
         EXH_CUDA_TRY(cudaGetLastError());
       }
       if ((level + 1) % LEVELS_PER_CHECK == 0) {
