@@ -180,16 +180,18 @@ def context():
 
 
 _POOL_MIN_BYTES = 1 << 20
-_POOL_PER_SHAPE = 2
+_POOL_MAX_BUFFERS = 16
 
 
 def host_empty(shape, dtype):
     """An uninitialised host array for a large output that the library fills
-    completely.  Arrays of 1 MB or more come from a per-thread pool of up to
-    two buffers per shape: a buffer is handed out again only once the pool
-    holds the last reference to it (the caller has dropped it), so a result
-    never shares memory with a live array; the pool saves the page faults and
-    zero-fill of a fresh allocation on every call in a loop."""
+    completely.  Arrays of 1 MB or more are views of byte buffers from a
+    per-thread pool: a buffer at least as large as the request (and at most
+    twice) is handed out again only once the pool holds the last reference to
+    it (the caller has dropped every array viewing it), so a result never
+    shares memory with a live array.  Outputs whose length changes from call
+    to call (halo catalogues) reuse the same buffers; the pool saves the page
+    faults and zero-fill of a fresh allocation on every call in a loop."""
     dt = np.dtype(dtype)
     shape = tuple(int(x) for x in (shape if isinstance(shape, (tuple, list)) else (shape,)))
     nbytes = int(np.prod(shape, dtype=np.int64)) * dt.itemsize
@@ -197,16 +199,23 @@ def host_empty(shape, dtype):
         return np.empty(shape, dtype=dt)
     pool = getattr(_tls, "pool", None)
     if pool is None:
-        pool = _tls.pool = {}
-    bufs = pool.setdefault((shape, dt.str), [])
-    for i in range(len(bufs)):
-        if sys.getrefcount(bufs[i]) <= 2:        # the list entry and getrefcount's argument
-            return bufs[i]
-    a = np.empty(shape, dtype=dt)
-    bufs.append(a)
-    if len(bufs) > _POOL_PER_SHAPE:
-        bufs.pop(0)
-    return a
+        pool = _tls.pool = []
+    pick = -1
+    for i in range(len(pool)):
+        cap = pool[i].nbytes
+        if nbytes <= cap <= 2 * nbytes and sys.getrefcount(pool[i]) <= 2:   # list entry + argument
+            if pick < 0 or cap < pool[pick].nbytes:
+                pick = i
+    if pick < 0:
+        pool.append(np.empty(nbytes + nbytes // 8, dtype=np.uint8))
+        pick = len(pool) - 1
+        if len(pool) > _POOL_MAX_BUFFERS:            # drop the oldest buffer nobody holds
+            for i in range(len(pool) - 1):
+                if sys.getrefcount(pool[i]) <= 2:
+                    del pool[i]
+                    pick -= 1
+                    break
+    return pool[pick][:nbytes].view(dt).reshape(shape)
 
 
 def ptr(a):
