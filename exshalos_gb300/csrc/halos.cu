@@ -312,8 +312,8 @@ k_qs_place(const float* __restrict__ key, const unsigned* __restrict__ id, const
       act[q] = p < end && !isL[q];
       a[q] = p - s.lo;
     }
-    // a chain position a < nL is an L rank, so every load of the four-step
-    // table moves a chain four steps or to its end
+    // a chain position a < nL is an L rank, so every load of the eight-step
+    // table moves a chain eight steps or to its end
     const int* js = j4 + s.lo;
     for (int it = 0; it <= s.hi - s.lo; it++) {      // each load moves a chain up to four steps
       bool any = false;
@@ -379,7 +379,7 @@ __device__ __forceinline__ int chain_next(int a, int2 v, int nL) {
 // share a position, and the step depends on the position only):
 // DOUBLE == false: jt[r] = position two steps after r, or the chain's end
 // (>= nL) if it comes first; DOUBLE == true: jo[r] = jt applied twice (four
-// steps).  Phase 2 then walks four steps per load.
+// steps), applied again for eight.  Phase 2 then walks eight steps per load.
 template <bool DOUBLE>
 __global__ void __launch_bounds__(CH_T)
 k_qs_jump(const Seg* __restrict__ segs, const int* __restrict__ cseg, const int* __restrict__ coff,
@@ -774,12 +774,13 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
                                                    lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi, j4);
         k_qs_jump<false><<<max_chunks, CH_T, 0, st>>>(d_segs, d_cseg, d_coff, &ctl->nch, d_nl, chain, nullptr, j2);
         k_qs_jump<true><<<max_chunks, CH_T, 0, st>>>(d_segs, d_cseg, d_coff, &ctl->nch, d_nl, chain, j2, j4);
+        k_qs_jump<true><<<max_chunks, CH_T, 0, st>>>(d_segs, d_cseg, d_coff, &ctl->nch, d_nl, chain, j4, j2);
         k_qs_place<2><<<max_chunks, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL, d_nl,
-                                                   lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi, j4);
+                                                   lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi, j2);
         k_qs_children<<<exh_div_up(max_segs, 128), 128, 0, st>>>(d_segs, d_nl, ctl, d_next, d_small, d_single,
                                                                  max_segs, cap_small);
         k_qs_chunks<<<1, QS_CHUNK_T, 0, st>>>(ctl, d_next, d_segs, d_cfirst, d_cseg, d_coff, max_chunks);
-        count_launch(9);
+        count_launch(10);
         EXH_CUDA_TRY(cudaGetLastError());
       }
       if ((level + 1) % LEVELS_PER_CHECK == 0) {
