@@ -1504,7 +1504,7 @@ int flags_to_reference(const HaloDev& h, size_t ng, int64_t* out_dev, cudaStream
 }
 
 // ------------------------------------------------------------------ masses
-constexpr int MASS_CHUNK = 32;
+constexpr int MASS_CHUNK = 8;
 
 
 __global__ void k_masses(const TausJump* __restrict__ J, TausState s0, DevSpline sI, DevSpline sInv, const int* __restrict__ hpeak,
