@@ -39,7 +39,8 @@ ND, LC, NK_PK = 256, 2.0, 128
 BARRIER = dict(a=1.0, beta=0.12, alpha=0.0)
 # kernel classes whose time is set by dependent loads rather than bandwidth
 LATENCY_NOTES = {
-    "sort": "latency-bound: exact Lomuto order, dependent L2 loads along the > chains of each level",
+    "sort": "latency-bound: exact Lomuto order, dependent L2 loads along the > chains of each level "
+            "(eight steps per load through per-level jump tables)",
     "grow": "latency-bound: per-peak shell gathers and reservation rounds",
     "mass": "FP64 spline evaluations",
     "halo_disp": "per-halo gathers over member cells",
