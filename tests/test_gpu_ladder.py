@@ -65,3 +65,21 @@ def test_ladder_repeated_calls_replay_the_same_work(pk):
     th.start()
     th.join()
     assert np.array_equal(res["m"], maps[3])
+
+
+def test_ladder_graph_follows_size_and_radius_changes(pk):
+    """Alternating box sizes and radius counts in one context (buffers grow,
+    tables change, the captured loop must not be replayed on stale
+    arguments): every map equals the one of a fresh context."""
+    import threading
+    from exshalos_gb300.lib import exshalos as ex
+    k, P = pk
+    seq = [(32, 6), (64, 12), (32, 6), (32, 6), (64, 12), (64, 8), (64, 8), (32, 6)]
+    got = [ex.smoothing_ladder(k, P, 20.0, nd, nd, nd, 2.0, seed=9, n_radii=nr)["cross"].copy() for nd, nr in seq]
+    for (nd, nr), g in zip(seq, got):
+        res = {}
+        th = threading.Thread(target=lambda: res.setdefault(
+            "m", ex.smoothing_ladder(k, P, 20.0, nd, nd, nd, 2.0, seed=9, n_radii=nr)["cross"].copy()))
+        th.start()
+        th.join()
+        assert np.array_equal(res["m"], g), (nd, nr)
