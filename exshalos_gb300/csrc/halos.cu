@@ -283,7 +283,7 @@ k_qs_place(const float* __restrict__ key, const unsigned* __restrict__ id, const
            const int* __restrict__ cseg, const int* __restrict__ coff, const int* __restrict__ nchunks,
            const int* __restrict__ cLoff, const int* __restrict__ segNL, int* __restrict__ lam,
            int2* __restrict__ chain, float* __restrict__ okey, unsigned* __restrict__ oid, float* __restrict__ fkey,
-           unsigned* __restrict__ fid, const int* __restrict__ j4) {
+           unsigned* __restrict__ fid, const int* __restrict__ jt) {
   const int ch = blockIdx.x;
   if (ch >= *nchunks) return;
   const int sidx = cseg[ch];
@@ -312,9 +312,9 @@ k_qs_place(const float* __restrict__ key, const unsigned* __restrict__ id, const
       act[q] = p < end && !isL[q];
       a[q] = p - s.lo;
     }
-    // a chain position a < nL is an L rank, so every load of the eight-step
-    // table moves a chain eight steps or to its end
-    const int* js = j4 + s.lo;
+    // a chain position a < nL is an L rank, so every load of the jump table
+    // moves a chain JUMP_STEPS steps or to its end
+    const int* js = jt + s.lo;
     for (int it = 0; it <= s.hi - s.lo; it++) {      // each load moves a chain up to four steps
       bool any = false;
 #pragma unroll
@@ -375,32 +375,38 @@ __device__ __forceinline__ int chain_next(int a, int2 v, int nL) {
   return a + c * max(steps, 1);
 }
 
-// Jump tables over the L ranks of every segment of the level (chains never
-// share a position, and the step depends on the position only):
-// DOUBLE == false: jt[r] = position two steps after r, or the chain's end
-// (>= nL) if it comes first; DOUBLE == true: jo[r] = jt applied twice (four
-// steps), applied again for eight.  Phase 2 then walks eight steps per load.
-template <bool DOUBLE>
+// Jump table over the L ranks of every segment of the level (chains never
+// share a position, and the step depends on the position only): jo[r] =
+// the position JUMP_STEPS steps after r, or the chain's end (>= nL) if it
+// comes first.  Phase 2 then walks JUMP_STEPS steps per load.  The table is
+// built in one pass: every rank follows its own chain for JUMP_STEPS
+// dependent loads, all ranks at once.
+constexpr int JUMP_STEPS = 8;
+
 __global__ void __launch_bounds__(CH_T)
 k_qs_jump(const Seg* __restrict__ segs, const int* __restrict__ cseg, const int* __restrict__ coff,
           const int* __restrict__ nchunks, const int* __restrict__ segNL, const int2* __restrict__ chain,
-          const int* __restrict__ jt, int* __restrict__ jo) {
+          int* __restrict__ jo) {
   const int ch = blockIdx.x;
   if (ch >= *nchunks) return;
   const int sidx = cseg[ch];
   const Seg s = segs[sidx];
   const int nL = segNL[sidx];
   const int r0 = coff[ch], r1 = min(min(r0 + CH, s.hi - s.lo), nL);
-  for (int r = r0 + threadIdx.x; r < r1; r += CH_T) {
-    int a;
-    if (!DOUBLE) {
-      a = chain_next(r, __ldg(&chain[s.lo + r]), nL);
-      if (a < nL) a = chain_next(a, __ldg(&chain[s.lo + a]), nL);
-    } else {
-      a = __ldg(&jt[s.lo + r]);
-      if (a < nL) a = __ldg(&jt[s.lo + a]);
-    }
-    jo[s.lo + r] = a;
+  const int2* cs = chain + s.lo;
+  constexpr int PER = CH / CH_T;                   // ranks per thread, followed together
+  int a[PER];
+#pragma unroll
+  for (int q = 0; q < PER; q++) a[q] = r0 + threadIdx.x + q * CH_T;
+#pragma unroll
+  for (int st = 0; st < JUMP_STEPS; st++)
+#pragma unroll
+    for (int q = 0; q < PER; q++)
+      if (a[q] < nL && r0 + threadIdx.x + q * CH_T < r1) a[q] = chain_next(a[q], __ldg(&cs[a[q]]), nL);
+#pragma unroll
+  for (int q = 0; q < PER; q++) {
+    const int r = r0 + threadIdx.x + q * CH_T;
+    if (r < r1) jo[s.lo + r] = a[q];
   }
 }
 
@@ -712,13 +718,12 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
   float* fk = reinterpret_cast<float*>(i1 + cap);
   // final arrays live in B_PEAKS2
   EXH_TRY(c.buf[B_PEAKS2].ensure((sizeof(float) + sizeof(unsigned)) * cap + sizeof(int) * (cap + 1) +
-                                  sizeof(int2) * cap + 2 * sizeof(int) * cap));
+                                  sizeof(int2) * cap + sizeof(int) * cap));
   fk = c.buf[B_PEAKS2].as<float>();
   unsigned* fi = reinterpret_cast<unsigned*>(fk + cap);
   int* lam = reinterpret_cast<int*>(fi + cap);
   int2* chain = reinterpret_cast<int2*>(lam + cap + (cap & 1));     // 8-byte aligned
-  int* j2 = reinterpret_cast<int*>(chain + cap);                   // jump tables of the > chains
-  int* j4 = j2 + cap;
+  int* j2 = reinterpret_cast<int*>(chain + cap);                   // jump table of the > chains
   if (np <= 1) {
     if (np == 1) {
       EXH_CUDA_TRY(cudaMemcpyAsync(fk, k0, sizeof(float), cudaMemcpyDeviceToDevice, st));
@@ -769,18 +774,16 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
         k_qs_count<<<max_chunks, CH_T, 0, st>>>(kb[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL);
         k_qs_seg_scan<<<max_segs, 256, 0, st>>>(d_cfirst, &ctl->nseg, d_cL, d_nl);
         k_qs_place<1><<<max_chunks, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL, d_nl,
-                                                   lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi, j4);
+                                                   lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi, j2);
         k_qs_place<3><<<max_chunks, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL, d_nl,
-                                                   lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi, j4);
-        k_qs_jump<false><<<max_chunks, CH_T, 0, st>>>(d_segs, d_cseg, d_coff, &ctl->nch, d_nl, chain, nullptr, j2);
-        k_qs_jump<true><<<max_chunks, CH_T, 0, st>>>(d_segs, d_cseg, d_coff, &ctl->nch, d_nl, chain, j2, j4);
-        k_qs_jump<true><<<max_chunks, CH_T, 0, st>>>(d_segs, d_cseg, d_coff, &ctl->nch, d_nl, chain, j4, j2);
+                                                   lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi, j2);
+        k_qs_jump<<<max_chunks, CH_T, 0, st>>>(d_segs, d_cseg, d_coff, &ctl->nch, d_nl, chain, j2);
         k_qs_place<2><<<max_chunks, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL, d_nl,
                                                    lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi, j2);
         k_qs_children<<<exh_div_up(max_segs, 128), 128, 0, st>>>(d_segs, d_nl, ctl, d_next, d_small, d_single,
                                                                  max_segs, cap_small);
         k_qs_chunks<<<1, QS_CHUNK_T, 0, st>>>(ctl, d_next, d_segs, d_cfirst, d_cseg, d_coff, max_chunks);
-        count_launch(10);
+        count_launch(8);
         EXH_CUDA_TRY(cudaGetLastError());
       }
       if ((level + 1) % LEVELS_PER_CHECK == 0) {
