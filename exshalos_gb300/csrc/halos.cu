@@ -865,7 +865,19 @@ __device__ __forceinline__ void peak_coords(unsigned cell, const HaloScalars& hs
 // mean are broadcast from lane 0.
 // Returns 0 ok, 1 count beyond the sigma table, 2 shell beyond the tables;
 // gexit is the last shell read (the rejected one).
-__device__ int grow_warp(const GrowArgs& A, const int* __restrict__ flag, int x0, int y0, int z0, float pden,
+// Claimed cells during growth, one bit per cell (ng / 32 words, about 2 MB
+// at 256^3, resident in L2): set wherever a committing peak writes a flag, and
+// flags are only ever added while the halos grow, so a set bit is exactly a
+// flag other than FLAG_FREE.  The growth passes test the bit instead of
+// reading the 4-byte flag beside every density value.
+__device__ __forceinline__ bool cell_claimed(const unsigned* __restrict__ claimed, size_t cell) {
+  return (__ldg(&claimed[cell >> 5]) >> (cell & 31)) & 1u;
+}
+__device__ __forceinline__ void claim_cell(unsigned* claimed, size_t cell) {
+  atomicOr(&claimed[cell >> 5], 1u << (cell & 31));
+}
+
+__device__ int grow_warp(const GrowArgs& A, const unsigned* __restrict__ claimed, int x0, int y0, int z0, float pden,
                          int lane, double* wbuf, int& count_out, int& gtmp_out, int& gexit_out) {
   const HaloScalars& hs = A.hs;
   double den = (double)pden, den_tmp = (double)pden;     // meaningful in lane 0
@@ -888,7 +900,7 @@ __device__ int grow_warp(const GrowArgs& A, const int* __restrict__ flag, int x0
       const int q = base + lane;
       if (q < s1) {
         const size_t cell = cell_at(x0, y0, z0, A.t.off_cap[q], hs);
-        wbuf[lane] = (flag[cell] != FLAG_FREE) ? mneg : (double)A.delta[cell];
+        wbuf[lane] = cell_claimed(claimed, cell) ? mneg : (double)A.delta[cell];
       }
       __syncwarp();
       const int n = min(32, s1 - base);
@@ -970,7 +982,7 @@ __device__ __forceinline__ int fb_ge(FBound b, float t) {
   return -1;
 }
 
-__device__ int grow_warp_f32(const GrowArgs& A, const int* __restrict__ flag, int x0, int y0, int z0, float pden,
+__device__ int grow_warp_f32(const GrowArgs& A, const unsigned* __restrict__ claimed, int x0, int y0, int z0, float pden,
                              int lane, int& count_out, int& gtmp_out, int& gexit_out) {
   const HaloScalars& hs = A.hs;
   FBound den{pden, 0.f}, den_tmp{pden, 0.f};
@@ -996,7 +1008,7 @@ __device__ int grow_warp_f32(const GrowArgs& A, const int* __restrict__ flag, in
     int steps = 0;
     for (int q = s0 + lane; q < s1; q += 32) {
       const size_t cell = cell_at(x0, y0, z0, A.t.off_cap[q], hs);
-      if (flag[cell] != FLAG_FREE) foreign = true;
+      if (cell_claimed(claimed, cell)) foreign = true;
       const float v = A.delta[cell];
       s += v;
       sa += fabsf(v);
@@ -1064,7 +1076,7 @@ __device__ __forceinline__ void count_push(int* n) {
 // the shell sums are sequential (bound depth = cells in the shell).  Returns
 // 3 when a comparison is undecided or the growth would pass shell LANE_GMAX;
 // the warp path then redoes the peak from the start.
-__device__ int grow_lane_f32(const GrowArgs& A, const int* __restrict__ flag, int x0, int y0, int z0, float pden,
+__device__ int grow_lane_f32(const GrowArgs& A, const unsigned* __restrict__ claimed, int x0, int y0, int z0, float pden,
                              int& count_out, int& gtmp_out, int& gexit_out) {
   const HaloScalars& hs = A.hs;
   FBound den{pden, 0.f}, den_tmp{pden, 0.f};
@@ -1090,7 +1102,7 @@ __device__ int grow_lane_f32(const GrowArgs& A, const int* __restrict__ flag, in
     bool foreign = false;
     for (int q = s0; q < s1; q++) {
       const size_t cell = cell_at(x0, y0, z0, A.t.off_cap[q], hs);
-      foreign |= flag[cell] != FLAG_FREE;
+      foreign |= cell_claimed(claimed, cell);
       const float v = A.delta[cell];
       sm += v;
       sa += fabsf(v);
@@ -1129,6 +1141,7 @@ struct RoundArgs {
   unsigned char* state;
   int* flag;
   unsigned* resv;
+  unsigned* claimed;   // one bit per cell: flag != FLAG_FREE
   int tag;
   int* cnt;
   int* gtmp;
@@ -1166,7 +1179,7 @@ k_tentative(GrowArgs A, const int* __restrict__ list, const int* __restrict__ nl
     const int r = list[t];
     const int64_t l = A.np - 1 - r;
     const unsigned cell0 = A.id[l];
-    if (R.flag[cell0] != FLAG_FREE) {        // find_halos.c:233: the peak is already inside a halo
+    if (cell_claimed(R.claimed, cell0)) {    // find_halos.c:233: the peak is already inside a halo
       R.state[r] = 1;
       R.cnt[r] = 0;
       continue;
@@ -1175,7 +1188,7 @@ k_tentative(GrowArgs A, const int* __restrict__ list, const int* __restrict__ nl
     int x, y, z;
     peak_coords(cell0, A.hs, x, y, z);
     int count, gt, ge;
-    const int st = grow_lane_f32(A, R.flag, x, y, z, A.key[l], count, gt, ge);
+    const int st = grow_lane_f32(A, R.claimed, x, y, z, A.key[l], count, gt, ge);
     if (st == 3) {
       list_push(R.wlist, R.nw, r);
       continue;
@@ -1205,8 +1218,8 @@ k_tentative_warp(GrowArgs A, RoundArgs R) {
     int x, y, z;
     peak_coords(cell0, A.hs, x, y, z);
     int count, gt, ge;
-    int st = grow_warp_f32(A, R.flag, x, y, z, A.key[l], lane, count, gt, ge);
-    if (st == 3) st = grow_warp(A, R.flag, x, y, z, A.key[l], lane, wb[threadIdx.x >> 5], count, gt, ge);
+    int st = grow_warp_f32(A, R.claimed, x, y, z, A.key[l], lane, count, gt, ge);
+    if (st == 3) st = grow_warp(A, R.claimed, x, y, z, A.key[l], lane, wb[threadIdx.x >> 5], count, gt, ge);
     if (lane == 0) { R.cnt[r] = count; R.gtmp[r] = gt; R.gexit[r] = ge; R.gst[r] = st; }
     if (lane == 0 && R.nwords) R.nwords[r] += tentative_words(A, ge);
     const unsigned key = resv_key(R.tag, r);
@@ -1263,9 +1276,14 @@ k_commit(GrowArgs A, const int* __restrict__ list, const int* __restrict__ nlist
     }
     if (!commit_status(R, r)) continue;
     const int we = A.t.start_all[R.gtmp[r]];     // cells with r^2 < grows_tmp
-    for (int q = 0; q < we; q++) R.flag[cell_at(x, y, z, A.t.off_all[q], A.hs)] = r;
+    for (int q = 0; q < we; q++) {
+      const size_t cq = cell_at(x, y, z, A.t.off_all[q], A.hs);
+      R.flag[cq] = r;
+      claim_cell(R.claimed, cq);
+    }
     if (R.nwords) R.nwords[r] += (unsigned)we;
     R.flag[cell0] = -(r + 2);
+    claim_cell(R.claimed, cell0);
   }
 }
 
@@ -1293,10 +1311,17 @@ k_commit_warp(GrowArgs A, RoundArgs R) {
     if (lane == 0) keep = commit_status(R, r);
     if (!__shfl_sync(0xffffffffu, (int)keep, 0)) continue;
     const int we = A.t.start_all[R.gtmp[r]];
-    for (int q = lane; q < we; q += 32) R.flag[cell_at(x, y, z, A.t.off_all[q], A.hs)] = r;
+    for (int q = lane; q < we; q += 32) {
+      const size_t cq = cell_at(x, y, z, A.t.off_all[q], A.hs);
+      R.flag[cq] = r;
+      claim_cell(R.claimed, cq);
+    }
     if (lane == 0 && R.nwords) R.nwords[r] += (unsigned)we;
     __syncwarp();
-    if (lane == 0) R.flag[cell0] = -(r + 2);
+    if (lane == 0) {
+      R.flag[cell0] = -(r + 2);
+      claim_cell(R.claimed, cell0);
+    }
   }
 }
 
@@ -1367,9 +1392,11 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   }
   const size_t ng = b.ng;
   const size_t npr = std::max<int64_t>(nproc, 1);
-  EXH_TRY(c.buf[B_FLAG].ensure(sizeof(int) * ng * 2));
+  const size_t nclaim = ng / 32 + 1;
+  EXH_TRY(c.buf[B_FLAG].ensure(sizeof(int) * ng * 2 + sizeof(unsigned) * nclaim));
   h->flag = c.buf[B_FLAG].as<int>();
   h->resv = reinterpret_cast<unsigned*>(h->flag + ng);
+  unsigned* claimed = h->resv + ng;
   EXH_TRY(c.buf[B_HALO].ensure(npr * (sizeof(int) * 8 + 1) + 64));
   h->gfree = c.buf[B_HALO].as<int>();
   h->gfin = h->gfree + npr;
@@ -1382,6 +1409,7 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   h->state = reinterpret_cast<unsigned char*>(h->words + npr);
   EXH_CUDA_TRY(cudaMemsetAsync(h->flag, 0xff, sizeof(int) * ng, st));      // FLAG_FREE
   EXH_CUDA_TRY(cudaMemsetAsync(h->resv, 0, sizeof(unsigned) * ng, st));
+  EXH_CUDA_TRY(cudaMemsetAsync(claimed, 0, sizeof(unsigned) * nclaim, st));
   EXH_CUDA_TRY(cudaMemsetAsync(h->state, 0, npr, st));
   EXH_CUDA_TRY(cudaMemsetAsync(h->cnt, 0, sizeof(int) * npr, st));
   h->nh = 0;
@@ -1427,7 +1455,7 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
     EXH_CUDA_TRY(cudaMemsetAsync(dcnt + 3 - cur, 0, sizeof(int), st));      // next list
     EXH_CUDA_TRY(cudaMemsetAsync(dcnt + 4, 0, sizeof(int) * 2, st));        // warp lists
     RoundArgs R;
-    R.state = h->state; R.flag = h->flag; R.resv = h->resv; R.tag = tag;
+    R.state = h->state; R.flag = h->flag; R.resv = h->resv; R.claimed = claimed; R.tag = tag;
     R.cnt = h->cnt; R.gtmp = h->gfin; R.gexit = gexit; R.gst = gst; R.gfin = h->gfin;
     R.npend = dcnt; R.err = dcnt + 1; R.next = lists[cur ^ 1]; R.nnext = dcnt + 3 - cur;
     R.wlist = wlist; R.nw = dcnt + 4; R.clist = clist; R.nc = dcnt + 5;
