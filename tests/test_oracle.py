@@ -167,7 +167,7 @@ def test_ladder_matches_numpy_restatement(orc, pk):
         x = kk * float(r)
         with np.errstate(invalid="ignore", divide="ignore"):
             w = np.where(x > 0, 3 * (np.sin(x) - x * np.cos(x)) / np.where(x > 0, x, 1) ** 3, 1.0)
-        fields.append(np.fft.irfftn(dk * w, s=(nd, nd, nd)) * nd ** 3 * p.Normx_d)
+        fields.append(np.fft.irfftn(dk * w, s=(nd, nd, nd), axes=(0, 1, 2)) * nd ** 3 * p.Normx_d)
     # barriers at the 90th percentile of each smoothed field
     B = np.array([np.percentile(fl, 90) for fl in fields], dtype=np.float32)
     want = np.full((nd, nd, nd), 255, dtype=np.uint8)
