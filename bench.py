@@ -92,26 +92,46 @@ class ClockSampler:
     FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
+    INTERVAL_MS = 50
+
     def __init__(self, device):
         self.device = device
         self.proc = None
-        self.lines = []
+        self.lines = []          # (monotonic time, csv line)
+        self.windows = []
 
     def start(self):
+        """Start nvidia-smi and wait (at most 5 s) for its first sample, so
+        that the sampler is live when the timed region opens."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", str(self.INTERVAL_MS)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except OSError:
             self.proc = None
+            return
+        t_end = time.monotonic() + 5.0
+        while not self.lines and time.monotonic() < t_end and self.proc.poll() is None:
+            time.sleep(0.01)
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.monotonic(), line.strip()))
+
+    def open_window(self):
+        self.windows.append([time.monotonic(), None])
+
+    def close_window(self):
+        if self.windows and self.windows[-1][1] is None:
+            self.windows[-1][1] = time.monotonic()
 
     def stop(self):
+        """Median SM clock and the throttle reasons seen.  With windows
+        (timed regions) marked, only the samples taken inside them count, and
+        the sample before the first window is added when a window is shorter
+        than the sampling interval and caught none."""
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -119,9 +139,17 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
+        lines = self.lines
+        if self.windows:
+            inside = [(t, ln) for t, ln in lines
+                      if any(a <= t <= (b if b is not None else float("inf")) for a, b in self.windows)]
+            if not inside:
+                before = [(t, ln) for t, ln in lines if t < self.windows[0][0]]
+                inside = before[-1:]
+            lines = inside
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for _, ln in lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 6:
                 continue
@@ -408,11 +436,13 @@ def run_ours(args, ws, rank, local):
     s_halo = torch.cuda.Stream(priority=-1)
     hs = C.c_void_p(s_halo.cuda_stream)
 
-    def step(seed):
+    def step(seed, serial=False):
+        # serial: the ladder on the halo chain's stream (the per-class timing
+        # pass, where each class's event time must cover its own kernels only)
         prm = _capi.default_params(ndx=ND, ndy=ND, ndz=ND, Lc=LC, seed=seed, DO_2LPT=1, **BARRIER)
         _capi.check(L_.exh_smoothing_ladder(ctx_lad, _capi.ptr(k), _capi.ptr(P), k.size, prm, N_RADII, R_LADDER,
                                             _capi.ptr(cross_dev), None, None, _capi.EXH_MEM_DEVICE,
-                                            C.c_void_p(s_lad.cuda_stream)))
+                                            hs if serial else C.c_void_p(s_lad.cuda_stream)))
         _capi.check(L_.exh_halos_box_from_pk(ctx, _capi.ptr(k), _capi.ptr(P), k.size, prm, C.byref(nh), hs))
         _capi.check(L_.exh_halos_fetch(ctx, _capi.ptr(posh_dev), None, None, None, None, None, None, None, None,
                                        _capi.EXH_MEM_DEVICE, hs))
@@ -433,6 +463,7 @@ def run_ours(args, ws, rank, local):
     barrier(ws)
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks.open_window()
     ev0.record()
     s_lad.wait_stream(torch.cuda.current_stream())
     s_halo.wait_stream(torch.cuda.current_stream())
@@ -442,16 +473,22 @@ def run_ours(args, ws, rank, local):
     torch.cuda.current_stream().wait_stream(s_halo)
     ev1.record()
     torch.cuda.synchronize()
+    clocks.close_window()
     barrier(ws)
     launches = _capi.launch_count() - l0
-    clk = clocks.stop()
     # per-kernel-class times come from a second pass of the same steps with
     # CUDA events around every launch (they add host work, so the headline
-    # is timed without them); the ladder then launches its kernels one by one
+    # is timed without them); in that pass every stage runs on one stream
+    # (the ladder on the halo chain's, the library's LPT without its fork)
+    # and the ladder launches its kernels one by one
     _capi.timing_enable(True)
+    clocks.open_window()
     for s in range(args.steps):
-        step(seed0 + 100 + s)
+        step(seed0 + 100 + s, serial=True)
     torch.cuda.synchronize()
+    clocks.close_window()
+    clk = clocks.stop()
+    clk["windows"] = "the timed steps and the per-class pass"
     rep = _capi.timing_report()
     _capi.timing_enable(False)
     t_dev = ev0.elapsed_time(ev1) / 1000.0
@@ -525,7 +562,8 @@ def run_ours(args, ws, rank, local):
                    "l2": "inputs and intermediates (>1 GB per realisation) exceed L2",
                    "smoothing_ladder": f"{N_RADII} radii, Lc..{R_LADDER} Mpc/h, u8 first-crossing map",
                    "class_timing": "stage_ms_per_step, roofline_by_class and roofline from a second pass of the "
-                                   "same number of steps with CUDA events around every launch",
+                                   "same number of steps with CUDA events around every launch, all stages on one stream "
+                                   "(no overlap, so each class's time is its own kernels')",
                    "mean_halos": float(np.mean(nh_seen[-args.steps:])) if nh_seen else None},
         "e2e": {"value": e2e, "unit": "realisations/s", "h2d_bytes_per_step": int(h2d / e2e_steps),
                 "d2h_bytes_per_step": int(d2h / e2e_steps)},
@@ -592,11 +630,13 @@ def run_box512(args, ws, rank, local):
     clocks.start()
     _capi.timing_enable(True)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks.open_window()
     ev0.record()
     for s in range(args.steps):
         step(1 + s)
     ev1.record()
     torch.cuda.synchronize()
+    clocks.close_window()
     rep = _capi.timing_report()
     _capi.timing_enable(False)
     clk = clocks.stop()

@@ -121,6 +121,10 @@ struct Ctx {
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int side_stream(cudaStream_t* out);
+  // the stream for work forked from st: the side stream, or st itself while
+  // kernel-class timing is on (each class's event time then covers its own
+  // kernels only, not the ones of the other stream running beside them)
+  int fork_stream(cudaStream_t st, cudaStream_t* out);
   // galaxies of the last exh_hod_populate (B_HODG)
   int64_t hod_ng = -1;
   int hod_vel = 0;

@@ -87,6 +87,12 @@ int Ctx::side_stream(cudaStream_t* out) {
   return EXH_OK;
 }
 
+int Ctx::fork_stream(cudaStream_t st, cudaStream_t* out) {
+  EXH_TRY(side_stream(out));
+  if (timing_on()) *out = st;
+  return EXH_OK;
+}
+
 int Ctx::get_plan(int nx, int ny, int nz, FFTPlan3D** out) {
   auto key = std::make_tuple(nx, ny, nz);
   auto it = plans.find(key);

@@ -100,6 +100,75 @@ k_fft4_strided(Src src, Dst dst, const float2* __restrict__ tw, float sgn, int i
   }
 }
 
+// Strided pass of length 512 = 8 x 8 x 8.  The two-factor split 32 x 16
+// would hold a 32-point DFT per thread (beyond the register budget at full
+// occupancy: it spills) and leave half the threads idle in its first step;
+// here 64 threads per column each run three 8-point DFTs:
+//   A: j = q + 64 j1 (q < 64): DFT over j1 -> k1, times W_512^(q k1);
+//   B: for each k1, q = r + 8 s: DFT over s -> k2a, times W_64^(r k2a);
+//   C: for each (k1, k2a): DFT over r -> k2b; output k1 + 8 k2a + 64 k2b,
+// with two shared-memory exchanges.  Positions carry one float2 of padding
+// per 8, so the four positions a warp touches at once in every exchange
+// alternate between the two bank halves.
+constexpr int F512_W = 8;                   // columns per tile: 64 B row segments
+constexpr int F512_T = 64 * F512_W;
+__device__ __forceinline__ int f512_at(int p, int c) { return (p + (p >> 3)) * F512_W + c; }
+
+// The three stages for column c of a tile, thread q < 64 of that column;
+// ld(j) returns element j of the column.  On return v[k2b] holds output
+// k1 + 8 k2a + 64 k2b with k1 = q >> 3, k2a = q & 7; sm (f512_at layout,
+// (512 + 64) F512_W float2) may be written again after a barrier.
+template <class Load>
+__device__ __forceinline__ void f512_run(Load ld, float2* sm, const float2* __restrict__ tw, float sgn, int c,
+                                         int q, float2 (&v)[8]) {
+#pragma unroll
+  for (int j1 = 0; j1 < 8; j1++) v[j1] = ld(q + 64 * j1);
+  dft<8>(v, sgn);
+#pragma unroll
+  for (int k1 = 0; k1 < 8; k1++) {
+    float2 x = v[k1];
+    if (k1 != 0 && q != 0) x = cmul(x, tw_get(tw, q * k1, sgn));
+    sm[f512_at(k1 * 64 + q, c)] = x;
+  }
+  __syncthreads();
+  {
+    const int k1 = q >> 3, r = q & 7;
+#pragma unroll
+    for (int s = 0; s < 8; s++) v[s] = sm[f512_at(k1 * 64 + r + 8 * s, c)];
+    __syncthreads();
+    dft<8>(v, sgn);
+#pragma unroll
+    for (int k2a = 0; k2a < 8; k2a++) {
+      float2 x = v[k2a];
+      if (k2a != 0 && r != 0) x = cmul(x, tw_get(tw, 8 * r * k2a, sgn));
+      sm[f512_at(k1 * 64 + 8 * k2a + r, c)] = x;
+    }
+  }
+  __syncthreads();
+  {
+    const int k1 = q >> 3, k2a = q & 7;
+#pragma unroll
+    for (int r = 0; r < 8; r++) v[r] = sm[f512_at(k1 * 64 + 8 * k2a + r, c)];
+    dft<8>(v, sgn);
+  }
+}
+
+template <class Src, class Dst>
+__global__ void __launch_bounds__(F512_T, 3)
+k_fft8_strided512(Src src, Dst dst, const float2* __restrict__ tw, float sgn, int inner) {
+  __shared__ float2 sm[(512 + 64) * F512_W];
+  const int o = blockIdx.y, i0 = blockIdx.x * F512_W;
+  const int nb = min(F512_W, inner - i0);
+  const int c = threadIdx.x % F512_W, q = threadIdx.x / F512_W;
+  float2 v[8];
+  f512_run([&](int j) { return (c < nb) ? src(o, j, i0 + c) : make_float2(0.f, 0.f); }, sm, tw, sgn, c, q, v);
+  if (c < nb) {
+    const int k1 = q >> 3, k2a = q & 7;
+#pragma unroll
+    for (int k2b = 0; k2b < 8; k2b++) dst(o, k1 + 8 * k2a + 64 * k2b, i0 + c, v[k2b]);
+  }
+}
+
 // Row stride (float2) of the row kernels' shared memory: room for the
 // padded intermediate of fs_rows_smem, and == 8 (mod 16) so that the 4 or 2
 // rows a warp touches at once fall on disjoint bank pairs.
@@ -237,10 +306,19 @@ inline int fs_split(int n) {
 
 #define EXH_FS_CASES(X) \
   X(4, 4) X(8, 3) X(8, 4) X(8, 6) X(8, 8) X(8, 12) X(16, 8) X(16, 12) X(16, 16) X(32, 16)
+// strided passes: length 512 runs k_fft8_strided512 instead
+#define EXH_FS_STRIDED_CASES(X) \
+  X(4, 4) X(8, 3) X(8, 4) X(8, 6) X(8, 8) X(8, 12) X(16, 8) X(16, 12) X(16, 16)
 
 template <class Src, class Dst>
 inline bool launch_fs_strided(Src src, Dst dst, int n, const float2* tw, float sgn, int outer, int inner,
                               cudaStream_t st, cudaError_t* err) {
+  if (n == 512) {
+    dim3 grid(exh_div_up(inner, F512_W), outer);
+    k_fft8_strided512<Src, Dst><<<grid, F512_T, 0, st>>>(src, dst, tw, sgn, inner);
+    *err = cudaGetLastError();
+    return true;
+  }
   switch (fs_split(n)) {
 #define X(a, b)                                                                     \
   case a * 1000 + b: {                                                              \
@@ -249,7 +327,7 @@ inline bool launch_fs_strided(Src src, Dst dst, int n, const float2* tw, float s
     *err = cudaGetLastError();                                                      \
     return true;                                                                    \
   }
-    EXH_FS_CASES(X)
+    EXH_FS_STRIDED_CASES(X)
 #undef X
     default: return false;
   }

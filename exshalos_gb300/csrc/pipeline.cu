@@ -230,7 +230,7 @@ int exh_halos_box_from_pk(exh_ctx* ctx, const float* k, const float* P, int Nk, 
   // (whose sort and growth are latency-bound and leave most SMs idle); the
   // halo sums wait for it.  The two share no buffer.
   cudaStream_t side;
-  EXH_TRY(c.side_stream(&side));
+  EXH_TRY(c.fork_stream(st, &side));
   FieldModes modes = make_modes(b, A_dev, prm->fixed, prm->phase);
   EXH_TRY(c.buf[B_S].ensure(sizeof(float) * 3 * ng));
   EXH_TRY(c.buf[B_PHI1].ensure(sizeof(float) * ng));
@@ -363,7 +363,7 @@ int exh_halos_box_from_grid(exh_ctx* ctx, const float* delta, int ndx, int ndy, 
       EXH_TRY(c.buf[B_PHI2].ensure(sizeof(float) * ng));
       phi2 = c.buf[B_PHI2].as<float>();
     }
-    EXH_TRY(c.side_stream(&side));
+    EXH_TRY(c.fork_stream(st, &side));
     EXH_CUDA_TRY(cudaEventRecord(c.ev_fork, st));
     EXH_CUDA_TRY(cudaStreamWaitEvent(side, c.ev_fork, 0));
     EXH_TRY(lpt_run_grid(c, b, d, prm->k_smooth, prm->DO_2LPT != 0, S, V, phi1, phi2, side));

@@ -105,6 +105,19 @@ int cic_assign(Ctx& c, const float* pos_dev, int64_t np, int nd, float L, float*
 // ------------------------------------------------------------------ P(k)
 __device__ __forceinline__ float sinc_f(float x) { return x != 0.f ? sinf(x) / x : 1.f; }
 
+// Compensated (Neumaier) float sum of a run of same-bin modes; the run's
+// total goes to the double histogram as hi + lo.  Error of a run: about
+// 2^-24 of its total, whatever its length.
+struct RunSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float t = __fadd_rn(s, x);
+    c = __fadd_rn(c, fabsf(s) >= fabsf(x) ? __fadd_rn(__fsub_rn(s, t), x) : __fadd_rn(__fsub_rn(x, t), s));
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
 // Binning of one transformed tile res[i * W + b] (x index i < n, column
 // b < nb of the tile starting at inner index i0) into the block's shared
 // histograms.
@@ -116,7 +129,7 @@ __device__ __forceinline__ void bin_tile(const float2* res, int W, int n, int nb
   // touches the shared histogram once per run
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     int cur = -1;
-    double aP = 0.0, aK = 0.0;
+    RunSum aP, aK;
     unsigned aN = 0u;
     for (int bb = 0; bb < nb; bb++) {
       const int b = (bb + i) % nb;          // staggered start: rows of a warp hit different banks
@@ -138,25 +151,31 @@ __device__ __forceinline__ void bin_tile(const float2* res, int W, int n, int nb
         w = sinc_f(kx * bp.Lb * 0.5f) * sinc_f(ky * bp.Lb * 0.5f) * sinc_f(kz * bp.Lb * 0.5f);
         if (bp.window == 2) w = w * w;
       }
+      // the deconvolved mode and its power in float, as the reference forms
+      // them (gridk = out Normk / W, spectrum_h.c:161-162; re^2 + im^2,
+      // powermodule.c:66); only the sums are wider
       const float2 v = res[i * W + b];
-      const double s = (double)bp.Normk / (double)w;
-      const double re = (double)v.x * s, im = (double)v.y * s;
+      const float re = __fdiv_rn(__fmul_rn(v.x, bp.Normk), w);
+      const float im = __fdiv_rn(__fmul_rn(v.y, bp.Normk), w);
+      const float pw = __fadd_rn(__fmul_rn(re, re), __fmul_rn(im, im));
       if (bin != cur) {
         if (cur >= 0) {
-          atomicAdd(&hP[cur], aP);
-          atomicAdd(&hK[cur], aK);
+          atomicAdd(&hP[cur], aP.value());
+          atomicAdd(&hK[cur], aK.value());
           atomicAdd(&hN[cur], aN);
         }
         cur = bin;
-        aP = 0.0; aK = 0.0; aN = 0u;
+        aP = RunSum();
+        aK = RunSum();
+        aN = 0u;
       }
-      aP += re * re + im * im;
-      aK += (double)kmod;
+      aP.add(pw);
+      aK.add(kmod);
       aN++;
     }
     if (cur >= 0) {
-      atomicAdd(&hP[cur], aP);
-      atomicAdd(&hK[cur], aK);
+      atomicAdd(&hP[cur], aP.value());
+      atomicAdd(&hK[cur], aK.value());
       atomicAdd(&hN[cur], aN);
     }
   }
@@ -248,13 +267,58 @@ k_fft4_x_bin(const float2* __restrict__ work, const float2* __restrict__ tw, int
   }
 }
 
-// launches k_fft4_x_bin for the lengths with a four-step split; returns the
-// block count through nblk (0: not covered)
+// Length 512: the three radix-8 stages of k_fft8_strided512, the results
+// back in shared memory in natural order for bin_tile.
+__global__ void __launch_bounds__(F512_T, 2)
+k_fft8_x_bin512(const float2* __restrict__ work, const float2* __restrict__ tw, int nd, int nc, BinParams bp,
+                double* __restrict__ partP, double* __restrict__ partK, unsigned int* __restrict__ partN) {
+  constexpr int W = F512_W, n = 512;
+  extern __shared__ float2 dsm[];
+  float2* sm = dsm;                                   // (n + 64) W float2
+  double* hP = reinterpret_cast<double*>(sm + (n + 64) * W);
+  double* hK = hP + bp.Nk;
+  unsigned int* hN = reinterpret_cast<unsigned int*>(hK + bp.Nk);
+  const int inner = nd * nc;
+  const int i0 = blockIdx.x * W;
+  const int nb = min(W, inner - i0);
+  const int c = threadIdx.x % W, q = threadIdx.x / W;
+  for (int b = threadIdx.x; b < bp.Nk; b += blockDim.x) { hP[b] = 0.0; hK[b] = 0.0; hN[b] = 0u; }
+  float2 v[8];
+  f512_run([&](int j) { return (c < nb) ? work[(size_t)j * inner + i0 + c] : make_float2(0.f, 0.f); }, sm, tw,
+           -1.f, c, q, v);
+  __syncthreads();
+  {
+    const int k1 = q >> 3, k2a = q & 7;
+#pragma unroll
+    for (int k2b = 0; k2b < 8; k2b++) sm[(k1 + 8 * k2a + 64 * k2b) * W + c] = v[k2b];
+  }
+  __syncthreads();
+  bin_tile(sm, W, n, nb, i0, nd, nc, bp, hP, hK, hN);
+  __syncthreads();
+  for (int b = threadIdx.x; b < bp.Nk; b += blockDim.x) {
+    partP[(size_t)blockIdx.x * bp.Nk + b] = hP[b];
+    partK[(size_t)blockIdx.x * bp.Nk + b] = hK[b];
+    partN[(size_t)blockIdx.x * bp.Nk + b] = hN[b];
+  }
+}
+
+// launches k_fft4_x_bin (k_fft8_x_bin512 for 512) for the lengths with a
+// four-step split; returns the block count through nblk (0: not covered)
 static cudaError_t launch_fs_x_bin(const float2* work, const float2* tw, int nd, int nc, const BinParams& bp,
                                    double* partP, double* partK, unsigned* partN, int nblk_cap, int* nblk,
                                    cudaStream_t st) {
   *nblk = 0;
   const int inner = nd * nc;
+  if (nd == 512) {
+    const int nb = (int)exh_div_up(inner, F512_W);
+    if (nb > nblk_cap) return cudaSuccess;
+    const size_t sm = sizeof(float2) * (512 + 64) * F512_W + (size_t)bp.Nk * (2 * sizeof(double) + sizeof(unsigned)) + 16;
+    cudaError_t e = set_smem(k_fft8_x_bin512, sm);
+    if (e != cudaSuccess) return e;
+    k_fft8_x_bin512<<<nb, F512_T, sm, st>>>(work, tw, nd, nc, bp, partP, partK, partN);
+    *nblk = nb;
+    return cudaGetLastError();
+  }
   switch (fs_split(nd)) {
 #define X(A_, B_)                                                                                        \
   case A_ * 1000 + B_: {                                                                                 \
@@ -268,7 +332,7 @@ static cudaError_t launch_fs_x_bin(const float2* work, const float2* tw, int nd,
     *nblk = nb;                                                                                          \
     return cudaGetLastError();                                                                           \
   }
-    EXH_FS_CASES(X)
+    EXH_FS_STRIDED_CASES(X)
 #undef X
     default: return cudaSuccess;
   }
