@@ -661,6 +661,52 @@ def run_box512(args, ws, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_fft512(args, local):
+    """Kernel workload: a 512^3 real-to-complex transform and its inverse,
+    device-resident (1.1 GB: the real grid and the half-complex modes), each
+    direction three passes (row pass, y pass, x pass).  Reports ms per
+    transform and per kernel class with algorithmic GB/s (each pass one read
+    of its input and one write of its output) against the HBM copy peak."""
+    import torch
+    torch.cuda.set_device(local)
+    from exshalos_gb300 import _capi
+    L_ = _capi.load()
+    ctx = _capi.context()
+    nd = 512
+    nc = nd // 2 + 1
+    g = torch.Generator(device="cuda").manual_seed(5)
+    x = torch.randn(nd ** 3, device="cuda", generator=g)
+    kx = torch.empty(nd * nd * nc * 2, device="cuda")
+
+    def step():
+        _capi.check(L_.exh_fft_r2c_3d(ctx, nd, nd, nd, _capi.ptr(x), _capi.ptr(kx), None))
+        _capi.check(L_.exh_fft_c2r_3d(ctx, nd, nd, nd, _capi.ptr(kx), _capi.ptr(x), None))
+        x.mul_(1.0 / nd ** 3)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    _capi.timing_enable(True)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(args.steps):
+        step()
+    ev1.record()
+    torch.cuda.synchronize()
+    rep = _capi.timing_report()
+    _capi.timing_enable(False)
+    peak, peak_kind = measured_peak()
+    classes = {}
+    for kk, (cms, cnl, cby) in rep.items():
+        if cnl and cms > 0:
+            gbs = cby / (cms / 1000.0) / 1e9 if cby > 0 else None
+            classes[kk] = {"ms_per_launch": round(cms / cnl, 4), "launches": cnl,
+                           "gbs": round(gbs, 1) if gbs else None, "frac": round(gbs / peak, 4) if gbs else None}
+    print(json.dumps({"workload": "fft_512: r2c + c2r of a 512^3 grid, device-resident",
+                      "ms_per_roundtrip": ev0.elapsed_time(ev1) / args.steps, "peak_gbs": peak,
+                      "peak_source": peak_kind, "kernel_classes": classes}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -670,15 +716,19 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-workload summary")
     ap.add_argument("--lanes", type=int, default=12, help="lanes of the batched runner")
-    ap.add_argument("--workload", default="box_256", choices=["box_256", "box_512", "galaxies_256"],
+    ap.add_argument("--workload", default="box_256", choices=["box_256", "box_512", "galaxies_256", "fft_512"],
                     help="box_256: the headline line; box_512: the large-box kernel-class report; "
-                         "galaxies_256: the galaxy-population summary alone")
+                         "galaxies_256: the galaxy-population summary alone; fft_512: a 512^3 FFT round trip "
+                         "per kernel class")
     args = ap.parse_args()
     ws, rank, local = dist_init()
     if args.impl == "reference":
         run_reference(args, ws, rank)
     elif args.workload == "box_512":
         run_box512(args, ws, rank, local)
+    elif args.workload == "fft_512":
+        if rank == 0:
+            run_fft512(args, local)
     elif args.workload == "galaxies_256":
         if rank == 0:
             os.environ["EXH_DEVICE"] = str(local)

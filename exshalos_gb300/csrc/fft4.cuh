@@ -118,11 +118,9 @@ __device__ __forceinline__ int f512_at(int p, int c) { return (p + (p >> 3)) * F
 // ld(j) returns element j of the column.  On return v[k2b] holds output
 // k1 + 8 k2a + 64 k2b with k1 = q >> 3, k2a = q & 7; sm (f512_at layout,
 // (512 + 64) F512_W float2) may be written again after a barrier.
-template <class Load>
-__device__ __forceinline__ void f512_run(Load ld, float2* sm, const float2* __restrict__ tw, float sgn, int c,
-                                         int q, float2 (&v)[8]) {
-#pragma unroll
-  for (int j1 = 0; j1 < 8; j1++) v[j1] = ld(q + 64 * j1);
+// f512_core: the same from v[j1] = element q + 64 j1 already loaded.
+__device__ __forceinline__ void f512_core(float2 (&v)[8], float2* sm, const float2* __restrict__ tw, float sgn,
+                                          int c, int q) {
   dft<8>(v, sgn);
 #pragma unroll
   for (int k1 = 0; k1 < 8; k1++) {
@@ -151,6 +149,14 @@ __device__ __forceinline__ void f512_run(Load ld, float2* sm, const float2* __re
     for (int r = 0; r < 8; r++) v[r] = sm[f512_at(k1 * 64 + 8 * k2a + r, c)];
     dft<8>(v, sgn);
   }
+}
+
+template <class Load>
+__device__ __forceinline__ void f512_run(Load ld, float2* sm, const float2* __restrict__ tw, float sgn, int c,
+                                         int q, float2 (&v)[8]) {
+#pragma unroll
+  for (int j1 = 0; j1 < 8; j1++) v[j1] = ld(q + 64 * j1);
+  f512_core(v, sm, tw, sgn, c, q);
 }
 
 template <class Src, class Dst>

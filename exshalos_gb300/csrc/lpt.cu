@@ -147,7 +147,117 @@ k_brick_source(const float* __restrict__ S, int n0, int n1, int n2, float inv60l
   }
 }
 
+// Poisson factor of mode (e, col) of the x pass: Normk / (-k^2), zero at
+// k = 0 and above k_smooth (lpt.c:140-150)
+__device__ __forceinline__ float2 poisson_mode(float2 v, const KGrid& g, int e, int col, int nc, float normk) {
+  float kmod;
+  const float s = g.k2(e, col / nc, col % nc, kmod);
+  if (s == 0.f || kmod > g.k_smooth) return make_float2(0.f, 0.f);
+  const float f = -(kmod * kmod);
+  return make_float2(v.x / f * normk, v.y / f * normk);
+}
+
+// x pass of the 2LPT Poisson solve as register four-step FFTs (fft4.cuh):
+// forward, x Normk/(-k^2), inverse, on a tile of W columns; the modes go
+// back to shared memory in natural order between the two transforms.
+template <int N1, int N2>
+__global__ void __launch_bounds__(FS_THREADS, 2)
+k_fft4_x_poisson(float2* __restrict__ work, const float2* __restrict__ tw, int inner, KGrid g, float normk) {
+  using S = FsShape<N1, N2>;
+  constexpr int W = S::W, n = S::n;
+  __shared__ float2 sm[n * W];
+  const int i0 = blockIdx.x * W;
+  const int nb = min(W, inner - i0);
+  const int c = threadIdx.x % W, jj = threadIdx.x / W;
+  const int nc = g.n2 / 2 + 1;
+  const bool live = c < nb;
+  float2 v[N1];
+  float2 u[N2];
+  if (jj < N2) {
+#pragma unroll
+    for (int j1 = 0; j1 < N1; j1++)
+      v[j1] = live ? work[(size_t)(jj + N2 * j1) * inner + i0 + c] : make_float2(0.f, 0.f);
+    RDft<N1>::run(v, -1.f, [tw](int m) { return __ldg(&tw[m * N2]); });
+#pragma unroll
+    for (int k1 = 0; k1 < N1; k1++) {
+      float2 x = v[k1];
+      if (k1 != 0 && jj != 0) x = cmul(x, tw_get(tw, jj * k1, -1.f));
+      sm[(k1 * N2 + jj) * W + c] = x;
+    }
+  }
+  __syncthreads();
+  if (jj < N1) {
+#pragma unroll
+    for (int j2 = 0; j2 < N2; j2++) u[j2] = sm[(jj * N2 + j2) * W + c];
+    RDft<N2>::run(u, -1.f, [tw](int m) { return __ldg(&tw[m * N1]); });
+#pragma unroll
+    for (int k2 = 0; k2 < N2; k2++)
+      u[k2] = live ? poisson_mode(u[k2], g, jj + N1 * k2, i0 + c, nc, normk) : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  if (jj < N1) {
+#pragma unroll
+    for (int k2 = 0; k2 < N2; k2++) sm[(jj + N1 * k2) * W + c] = u[k2];
+  }
+  __syncthreads();
+  if (jj < N2) {
+#pragma unroll
+    for (int j1 = 0; j1 < N1; j1++) v[j1] = sm[(jj + N2 * j1) * W + c];
+  }
+  __syncthreads();
+  if (jj < N2) {
+    RDft<N1>::run(v, 1.f, [tw](int m) { return __ldg(&tw[m * N2]); });
+#pragma unroll
+    for (int k1 = 0; k1 < N1; k1++) {
+      float2 x = v[k1];
+      if (k1 != 0 && jj != 0) x = cmul(x, tw_get(tw, jj * k1, 1.f));
+      sm[(k1 * N2 + jj) * W + c] = x;
+    }
+  }
+  __syncthreads();
+  if (jj < N1) {
+#pragma unroll
+    for (int j2 = 0; j2 < N2; j2++) u[j2] = sm[(jj * N2 + j2) * W + c];
+    RDft<N2>::run(u, 1.f, [tw](int m) { return __ldg(&tw[m * N1]); });
+    if (live) {
+#pragma unroll
+      for (int k2 = 0; k2 < N2; k2++) work[(size_t)(jj + N1 * k2) * inner + i0 + c] = u[k2];
+    }
+  }
+}
+
+// The same for length 512 on the three radix-8 stages of k_fft8_strided512.
+__global__ void __launch_bounds__(F512_T, 2)
+k_fft8_x_poisson512(float2* __restrict__ work, const float2* __restrict__ tw, int inner, KGrid g, float normk) {
+  __shared__ float2 sm[(512 + 64) * F512_W];
+  const int i0 = blockIdx.x * F512_W;
+  const int nb = min(F512_W, inner - i0);
+  const int c = threadIdx.x % F512_W, q = threadIdx.x / F512_W;
+  const int nc = g.n2 / 2 + 1;
+  const bool live = c < nb;
+  const int k1 = q >> 3, k2a = q & 7;
+  float2 v[8];
+  f512_run([&](int j) { return live ? work[(size_t)j * inner + i0 + c] : make_float2(0.f, 0.f); }, sm, tw, -1.f,
+           c, q, v);
+#pragma unroll
+  for (int k2b = 0; k2b < 8; k2b++)
+    v[k2b] = live ? poisson_mode(v[k2b], g, k1 + 8 * k2a + 64 * k2b, i0 + c, nc, normk) : make_float2(0.f, 0.f);
+  __syncthreads();
+#pragma unroll
+  for (int k2b = 0; k2b < 8; k2b++) sm[f512_at(k1 + 8 * k2a + 64 * k2b, c)] = v[k2b];
+  __syncthreads();
+#pragma unroll
+  for (int j1 = 0; j1 < 8; j1++) v[j1] = sm[f512_at(q + 64 * j1, c)];
+  __syncthreads();
+  f512_core(v, sm, tw, 1.f, c, q);
+  if (live) {
+#pragma unroll
+    for (int k2b = 0; k2b < 8; k2b++) work[(size_t)(k1 + 8 * k2a + 64 * k2b) * inner + i0 + c] = v[k2b];
+  }
+}
+
 // x pass of the 2LPT Poisson solve: forward, x Normk/(-k^2), inverse
+// (shared-memory Stockham, for lengths without a register split)
 __global__ void __launch_bounds__(FFT_THREADS)
 k_fft_x_poisson(float2* __restrict__ work, RadixPlan pl, const float2* __restrict__ tw, int inner, KGrid g,
                 float normk) {
@@ -168,15 +278,7 @@ k_fft_x_poisson(float2* __restrict__ work, RadixPlan pl, const float2* __restric
     const int e = t / FFT_W, b = t % FFT_W;
     const int col = i0 + b;
     float2 v = res[e * FFT_W + b];
-    if (b < nb) {
-      float kmod;
-      const float s = g.k2(e, col / nc, col % nc, kmod);
-      if (s == 0.f || kmod > g.k_smooth) v = make_float2(0.f, 0.f);
-      else {
-        const float f = -(kmod * kmod);
-        v = make_float2(v.x / f * normk, v.y / f * normk);
-      }
-    }
+    if (b < nb) v = poisson_mode(v, g, e, col, nc, normk);
     res[e * FFT_W + b] = v;
   }
   __syncthreads();
@@ -398,11 +500,26 @@ static int lpt_from_phi1(Ctx& c, const BoxParams& b, float k_smooth, bool do2, f
   EXH_CUDA_TRY(launch_strided(CplxLoad{work, b.nd[1], p->nc}, CplxStore{work, b.nd[1], p->nc}, p->py, p->twy, -1.f,
                               b.nd[0], p->nc, st));
   const int inner = b.nd[1] * p->nc;
-  const size_t sm = smem_strided(b.nd[0]);
-  EXH_CUDA_TRY(set_smem(k_fft_x_poisson, sm));
   {
     KTimer kt(KC_FFT_STRIDED, st, 16.0 * b.nd[0] * inner);
-    k_fft_x_poisson<<<exh_div_up(inner, FFT_W), FFT_THREADS, sm, st>>>(work, p->px, p->twx, inner, g, b.Normk);
+    if (b.nd[0] == 512) {
+      k_fft8_x_poisson512<<<exh_div_up(inner, F512_W), F512_T, 0, st>>>(work, p->twx, inner, g, b.Normk);
+    } else {
+      switch (fs_split(b.nd[0])) {
+#define X(A_, B_)                                                                                       \
+  case A_ * 1000 + B_:                                                                                  \
+    k_fft4_x_poisson<A_, B_><<<exh_div_up(inner, FsShape<A_, B_>::W), FS_THREADS, 0, st>>>(work, p->twx, inner, g, \
+                                                                                       b.Normk);         \
+    break;
+        EXH_FS_STRIDED_CASES(X)
+#undef X
+        default: {
+          const size_t sm = smem_strided(b.nd[0]);
+          EXH_CUDA_TRY(set_smem(k_fft_x_poisson, sm));
+          k_fft_x_poisson<<<exh_div_up(inner, FFT_W), FFT_THREADS, sm, st>>>(work, p->px, p->twx, inner, g, b.Normk);
+        }
+      }
+    }
     count_launch(1);
     EXH_CUDA_TRY(cudaGetLastError());
   }
