@@ -32,6 +32,22 @@ __host__ __device__ __forceinline__ int exh_wrap(int i, int j, int nd) {
   return r;
 }
 
+// (i, j, k) of the row-major cell index of an n0 x n1 x n2 grid of ng cells;
+// 32-bit divisions while the index fits
+__device__ __forceinline__ void cell_ijk(size_t cell, size_t ng, int n1, int n2, int* i, int* j, int* k) {
+  if (ng <= 0xffffffffull) {
+    const unsigned c32 = (unsigned)cell, r = c32 / (unsigned)n2;
+    *k = (int)(c32 - r * (unsigned)n2);
+    *j = (int)(r % (unsigned)n1);
+    *i = (int)(r / (unsigned)n1);
+  } else {
+    *k = (int)(cell % n2);
+    const size_t r = cell / n2;
+    *j = (int)(r % n1);
+    *i = (int)(r / n1);
+  }
+}
+
 __host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }

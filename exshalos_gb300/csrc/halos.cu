@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "halos.cuh"
+#include "intdiv.cuh"
 #include "scan.cuh"
 #include "taus.cuh"
 
@@ -118,61 +119,109 @@ __device__ __forceinline__ void unpack_off(int p, int& i, int& j, int& k) {
 }
 
 // ------------------------------------------------------------------ peaks
-__device__ __forceinline__ bool is_peak(const float* __restrict__ d, int i, int j, int k, int n0, int n1, int n2,
-                                        float den) {
+// Strict maximum against the six periodic neighbours (find_halos.c:108-156).
+// The seven values of a cell are loaded before any comparison, so the loads
+// are in flight together (a short-circuit chain would issue them one by one).
+__device__ __forceinline__ void peak_load(const float* __restrict__ d, size_t cell, size_t ng, int n0, int n1,
+                                          int n2, float (&a)[7]) {
+  int i, j, k;
+  cell_ijk(cell, ng, n1, n2, &i, &j, &k);
   const size_t s1 = n2, s0 = (size_t)n1 * n2;
   const size_t c = (size_t)i * s0 + (size_t)j * s1;
-  return den > d[(size_t)exh_wrap(i, 1, n0) * s0 + (size_t)j * s1 + k] &&
-         den > d[(size_t)exh_wrap(i, -1, n0) * s0 + (size_t)j * s1 + k] &&
-         den > d[(size_t)i * s0 + (size_t)exh_wrap(j, 1, n1) * s1 + k] &&
-         den > d[(size_t)i * s0 + (size_t)exh_wrap(j, -1, n1) * s1 + k] &&
-         den > d[c + exh_wrap(k, 1, n2)] && den > d[c + exh_wrap(k, -1, n2)];
+  a[0] = d[cell];
+  a[1] = d[(size_t)exh_wrap(i, 1, n0) * s0 + (size_t)j * s1 + k];
+  a[2] = d[(size_t)exh_wrap(i, -1, n0) * s0 + (size_t)j * s1 + k];
+  a[3] = d[(size_t)i * s0 + (size_t)exh_wrap(j, 1, n1) * s1 + k];
+  a[4] = d[(size_t)i * s0 + (size_t)exh_wrap(j, -1, n1) * s1 + k];
+  a[5] = d[c + exh_wrap(k, 1, n2)];
+  a[6] = d[c + exh_wrap(k, -1, n2)];
+}
+// The same for grids of fewer than 2^32 cells: (i, j, k) by two fast
+// divisions and the six neighbours as 32-bit index offsets with the
+// periodic wrap applied by a branch per axis (s0 = n1 n2, ng32 = n0 s0).
+struct PeakGeom {
+  FastDiv fd1, fd2;
+  uint32_t n0, n1, n2, s0, ng32;
+};
+__device__ __forceinline__ void peak_load32(const float* __restrict__ d, uint32_t c, const PeakGeom& q,
+                                            float (&a)[7]) {
+  const uint32_t r = fd_div(c, q.fd2), k = c - r * q.n2;
+  const uint32_t i = fd_div(r, q.fd1), j = r - i * q.n1;
+  a[0] = d[c];
+  a[1] = d[i + 1 == q.n0 ? c - (q.ng32 - q.s0) : c + q.s0];
+  a[2] = d[i == 0 ? c + (q.ng32 - q.s0) : c - q.s0];
+  a[3] = d[j + 1 == q.n1 ? c - (q.s0 - q.n2) : c + q.n2];
+  a[4] = d[j == 0 ? c + (q.s0 - q.n2) : c - q.n2];
+  a[5] = d[k + 1 == q.n2 ? c - (q.n2 - 1) : c + 1];
+  a[6] = d[k == 0 ? c + (q.n2 - 1) : c - 1];
+}
+__device__ __forceinline__ bool peak_test(const float (&a)[7]) {
+  return (a[0] > a[1]) & (a[0] > a[2]) & (a[0] > a[3]) & (a[0] > a[4]) & (a[0] > a[5]) & (a[0] > a[6]);
 }
 
-constexpr int PK_T = 256;
+constexpr int PK_T = 256;          // cells per group: one count, eight mask words
+constexpr int PK_U = 4;            // groups a block takes at once (their loads in flight together)
+constexpr int PK_BLOCKS_PER_SM = 8;
+constexpr int PK_MASK_BLOCKS_PER_SM = 5;   // resident blocks of k_peak_mask (its launch bound)
 
-__global__ void k_peak_mask(const float* __restrict__ d, int n0, int n1, int n2, size_t ng,
-                            unsigned* __restrict__ mask, unsigned* __restrict__ cnt) {
-  const size_t cell = (size_t)blockIdx.x * PK_T + threadIdx.x;
-  bool pk = false;
-  if (cell < ng) {
-    const int k = (int)(cell % n2);
-    const size_t r = cell / n2;
-    const int j = (int)(r % n1), i = (int)(r / n1);
-    pk = is_peak(d, i, j, k, n0, n1, n2, d[cell]);
-  }
-  const unsigned m = __ballot_sync(0xffffffffu, pk);
-  __shared__ unsigned wc[PK_T / 32];
-  if ((threadIdx.x & 31) == 0) {
-    mask[cell >> 5] = m;
-    wc[threadIdx.x >> 5] = __popc(m);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned s = 0;
-    for (int w = 0; w < PK_T / 32; w++) s += wc[w];
-    cnt[blockIdx.x] = s;
-  }
-}
-
-__global__ void k_peak_write(const float* __restrict__ d, size_t ng, const unsigned* __restrict__ mask,
-                             const unsigned* __restrict__ off, float* __restrict__ key, unsigned* __restrict__ id) {
-  const size_t cell = (size_t)blockIdx.x * PK_T + threadIdx.x;
-  __shared__ unsigned wo[PK_T / 32];
-  const unsigned m = mask[cell >> 5];
-  if (threadIdx.x == 0) {
-    unsigned s = 0;
-    for (int w = 0; w < PK_T / 32; w++) {
-      wo[w] = s;
-      s += __popc(mask[((size_t)blockIdx.x * PK_T >> 5) + w]);
+// one bit per cell (mask word w: cells 32 w .. 32 w + 31) and the peak count
+// of every group of PK_T cells; blocks stride over runs of PK_U groups
+__global__ void __launch_bounds__(PK_T, PK_MASK_BLOCKS_PER_SM)
+k_peak_mask(const float* __restrict__ d, int n0, int n1, int n2, size_t ng, unsigned ngroups, PeakGeom q,
+            unsigned* __restrict__ mask, unsigned* __restrict__ cnt) {
+  const bool small = ng <= 0xffffffffull;
+  __shared__ unsigned wc[PK_U][PK_T / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (unsigned g0 = blockIdx.x * PK_U; g0 < ngroups; g0 += gridDim.x * PK_U) {
+    float a[PK_U][7];
+    bool live[PK_U];
+#pragma unroll
+    for (int u = 0; u < PK_U; u++) {
+      const size_t cell = (size_t)(g0 + u) * PK_T + threadIdx.x;
+      live[u] = g0 + u < ngroups && cell < ng;
+      if (live[u]) {
+        if (small) peak_load32(d, (uint32_t)cell, q, a[u]);
+        else peak_load(d, cell, ng, n0, n1, n2, a[u]);
+      }
     }
+#pragma unroll
+    for (int u = 0; u < PK_U; u++) {
+      const unsigned m = __ballot_sync(0xffffffffu, live[u] && peak_test(a[u]));
+      if (lane == 0 && g0 + u < ngroups) {
+        mask[((size_t)(g0 + u) * PK_T >> 5) + w] = m;
+        wc[u][w] = __popc(m);
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < PK_U && g0 + threadIdx.x < ngroups) {
+      unsigned s = 0;
+      for (int q = 0; q < PK_T / 32; q++) s += wc[threadIdx.x][q];
+      cnt[g0 + threadIdx.x] = s;
+    }
+    __syncthreads();
   }
-  __syncthreads();
-  const int lane = threadIdx.x & 31;
-  if (cell < ng && ((m >> lane) & 1u)) {
-    const unsigned pos = off[blockIdx.x] + wo[threadIdx.x >> 5] + __popc(m & ((1u << lane) - 1u));
-    key[pos] = d[cell];
-    id[pos] = (unsigned)cell;
+}
+
+// peaks in row-major cell order: group offset + the peaks of the words
+// before in the group + the lanes before in the word
+__global__ void __launch_bounds__(PK_T)
+k_peak_write(const float* __restrict__ d, size_t ng, unsigned ngroups, const unsigned* __restrict__ mask,
+             const unsigned* __restrict__ off, float* __restrict__ key, unsigned* __restrict__ id) {
+  __shared__ unsigned wo[PK_T / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (unsigned g = blockIdx.x; g < ngroups; g += gridDim.x) {
+    const size_t cell = (size_t)g * PK_T + threadIdx.x;
+    const unsigned m = mask[cell >> 5];
+    if (lane == 0) wo[w] = __popc(m);
+    __syncthreads();
+    unsigned before = 0;
+    for (int q = 0; q < w; q++) before += wo[q];
+    if (cell < ng && ((m >> lane) & 1u)) {
+      const unsigned pos = off[g] + before + __popc(m & ((1u << lane) - 1u));
+      key[pos] = d[cell];
+      id[pos] = (unsigned)cell;
+    }
+    __syncthreads();
   }
 }
 
@@ -187,8 +236,16 @@ int find_peaks(Ctx& c, const float* delta, const BoxParams& b, HaloDev* h, cudaS
   unsigned* off = cnt + nb;
   unsigned* sums = off + nb;
   unsigned* total = sums + nb + 32;
+  const unsigned grid = std::min<unsigned>(nb, EXH_NUM_SMS * PK_BLOCKS_PER_SM);
+  const unsigned grid_m = std::min<unsigned>(exh_div_up(nb, PK_U), EXH_NUM_SMS * PK_MASK_BLOCKS_PER_SM);
   { KTimer kt(KC_PEAKS, st, 4.0 * ng + ng / 8.0);
-  k_peak_mask<<<nb, PK_T, 0, st>>>(delta, b.nd[0], b.nd[1], b.nd[2], ng, mask, cnt); }
+  PeakGeom q;
+  q.fd1 = make_fastdiv((uint32_t)b.nd[1]);
+  q.fd2 = make_fastdiv((uint32_t)b.nd[2]);
+  q.n0 = b.nd[0]; q.n1 = b.nd[1]; q.n2 = b.nd[2];
+  q.s0 = q.n1 * q.n2;
+  q.ng32 = (uint32_t)ng;            // used only while ng < 2^32
+  k_peak_mask<<<grid_m, PK_T, 0, st>>>(delta, b.nd[0], b.nd[1], b.nd[2], ng, nb, q, mask, cnt); }
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   EXH_CUDA_TRY(exclusive_scan<unsigned>(cnt, off, nb, sums, total, st));
@@ -201,7 +258,7 @@ int find_peaks(Ctx& c, const float* delta, const BoxParams& b, HaloDev* h, cudaS
   h->key = c.buf[B_PEAKS].as<float>();
   h->id = reinterpret_cast<unsigned*>(h->key + cap);
   { KTimer kt(KC_PEAKS, st, ng / 8.0 + 12.0 * np);
-  k_peak_write<<<nb, PK_T, 0, st>>>(delta, ng, mask, off, h->key, h->id); }
+  k_peak_write<<<grid, PK_T, 0, st>>>(delta, ng, nb, mask, off, h->key, h->id); }
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   return EXH_OK;

@@ -66,14 +66,19 @@ __device__ __forceinline__ float d6f(float p1, float p2, float p3, float m1, flo
   return (p3 - m3) - 9.f * (p2 - m2) + 45.f * (p1 - m1);
 }
 
-// load a (ex) x (ey) x (ez) tile whose origin is (x0 - hx, y0 - hy, z0 - hz)
-__device__ __forceinline__ void load_tile(const float* __restrict__ f, float* t, int ex, int ey, int ez, int x0, int y0,
-                                          int z0, int hx, int hy, int hz, int n0, int n1, int n2) {
-  const int tot = ex * ey * ez, tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
+// load an EX x EY x EZ tile whose origin is (x0 - hx, y0 - hy, z0 - hz);
+// the extents are compile-time, so the index split costs no division
+template <int EX, int EY, int EZ>
+__device__ __forceinline__ void load_tile(const float* __restrict__ f, float* t, int x0, int y0, int z0, int hx,
+                                          int hy, int hz, int n0, int n1, int n2) {
+  constexpr int tot = EX * EY * EZ;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
+  const bool small = (size_t)n0 * n1 * n2 <= 0xffffffffull;     // 32-bit cell indexes
   for (int q = tid; q < tot; q += nt) {
-    const int dz = q % ez, r = q / ez, dy = r % ey, dx = r / ey;
+    const int dz = q % EZ, r = q / EZ, dy = r % EY, dx = r / EY;
     const int gx = exh_wrap(x0 - hx, dx, n0), gy = exh_wrap(y0 - hy, dy, n1), gz = exh_wrap(z0 - hz, dz, n2);
-    t[q] = f[((size_t)gx * n1 + gy) * n2 + gz];
+    t[q] = small ? f[((uint32_t)gx * (uint32_t)n1 + (uint32_t)gy) * (uint32_t)n2 + (uint32_t)gz]
+                 : f[((size_t)gx * n1 + gy) * n2 + gz];
   }
 }
 
@@ -85,7 +90,7 @@ k_brick_grad(const float* __restrict__ phi, int n0, int n1, int n2, float fac, f
   extern __shared__ float tile[];
   constexpr int EY = BY + 2 * H, EZ = BZ + 2 * H;
   const int z0 = blockIdx.x * BZ, y0 = blockIdx.y * BY, x0 = blockIdx.z * GX;
-  load_tile(phi, tile, GX + 2 * H, EY, EZ, x0, y0, z0, H, H, H, n0, n1, n2);
+  load_tile<GX + 2 * H, EY, EZ>(phi, tile, x0, y0, z0, H, H, H, n0, n1, n2);
   __syncthreads();
   const int tz = threadIdx.x, ty = threadIdx.y;
   const int gz = z0 + tz, gy = y0 + ty;
@@ -109,6 +114,28 @@ k_brick_grad(const float* __restrict__ phi, int n0, int n1, int n2, float fac, f
   }
 }
 
+// diag - x^2 - y^2 - z^2, which the reference forms in double from float
+// operands (pow(., 2.0), lpt.c:134): here in FP32 without the FP64 pipe.
+// Each square is split exactly into hi + lo by an FMA, the running value is
+// kept as s + c with s updated by an error-free TwoSum (Knuth), and the sum
+// is rounded once at the end: the error before that rounding is about 2^-47
+// of the largest term.
+__device__ __forceinline__ float source_combine(float diag, float x, float y, float z) {
+  float s = diag, c = 0.f;
+  const float p[3] = {x, y, z};
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const float hi = __fmul_rn(p[a], p[a]);
+    const float lo = __fmaf_rn(p[a], p[a], -hi);          // p^2 = hi + lo exactly
+    const float t = __fsub_rn(s, hi);
+    const float bb = __fsub_rn(t, s);                      // TwoSum of s and -hi
+    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(-hi, bb));
+    s = t;
+    c = __fsub_rn(__fadd_rn(c, e), lo);
+  }
+  return __fadd_rn(s, c);
+}
+
 // second-order source (lpt.c:116-134) from the first-order displacement
 __global__ void __launch_bounds__(256)
 k_brick_source(const float* __restrict__ S, int n0, int n1, int n2, float inv60lc, float* __restrict__ src) {
@@ -119,9 +146,9 @@ k_brick_source(const float* __restrict__ S, int n0, int n1, int n2, float inv60l
   float* tz_ = ty_ + SX * EY * EZ;                  // Sz: halo in z
   const size_t ng = (size_t)n0 * n1 * n2;
   const int z0 = blockIdx.x * BZ, y0 = blockIdx.y * BY, x0 = blockIdx.z * SX;
-  load_tile(S, tx, SX + 2 * H, EY, EZ, x0, y0, z0, H, H, H, n0, n1, n2);
-  load_tile(S + ng, ty_, SX, EY, EZ, x0, y0, z0, 0, H, H, n0, n1, n2);
-  load_tile(S + 2 * ng, tz_, SX, BY, EZ, x0, y0, z0, 0, 0, H, n0, n1, n2);
+  load_tile<SX + 2 * H, EY, EZ>(S, tx, x0, y0, z0, H, H, H, n0, n1, n2);
+  load_tile<SX, EY, EZ>(S + ng, ty_, x0, y0, z0, 0, H, H, n0, n1, n2);
+  load_tile<SX, BY, EZ>(S + 2 * ng, tz_, x0, y0, z0, 0, 0, H, n0, n1, n2);
   __syncthreads();
   const int tzz = threadIdx.x, tyy = threadIdx.y;
   const int gz = z0 + tzz, gy = y0 + tyy;
@@ -142,8 +169,7 @@ k_brick_source(const float* __restrict__ S, int n0, int n1, int n2, float inv60l
 #undef AY
 #undef AZ
     const float diag = pxx * pyy + pxx * pzz + pyy * pzz;
-    src[((size_t)(x0 + xx) * n1 + gy) * n2 + gz] =
-        (float)((double)diag - (double)pxy * pxy - (double)pxz * pxz - (double)pyz * pyz);
+    src[((size_t)(x0 + xx) * n1 + gy) * n2 + gz] = source_combine(diag, pxy, pxz, pyz);
   }
 }
 
@@ -374,19 +400,28 @@ k_halo_sum(const int* __restrict__ hpeak, const int* __restrict__ gfin, const un
 
 // particle positions q + S and velocities (lpt.c:82-92, 212-222, 229-242),
 // interleaved [ng][3]
+// The lattice coordinate (x + 1/2) Lc of every index of the three axes is
+// formed once per block (the reference's float product plus a double half
+// cell) into shared memory (n0 + n1 + n2 floats).
 __global__ void k_particles(const float* __restrict__ S, const float* __restrict__ V, int n0, int n1, int n2,
                             HaloOut o, float* __restrict__ pos, float* __restrict__ vel) {
+  extern __shared__ float xq_s[];
+  for (int t = threadIdx.x; t < n0 + n1 + n2; t += blockDim.x) {
+    const int x = t < n0 ? t : (t < n0 + n1 ? t - n0 : t - n0 - n1);
+    xq_s[t] = (float)((double)((float)x * o.Lc) + (double)o.Lc / 2.0);
+  }
+  __syncthreads();
+  const int base[3] = {0, n0, n0 + n1};
   const size_t ng = (size_t)n0 * n1 * n2;
   size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (; c < ng; c += stride) {
-    const int k = (int)(c % n2);
-    const size_t r = c / n2;
-    const int j = (int)(r % n1), i = (int)(r / n1);
+    int i, j, k;
+    cell_ijk(c, ng, n1, n2, &i, &j, &k);
     const int xc[3] = {i, j, k};
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-      const float xq = (float)((double)((float)xc[a] * o.Lc) + (double)o.Lc / 2.0);
+      const float xq = xq_s[base[a] + xc[a]];
       float p = xq + S[a * ng + c];
       if (p >= o.L[a]) p -= o.L[a];
       if (p < 0.f) p += o.L[a];
@@ -560,7 +595,9 @@ int aos_to_planes(const float* in, size_t ng, float* out, cudaStream_t st) {
 
 int particles(const BoxParams& b, const float* S, const float* V, const HaloOut& o, float* pos, float* vel,
               cudaStream_t st) {
-  k_particles<<<EXH_NUM_SMS * 16, 256, 0, st>>>(S, V, b.nd[0], b.nd[1], b.nd[2], o, pos, vel);
+  const size_t sm = sizeof(float) * ((size_t)b.nd[0] + b.nd[1] + b.nd[2]);
+  EXH_CUDA_TRY(set_smem(k_particles, sm));
+  k_particles<<<EXH_NUM_SMS * 16, 256, sm, st>>>(S, V, b.nd[0], b.nd[1], b.nd[2], o, pos, vel);
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   return EXH_OK;

@@ -12,6 +12,7 @@
 
 #include "ctx.cuh"
 #include "fft4.cuh"
+#include "fixedpoint.cuh"
 #include "spectrum.cuh"
 
 namespace exh {
@@ -25,12 +26,11 @@ namespace exh {
 // associative, so the grid does not depend on the order in which threads
 // land: every run, every stream schedule and every batch gives the same
 // bits.  Each cell is rounded to float once, from the exact fixed-point sum.
-// Range: 2^23 tracers in one cell before the 64-bit sum overflows.
-constexpr double CIC_Q = 1099511627776.0;        // 2^40
-constexpr double CIC_INV_Q = 1.0 / 1099511627776.0;
-
+// Range: 2^23 tracers in one cell before the 64-bit sum overflows.  The
+// conversions (round(w 2^40) in, (float)((double)sum 2^-40) out) run in
+// integer arithmetic (fixedpoint.cuh), off the FP64 pipe.
 __device__ __forceinline__ void cic_add(unsigned long long* g, float w) {
-  atomicAdd(g, __double2ull_rn((double)w * CIC_Q));
+  atomicAdd(g, (unsigned long long)fp_quanta40(w));
 }
 
 __global__ void k_cic(const float* __restrict__ pos, int64_t np, int nd, float L, float Ld,
@@ -76,7 +76,7 @@ __global__ void k_cic_normalise(const unsigned long long* __restrict__ acc, floa
   size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (; i < ng; i += stride) {
-    const float rho = (float)((double)acc[i] * CIC_INV_Q);
+    const float rho = fp_value40(acc[i]);
     grid[i] = rho * inv_mean - 1.f;
   }
 }
