@@ -85,7 +85,7 @@ extern "C" int exh_abundance_compute(exh_ctx* ctx, const float* Mh, int64_t nh, 
   // spectrum.c:566-578: the range from the masses, widened by 1e-4
   if (Mmin < 0.f || Mmax < 0.f) {
     const unsigned init[2] = {0xFFFFFFFFu, 0u};
-    EXH_CUDA_TRY(cudaMemcpyAsync(mm, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    EXH_TRY(upload_small(mm, init, sizeof(init), st));
     if (nh > 0) {
       k_mass_range<<<nb, AB_T, 0, st>>>(d, nh, mm);
       count_launch(1);

@@ -1,5 +1,6 @@
 // FFT plans and the plain 3-D transforms of the C ABI.
 #include <cmath>
+#include <cstring>
 #include <map>
 #include <mutex>
 #include <utility>
@@ -85,6 +86,25 @@ int Ctx::side_stream(cudaStream_t* out) {
   }
   *out = side;
   return EXH_OK;
+}
+
+namespace {
+struct SmallBlob {
+  unsigned char b[UPLOAD_SMALL_MAX];
+};
+__global__ void k_upload_small(unsigned char* __restrict__ dst, SmallBlob blob, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = blob.b[i];
+}
+}  // namespace
+
+int upload_small(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  if (bytes == 0) return EXH_OK;
+  if (!dst || !src || bytes > UPLOAD_SMALL_MAX) return EXH_E_INVALID;
+  SmallBlob blob;
+  std::memcpy(blob.b, src, bytes);
+  k_upload_small<<<1, 64, 0, st>>>(reinterpret_cast<unsigned char*>(dst), blob, (int)bytes);
+  count_launch(1);
+  return cudaGetLastError() == cudaSuccess ? EXH_OK : EXH_E_CUDA;
 }
 
 int Ctx::fork_stream(cudaStream_t st, cudaStream_t* out) {

@@ -266,6 +266,15 @@ int fft_plan_create(FFTPlan3D* p, int nx, int ny, int nz);
 void fft_plan_destroy(FFTPlan3D* p);
 void count_launch(int n);          // host-side launch counter (capi.cu)
 
+// A small host-to-device upload (at most 256 bytes: counters, control
+// blocks) carried as a kernel argument, so the bytes are captured when the
+// launch is enqueued and the host source may change or go out of scope at
+// once.  cudaMemcpyAsync from pageable memory does not promise that: where
+// the GPU reads pageable memory directly, the copy may run later, from
+// whatever the stack holds by then.  (fft.cu)
+constexpr size_t UPLOAD_SMALL_MAX = 256;
+int upload_small(void* dst, const void* src, size_t bytes, cudaStream_t st);
+
 inline size_t smem_strided(int n) { return sizeof(float2) * 2 * (size_t)n * FFT_W; }
 inline size_t smem_r2c(int M) { return sizeof(float2) * 2 * (size_t)M * FFT_LDB; }
 inline size_t smem_c2r(int M) { return sizeof(float2) * (3 * (size_t)M + 1) * FFT_LDB; }

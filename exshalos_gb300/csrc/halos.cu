@@ -815,8 +815,8 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
   SortCtl h0{};
   const Seg whole{0, np - 1, 0, 0};
   if (np > SORT_SMALL) h0.nnext = 1; else h0.nsmall = 1;
-  EXH_CUDA_TRY(cudaMemcpyAsync(np > SORT_SMALL ? d_next : d_small, &whole, sizeof(Seg), cudaMemcpyHostToDevice, st));
-  EXH_CUDA_TRY(cudaMemcpyAsync(ctl, &h0, sizeof(SortCtl), cudaMemcpyHostToDevice, st));
+  EXH_TRY(upload_small(np > SORT_SMALL ? d_next : d_small, &whole, sizeof(Seg), st));
+  EXH_TRY(upload_small(ctl, &h0, sizeof(SortCtl), st));
   SortCtl hc = h0;
   if (np > SORT_SMALL) {
     k_qs_chunks<<<1, QS_CHUNK_T, 0, st>>>(ctl, d_next, d_segs, d_cfirst, d_cseg, d_coff, max_chunks);
@@ -1496,7 +1496,7 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   count_launch(1);
   {
     const int init[6] = {0, 0, (int)nproc, 0, 0, 0};
-    EXH_CUDA_TRY(cudaMemcpyAsync(dcnt, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    EXH_TRY(upload_small(dcnt, init, sizeof(init), st));
   }
   (void)nbw;
   if (timing_on()) EXH_CUDA_TRY(cudaMemsetAsync(h->words, 0, sizeof(unsigned) * npr, st));

@@ -659,7 +659,8 @@ extern "C" int exh_hod_populate(exh_ctx* ctx, const float* posh, const float* ve
   hc.alpha = hp->alpha;
   hc.in_c = dC ? 1 : 0;
   const HodCtl ctl0{0xFFFFFFFFu, 0u, 0, 0, 0, 0, 0.0};
-  EXH_CUDA_TRY(cudaMemcpyAsync(ctl, &ctl0, sizeof(ctl0), cudaMemcpyHostToDevice, st));
+  static_assert(sizeof(ctl0) <= UPLOAD_SMALL_MAX, "control block fits a kernel argument");
+  EXH_TRY(upload_small(ctl, &ctl0, sizeof(ctl0), st));
   EXH_CUDA_TRY(cudaMemsetAsync(nsat, 0, sizeof(int) * n, st));
   EXH_CUDA_TRY(cudaMemsetAsync(extra, 0, sizeof(long long) * n, st));
   const unsigned nb = (unsigned)std::min<size_t>(exh_div_up(n, HOD_T), EXH_NUM_SMS * 8);

@@ -380,7 +380,12 @@ extern "C" int exh_grid_compute_ex(exh_ctx* ctx, const float* pos, const float* 
   for (unsigned b = 0; b < nb; b++)
     for (int q = 0; q < ngrid; q++) Mt[q] += hp[(size_t)b * ngrid + q];
   double* dM = part + (size_t)nb * ngrid;
-  EXH_CUDA_TRY(cudaMemcpyAsync(dM, Mt.data(), sizeof(double) * ngrid, cudaMemcpyHostToDevice, st));
+  if (sizeof(double) * ngrid <= UPLOAD_SMALL_MAX) {
+    EXH_TRY(upload_small(dM, Mt.data(), sizeof(double) * ngrid, st));
+  } else {
+    EXH_CUDA_TRY(cudaMemcpyAsync(dM, Mt.data(), sizeof(double) * ngrid, cudaMemcpyHostToDevice, st));
+    EXH_CUDA_TRY(cudaStreamSynchronize(st));     // Mt dies at return
+  }
   float* g = grid;
   if (mem == EXH_MEM_HOST) {
     EXH_TRY(c.buf[B_GRID].ensure(sizeof(float) * ng * ngrid));
