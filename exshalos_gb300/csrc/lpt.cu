@@ -340,6 +340,8 @@ k_halo_sum(const int* __restrict__ hpeak, const int* __restrict__ gfin, const un
     x0 = (int)(rr / n1);
     cnt = start_all[gfin[r]];
   }
+  // member sums: compensated float per term, FP64 only once per halo (the
+  // FP64 pipe bounded this kernel when every term went through it)
   double s[3] = {0, 0, 0}, v[3] = {0, 0, 0};
   auto cell_of = [&](int q, int xa, int ya, int za) {
     const int pk = off_all[q];
@@ -349,14 +351,17 @@ k_halo_sum(const int* __restrict__ hpeak, const int* __restrict__ gfin, const un
   };
   const bool small = valid && cnt <= 32;
   if (small) {
+    FSum fs[3], fv[3];
     for (int q = 0; q < cnt; q++) {
       const size_t c = cell_of(q, x0, y0, z0);
 #pragma unroll
       for (int a = 0; a < 3; a++) {
-        s[a] += (double)S[a * ng + c];
-        if (V) v[a] += (double)V[a * ng + c];
+        fs[a].add(S[a * ng + c]);
+        if (V) fv[a].add(V[a * ng + c]);
       }
     }
+#pragma unroll
+    for (int a = 0; a < 3; a++) { s[a] = fs[a].value(); v[a] = fv[a].value(); }
   }
   unsigned big = __ballot_sync(0xffffffffu, valid && !small);
   while (big) {
@@ -364,15 +369,18 @@ k_halo_sum(const int* __restrict__ hpeak, const int* __restrict__ gfin, const un
     big &= big - 1;
     const int bx = __shfl_sync(0xffffffffu, x0, b), by = __shfl_sync(0xffffffffu, y0, b);
     const int bz = __shfl_sync(0xffffffffu, z0, b), bc = __shfl_sync(0xffffffffu, cnt, b);
-    double ts[3] = {0, 0, 0}, tv[3] = {0, 0, 0};
+    FSum fs[3], fv[3];
     for (int q = lane; q < bc; q += 32) {
       const size_t c = cell_of(q, bx, by, bz);
 #pragma unroll
       for (int a = 0; a < 3; a++) {
-        ts[a] += (double)S[a * ng + c];
-        if (V) tv[a] += (double)V[a * ng + c];
+        fs[a].add(S[a * ng + c]);
+        if (V) fv[a].add(V[a * ng + c]);
       }
     }
+    double ts[3], tv[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) { ts[a] = fs[a].value(); tv[a] = fv[a].value(); }
 #pragma unroll
     for (int a = 0; a < 3; a++)
 #pragma unroll

@@ -105,18 +105,9 @@ int cic_assign(Ctx& c, const float* pos_dev, int64_t np, int nd, float L, float*
 // ------------------------------------------------------------------ P(k)
 __device__ __forceinline__ float sinc_f(float x) { return x != 0.f ? sinf(x) / x : 1.f; }
 
-// Compensated (Neumaier) float sum of a run of same-bin modes; the run's
-// total goes to the double histogram as hi + lo.  Error of a run: about
-// 2^-24 of its total, whatever its length.
-struct RunSum {
-  float s = 0.f, c = 0.f;
-  __device__ __forceinline__ void add(float x) {
-    const float t = __fadd_rn(s, x);
-    c = __fadd_rn(c, fabsf(s) >= fabsf(x) ? __fadd_rn(__fsub_rn(s, t), x) : __fadd_rn(__fsub_rn(x, t), s));
-    s = t;
-  }
-  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
-};
+// A run of same-bin modes is summed in a compensated float sum (FSum) and
+// goes to the double histogram as its exact hi + lo.
+using RunSum = FSum;
 
 // Binning of one transformed tile res[i * W + b] (x index i < n, column
 // b < nb of the tile starting at inner index i0) into the block's shared
