@@ -1,0 +1,65 @@
+"""Host-side pieces of bench.py that need no GPU (CPU): the clock record
+kept from nvidia-smi samples inside the timed windows, the DRAM traffic
+figures read from the committed ncu summaries, and the compulsory bytes of
+one 256^3 realisation."""
+import os
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import bench  # noqa: E402
+
+
+class _DoneProc:
+    def terminate(self):
+        pass
+
+    def wait(self, timeout=None):
+        return 0
+
+
+def _sampler(lines, windows):
+    s = bench.ClockSampler(0)
+    s.proc = _DoneProc()
+    s.lines = lines
+    s.windows = windows
+    return s
+
+
+def test_clock_samples_inside_windows_only():
+    ok = "2070, 2070, Not Active, Not Active, Not Active, Not Active"
+    lines = [(0.5, "1000, 2070, Not Active, Not Active, Not Active, Not Active"),   # before: idle clock
+             (1.5, ok), (1.7, ok),
+             (2.5, "1500, 2070, Active, Not Active, Not Active, Not Active"),      # between the windows
+             (3.2, "2070, 2070, Not Active, Not Active, Not Active, Active")]
+    clk = _sampler(lines, [[1.0, 2.0], [3.0, 4.0]]).stop()
+    assert clk["samples"] == 3
+    assert clk["sm_mhz"] == 2070.0 and clk["sm_max_mhz"] == 2070.0
+    assert clk["reasons"] == ["sw_power_cap"]      # hw_slowdown fell between the windows
+
+
+def test_clock_window_without_sample_takes_the_one_before():
+    lines = [(0.9, "2055, 2070, Not Active, Not Active, Not Active, Not Active"),
+             (1.2, "2070, 2070, Not Active, Not Active, Not Active, Not Active")]
+    clk = _sampler(lines, [[1.0, 1.05]]).stop()
+    assert clk["samples"] == 1 and clk["sm_mhz"] == 2055.0
+
+
+def test_clock_without_windows_uses_every_sample():
+    lines = [(t, "2070, 2070, Not Active, Not Active, Not Active, Not Active") for t in (1.0, 2.0, 3.0)]
+    assert _sampler(lines, []).stop()["samples"] == 3
+
+
+def test_committed_traffic_covers_the_roofline_classes():
+    t = bench.committed_traffic()
+    for cls in ("fft_strided", "fft_rows", "sort", "grow"):
+        assert cls in t and t[cls] > 1e6, cls
+
+
+def test_step_bytes_of_a_256_cube_realisation():
+    # field 8Nc, c2r 8Nc + 4N, ladder 50 (8Nc + 2N), peaks + growth 8N, 1LPT 8Nc + 20N,
+    # 2LPT 52N + 16Nc, CIC + P(k) 12 nh + 8N + 16Nc: about 7.09 GB with 1e6 halos
+    b = bench.step_algorithmic_bytes(256, 50, 1.0e6)
+    assert abs(b - 7.088e9) < 0.01e9
