@@ -32,19 +32,6 @@ __host__ __device__ __forceinline__ int exh_wrap(int i, int j, int nd) {
   return r;
 }
 
-// Compensated (Neumaier) float sum, kept as s + c: its error is about 2^-24
-// of the total plus 2^-48 of the sum of magnitudes, and the FP64 pipe is not
-// used per term.  value() = s + c exactly in double.
-struct FSum {
-  float s = 0.f, c = 0.f;
-  __device__ __forceinline__ void add(float x) {
-    const float t = __fadd_rn(s, x);
-    c = __fadd_rn(c, fabsf(s) >= fabsf(x) ? __fadd_rn(__fsub_rn(s, t), x) : __fadd_rn(__fsub_rn(x, t), s));
-    s = t;
-  }
-  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
-};
-
 // (i, j, k) of the row-major cell index of an n0 x n1 x n2 grid of ng cells;
 // 32-bit divisions while the index fits
 __device__ __forceinline__ void cell_ijk(size_t cell, size_t ng, int n1, int n2, int* i, int* j, int* k) {

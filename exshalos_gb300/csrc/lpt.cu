@@ -14,6 +14,7 @@
 
 #include "ctx.cuh"
 #include "fft4.cuh"
+#include "fp32sum.cuh"
 #include "field.cuh"
 #include "halos.cuh"
 #include "lpt.cuh"
@@ -112,28 +113,6 @@ k_brick_grad(const float* __restrict__ phi, int n0, int n1, int n2, float fac, f
       if (V) { if (ADD) V[a * ng + c] += fv * s; else V[a * ng + c] = fv * s; }
     }
   }
-}
-
-// diag - x^2 - y^2 - z^2, which the reference forms in double from float
-// operands (pow(., 2.0), lpt.c:134): here in FP32 without the FP64 pipe.
-// Each square is split exactly into hi + lo by an FMA, the running value is
-// kept as s + c with s updated by an error-free TwoSum (Knuth), and the sum
-// is rounded once at the end: the error before that rounding is about 2^-47
-// of the largest term.
-__device__ __forceinline__ float source_combine(float diag, float x, float y, float z) {
-  float s = diag, c = 0.f;
-  const float p[3] = {x, y, z};
-#pragma unroll
-  for (int a = 0; a < 3; a++) {
-    const float hi = __fmul_rn(p[a], p[a]);
-    const float lo = __fmaf_rn(p[a], p[a], -hi);          // p^2 = hi + lo exactly
-    const float t = __fsub_rn(s, hi);
-    const float bb = __fsub_rn(t, s);                      // TwoSum of s and -hi
-    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(-hi, bb));
-    s = t;
-    c = __fsub_rn(__fadd_rn(c, e), lo);
-  }
-  return __fadd_rn(s, c);
 }
 
 // second-order source (lpt.c:116-134) from the first-order displacement

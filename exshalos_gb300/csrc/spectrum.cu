@@ -13,6 +13,7 @@
 #include "ctx.cuh"
 #include "fft4.cuh"
 #include "fixedpoint.cuh"
+#include "fp32sum.cuh"
 #include "spectrum.cuh"
 
 namespace exh {
