@@ -664,7 +664,12 @@ extern "C" int exh_diff_backward(exh_ctx* ctx, double grad_loss, float* grad_noi
   float* gbin = D.buf[DB_KNOTS].as<float>();
   double* kpart = reinterpret_cast<double*>(reinterpret_cast<char*>(gbin) + ((sizeof(float) * Nk + 15) & ~size_t(15)));
   double* kout = kpart + (size_t)EXH_NUM_SMS * 2 * MAX_KNOTS;
-  EXH_CUDA_TRY(cudaMemcpyAsync(gbin, gb.data(), sizeof(float) * Nk, cudaMemcpyHostToDevice, st));
+  if (sizeof(float) * Nk <= UPLOAD_SMALL_MAX) {
+    EXH_TRY(upload_small(gbin, gb.data(), sizeof(float) * Nk, st));
+  } else {
+    EXH_CUDA_TRY(cudaMemcpyAsync(gbin, gb.data(), sizeof(float) * Nk, cudaMemcpyHostToDevice, st));
+    EXH_CUDA_TRY(cudaStreamSynchronize(st));      // gb dies at return
+  }
   // P(k) and r2c adjoint: dchi2/dgrid
   EXH_CUDA_TRY(fft_c2r_3d(*p, BinGradLoad{X, gbin, g, D.bp}, work, RealPairStore{ggrid, nd, 1.f}, st));
   // CIC adjoint: delta = rho * ng / np - 1 with np = ng
