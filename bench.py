@@ -223,26 +223,52 @@ def cpu_baseline_sample(k, P, seed=1):
     return dt, equiv, nthr
 
 
+MAX_SKIPPED = 16            # realisations skipped at most (range errors) before a run gives up
+
+
+def run_seeds(fn, steps, first_seed, range_error, max_skipped=MAX_SKIPPED):
+    """Call fn(seed) on seeds first_seed, first_seed + 1, ... until `steps`
+    calls have completed.  A seed whose realisation raises `range_error` (a
+    halo mass outside the mass-function splines, where the reference's
+    gsl_spline_eval aborts, find_halos.c:472-474) is skipped, recorded and
+    not counted; both arms of the benchmark use this policy on the same seed
+    list.  Returns (results of the completed calls, completed seeds, skipped
+    seeds)."""
+    out, done, skipped = [], [], []
+    s = first_seed
+    while len(done) < steps:
+        if len(skipped) > max_skipped:
+            raise RuntimeError(f"more than {max_skipped} realisations failed with range errors")
+        try:
+            out.append(fn(s))
+            done.append(s)
+        except range_error:
+            skipped.append(s)
+        s += 1
+    return out, done, skipped
+
+
 def run_reference(args, ws, rank):
     from exshalos_gb300.workloads import synthetic_pk
+    from oracle import orc
     if rank != 0:
         return
     k, P = synthetic_pk()
     k, P = k.astype(np.float32), P.astype(np.float32)
-    for w in range(args.warmup):
-        cpu_baseline_sample(k, P, seed=100 + w)
-    tot, eq = 0.0, 0.0
-    nthr = 1
-    for s in range(args.steps):
-        dt, e, nthr = cpu_baseline_sample(k, P, seed=s + 1)
-        tot += dt
-        eq += e
+    run_seeds(lambda s: cpu_baseline_sample(k, P, seed=s), args.warmup, 100, orc.RangeError)
+    res, done, skipped = run_seeds(lambda s: cpu_baseline_sample(k, P, seed=s), args.steps, 1, orc.RangeError)
+    tot = sum(r[0] for r in res)
+    eq = sum(r[1] for r in res)
+    nthr = res[-1][2] if res else 1
     v = eq / tot
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "realisations/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tot / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "box_256 (nd=256, Lc=2, L=512, 2LPT, barrier a=1 beta=0.12 alpha=0, CIC 256^3, "
-                                   "P(k) 128 bins, 50-radius ladder)", "sample": "one full 256^3 realisation per step"},
+                                   "P(k) 128 bins, 50-radius ladder)", "sample": "one full 256^3 realisation per step",
+                       "seeds": [done[0], done[-1]] if done else None, "skipped_seeds": skipped,
+                       "skip_policy": "realisations whose halo masses leave the mass-function splines (the "
+                                      "reference's GSL spline aborts there) are skipped and not timed"},
             "cpu_baseline": {"value": v, "unit": "realisations/s", "cores": nthr, "kind": "port",
                              "sample": "one 256^3 realisation (field, halos, 2LPT, CIC, P(k)) per step; ladder timed on "
                                        f"{LADDER_SAMPLE} of {N_RADII} radii and scaled"},
@@ -259,6 +285,66 @@ def step_algorithmic_bytes(nd, n_radii, nh):
     Nc = float(nd) * nd * (nd // 2 + 1)
     return (8 * Nc + (8 * Nc + 4 * N) + n_radii * (8 * Nc + 2 * N) + 8 * N + (8 * Nc + 20 * N) +
             (52 * N + 16 * Nc) + (12 * nh + 8 * N + 16 * Nc))
+
+
+def _rel_rms(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.sqrt(np.mean((a - b) ** 2) / np.mean(b ** 2)))
+
+
+def accuracy_summary(k, P, seed):
+    """Error figures of one box_256 realisation (a timed seed), computed
+    after the timed region: the catalogue against the oracle's Find_Halos on
+    the GPU's float field (bit-exact or not), the field, the halo
+    displacements, the CIC grid and the 128-bin P(k) against the FP64
+    oracle (same positions / same grid), the whole chain's P(k) against the
+    FP64 chain on the same catalogue, and the fraction of cells whose
+    first-crossing radius in the 50-radius ladder differs from the FP64
+    ladder's."""
+    from exshalos_gb300 import simulation
+    from exshalos_gb300.lib import exshalos as exl
+    from oracle import orc
+    nthr = os.cpu_count() or 1
+    orc.set_threads(nthr, prec="f64")
+    Lbox = ND * LC
+    r = exl.halos_box_from_pk(k, P, 1e5, ND, ND, ND, LC, seed, 1e4, 0.31, 0.0, -1.0, 1, BARRIER["a"],
+                              BARRIER["beta"], BARRIER["alpha"], 0, 0.0, 1, 0, 0, 1, 1, 0, 0, 1, _catalogue=True)
+    r = {kk: np.array(v) for kk, v in r.items()}
+    p = orc.make_params(ND, LC, seed=seed, **BARRIER)
+    ref = orc.find_halos(p, r["grid"], orc.sigma_tables(p, k, P))
+    same = bool(r["Mh"].size == ref["nh"] and np.array_equal(r["x"], ref["x"]) and
+                np.array_equal(r["count"], ref["count"]) and
+                np.array_equal(r["Mh"].view(np.uint32), ref["Mh"].view(np.uint32)) and
+                np.array_equal(r["flag"].reshape(-1), ref["flag"]))
+    modes = orc.field_modes(p, k, P, stream=1)
+    e_field = _rel_rms(r["grid"], orc.field_real(p, modes))
+    lp = orc.lpt_posh(p, k, P, ref["flag"], ref["x"], ref["count"], do_2lpt=1, modes=modes)
+    centre = LC * (ref["x"] + 0.5)
+    wrap = lambda d: (d + Lbox / 2) % Lbox - Lbox / 2          # noqa: E731
+    dD = wrap(r["posh"].astype(np.float64) - lp["posh"])
+    e_disp = float(np.sqrt(np.mean(dD ** 2) / np.mean(wrap(lp["posh"] - centre) ** 2)))
+    grid = simulation.Compute_Density_Grid(r["posh"], nd=ND, L=Lbox, window="CIC")
+    e_grid = _rel_rms(grid, orc.cic(r["posh"].astype(np.float64), ND, Lbox))
+    pk = simulation.Compute_Power_Spectrum(grid, L=Lbox, window="CIC", Nk=NK_PK)
+    kmin, kmax = np.float32(2 * np.pi / Lbox), np.float32(np.pi / Lbox * ND)
+    want = orc.power(np.asarray(grid, dtype=np.float64), Lbox, window=2, Nk=NK_PK, kmin=kmin, kmax=kmax)
+    m = want["Nk"] > 0
+    chain = orc.power(orc.cic(lp["posh"], ND, Lbox), Lbox, window=2, Nk=NK_PK, kmin=kmin, kmax=kmax)
+    cr = exl.smoothing_ladder(k, P, R_LADDER, ND, ND, ND, LC, seed=seed, n_radii=N_RADII, **BARRIER)
+    want_cross = orc.ladder(orc.make_params(ND, LC, seed=seed), modes, cr["R"], cr["B"])
+    return {"seed": int(seed), "halos": int(ref["nh"]), "catalogue_identical": same,
+            "field_rel_rms_vs_fp64": e_field, "halo_displacement_rel_rms_vs_fp64": e_disp,
+            "cic_rel_rms_vs_fp64": e_grid,
+            "pk_counts_identical": bool(np.array_equal(pk["Nk"], want["Nk"])),
+            "pk_max_rel_err_vs_fp64": float(np.max(np.abs(pk["Pk"][m] / want["Pk"][m] - 1))),
+            "pk_chain_max_rel_err_vs_fp64": float(np.max(np.abs(pk["Pk"][m] / chain["Pk"][m] - 1))),
+            "ladder_flip_fraction": float(np.mean(cr["cross"] != want_cross)),
+            "ladder_crossed_fraction": float(np.mean(want_cross != 255)),
+            "how": "one timed seed after the timed region; catalogue vs the oracle's Find_Halos on the GPU field; "
+                   "field, halo displacements (same labelling), CIC (same positions), P(k) (same grid) and the "
+                   "chain's P(k) (FP64 LPT -> CIC -> P(k) on the same catalogue) vs the FP64 oracle; flips vs the "
+                   "FP64 ladder of the same modes"}
 
 
 def batched_summary(k, P, lanes, seed0=0):
@@ -453,9 +539,10 @@ def run_ours(args, ws, rank, local):
                                          _capi.EXH_MEM_DEVICE, hs))
         nh_seen.append(nh.value)
 
+    # the same seed policy as the reference arm: a realisation whose halo
+    # masses leave the mass-function splines is skipped (run_seeds)
     seed0 = 1000 * rank + 1
-    for w in range(args.warmup):
-        step(seed0 + 500 + w)
+    run_seeds(step, args.warmup, seed0 + 500, _capi.HaloRangeError)
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
@@ -467,8 +554,7 @@ def run_ours(args, ws, rank, local):
     ev0.record()
     s_lad.wait_stream(torch.cuda.current_stream())
     s_halo.wait_stream(torch.cuda.current_stream())
-    for s in range(args.steps):
-        step(seed0 + s)
+    _, done_seeds, skipped_seeds = run_seeds(step, args.steps, seed0, _capi.HaloRangeError)
     torch.cuda.current_stream().wait_stream(s_lad)
     torch.cuda.current_stream().wait_stream(s_halo)
     ev1.record()
@@ -483,8 +569,7 @@ def run_ours(args, ws, rank, local):
     # and the ladder launches its kernels one by one
     _capi.timing_enable(True)
     clocks.open_window()
-    for s in range(args.steps):
-        step(seed0 + 100 + s, serial=True)
+    run_seeds(lambda s: step(s, serial=True), args.steps, seed0 + 100, _capi.HaloRangeError)
     torch.cuda.synchronize()
     clocks.close_window()
     clk = clocks.stop()
@@ -506,13 +591,11 @@ def run_ours(args, ws, rank, local):
         pk = simulation.Compute_Power_Spectrum(grid, L=float(Lbox), window="CIC", Nk=NK_PK)
         return cr, r, grid, pk
 
-    for w in range(min(args.warmup, 2)):               # untimed: the public API's host buffers settle
-        e2e_step(seed0 + 150 + w)
+    run_seeds(e2e_step, min(args.warmup, 2), seed0 + 150, _capi.HaloRangeError)   # untimed: host buffers settle
     barrier(ws)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for s in range(e2e_steps):
-        cr, r, grid, pk = e2e_step(seed0 + 200 + s)
+    for cr, r, grid, pk in run_seeds(e2e_step, e2e_steps, seed0 + 200, _capi.HaloRangeError)[0]:
         n = r["posh"].shape[0]
         h2d += k.nbytes + P.nbytes + 12 * n + 4 * ng
         d2h += cr["cross"].nbytes + 16 * n + 4 * ng + pk["k"].nbytes + pk["Pk"].nbytes + pk["Nk"].nbytes
@@ -540,6 +623,9 @@ def run_ours(args, ws, rank, local):
                "frac": step_gbs / peak,
                "note": "whole realisation: compulsory bytes of every stage over the step time; the sort and the "
                        "growth are latency-bound, so this stays far below the streaming passes' fractions"}
+    accuracy = None
+    if rank == 0 and not args.no_accuracy:
+        accuracy = accuracy_summary(k, P, done_seeds[0])
     batched = None if args.no_batched else batched_summary(k, P, args.lanes, seed0=1000 * rank)
     differentiable = None if args.no_batched else diff_summary(k, P)
     galaxies = None if args.no_batched else galaxies_summary(k, P, reps=5, cpu=not args.no_cpu_baseline)
@@ -564,7 +650,8 @@ def run_ours(args, ws, rank, local):
                    "class_timing": "stage_ms_per_step, roofline_by_class and roofline from a second pass of the "
                                    "same number of steps with CUDA events around every launch, all stages on one stream "
                                    "(no overlap, so each class's time is its own kernels')",
-                   "mean_halos": float(np.mean(nh_seen[-args.steps:])) if nh_seen else None},
+                   "mean_halos": float(np.mean(nh_seen[-args.steps:])) if nh_seen else None,
+                   "seeds": [done_seeds[0], done_seeds[-1]], "skipped_seeds": skipped_seeds},
         "e2e": {"value": e2e, "unit": "realisations/s", "h2d_bytes_per_step": int(h2d / e2e_steps),
                 "d2h_bytes_per_step": int(d2h / e2e_steps)},
         "gpu_launches": int(launches),
@@ -577,6 +664,7 @@ def run_ours(args, ws, rank, local):
         "roofline_by_class": by_class,
         "clocks": clk,
         "cpu_baseline": cpu,
+        "accuracy": accuracy,
         "batched": batched,
         "differentiable": differentiable,
         "galaxies": galaxies,
@@ -715,6 +803,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-workload summary")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the error figures against the FP64 oracle")
     ap.add_argument("--lanes", type=int, default=12, help="lanes of the batched runner")
     ap.add_argument("--workload", default="box_256", choices=["box_256", "box_512", "galaxies_256", "fft_512"],
                     help="box_256: the headline line; box_512: the large-box kernel-class report; "

@@ -152,6 +152,12 @@ class ExhError(RuntimeError):
     pass
 
 
+class HaloRangeError(ExhError):
+    """EXH_E_RANGE: a halo beyond the sigma table or a mass outside the
+    mass-function splines (the reference's GSL spline aborts there,
+    find_halos.c:472-474)."""
+
+
 def check(status):
     if status == EXH_OK:
         return
@@ -163,6 +169,8 @@ def check(status):
         raise MemoryError(msg)
     if status == EXH_E_UNSUPPORTED:
         raise NotImplementedError(msg)
+    if status == EXH_E_RANGE:
+        raise HaloRangeError(msg)
     raise ExhError(msg)
 
 

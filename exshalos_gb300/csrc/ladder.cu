@@ -379,8 +379,11 @@ int smoothing_ladder(Ctx& c, const BoxParams& b, const FieldModes& modes, int n_
     KTimer kt(KC_OTHER, st, 4.0 * n_radii * nn);
     k_ladder_wtab<<<EXH_NUM_SMS * 8, 256, 0, st>>>(dR, n_radii, nn, kf, wtab);
     count_launch(1);
-    EXH_CUDA_TRY(cudaGetLastError());
-    EXH_CUDA_TRY(cudaStreamSynchronize(st));    // R is the caller's host array
+    const cudaError_t le = cudaGetLastError();
+    // the copy reads host memory that the next call may reassign: wait for
+    // it before returning, also when the launch failed
+    EXH_CUDA_TRY(cudaStreamSynchronize(st));
+    EXH_CUDA_TRY(le);
     c.ladder_key = key;
   }
   EXH_CUDA_TRY(cudaMemsetAsync(cross, 255, b.ng, st));

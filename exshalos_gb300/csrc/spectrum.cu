@@ -518,9 +518,18 @@ extern "C" int exh_power_compute_noalloc(const float* grid, int nd, float L, int
     exh_set_error_msg("exh_power_compute_noalloc: Nk must be in [1, 256]", __FILE__, __LINE__);
     return EXH_E_INVALID;
   }
-  if (!(L > 0.f) || !(k_max > k_min) || window < 0 || window > 2) {
-    exh_set_error_msg("need L > 0, k_max > k_min and window 0, 1 or 2", __FILE__, __LINE__);
+  if (!(L > 0.f) || !(k_max > k_min)) {
+    exh_set_error_msg("need L > 0 and k_max > k_min", __FILE__, __LINE__);
     return EXH_E_INVALID;
+  }
+  if (window < 0 || window > 2) {     // as exh_power_compute
+    exh_set_error_msg("windows 0 (none), 1 (NGP), 2 (CIC) are built", __FILE__, __LINE__);
+    return EXH_E_UNSUPPORTED;
+  }
+  if (timing_on()) {
+    // kernel-class timing creates CUDA events, which this entry point must not
+    exh_set_error_msg("exh_power_compute_noalloc: turn kernel-class timing off first", __FILE__, __LINE__);
+    return EXH_E_UNSUPPORTED;
   }
   int dev = 0;
   EXH_CUDA_TRY(cudaGetDevice(&dev));

@@ -116,10 +116,13 @@ int exh_abundance_compute(exh_ctx *ctx, const float *Mh, int64_t nh, float Mmin,
  * grid, k_out, P_out and count_out are all device pointers and nothing is
  * allocated: the work arrays live in one static device array of about
  * 1.8 MB that every GPU loading the library keeps until exit.  Limits:
- * nd even, 2^a 3^b, nd <= 64; Nk <= 256 (EXH_E_INVALID beyond).  The first
- * call on a device looks up that array's device address; make it before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * race.  Kernel-class timing (exh_timing_enable) must be off. */
+ * nd even, 2^a 3^b, nd <= 64; Nk <= 256 (EXH_E_INVALID beyond); windows
+ * 0..2 (EXH_E_UNSUPPORTED beyond, as exh_power_compute).  The first call on
+ * a device looks up that array's device address and keeps it for the life
+ * of the process; make that call before any stream capture, and do not use
+ * the library on a device after cudaDeviceReset.  All calls share the array:
+ * calls that overlap on the GPU race.  Kernel-class timing
+ * (exh_timing_enable) must be off (EXH_E_UNSUPPORTED otherwise). */
 int exh_power_compute_noalloc(const float *grid, int nd, float L, int window, int Nk, float k_min,
                               float k_max, float *k_out, float *P_out, int64_t *count_out, void *stream);
 

@@ -14,6 +14,11 @@ from . import build as _build
 _LIBS = {}
 
 
+class RangeError(RuntimeError):
+    """A halo mass outside the mass-function splines: the reference's
+    gsl_spline_eval aborts there (find_halos.c:472-474)."""
+
+
 class Params(C.Structure):
     _fields_ = [
         ("Om0", C.c_float), ("redshift", C.c_float), ("dc", C.c_float), ("rhoc", C.c_float),
@@ -155,8 +160,10 @@ def find_halos(p, delta, tables, prec="f64"):
     Int = np.ascontiguousarray(tables["Int"], dtype=np.float64)
     nh = L.orc_find_halos(C.byref(p), _ptr(delta), _ptr(btab), int(tables["Ncells"]), _ptr(M), _ptr(Int),
                           M.size, _ptr(flag), _ptr(hx), _ptr(hc), _ptr(Mh), C.c_size_t(cap), C.byref(npo))
+    if nh == (1 << 64) - 2:
+        raise RangeError("oracle halo finder: a halo mass outside the mass-function splines")
     if nh >= (1 << 63):
-        raise RuntimeError("oracle halo finder reported a range error")
+        raise RuntimeError("oracle halo finder failed")
     return {"nh": nh, "np": npo.value, "x": hx[:3 * nh].reshape(nh, 3), "count": hc[:nh],
             "Mh": Mh[:nh], "flag": flag}
 
@@ -214,6 +221,8 @@ def halos_box_from_pk(k, P, nd=64, Lc=4.0, Om0=0.31, z=0.0, dc=-1.0, Nmin=1, a=1
                                  C.c_float(z), C.c_float(dc), int(Nmin), C.c_float(a), C.c_float(beta),
                                  C.c_float(alpha), int(seed), int(stream), int(fixed), C.c_float(phase),
                                  C.c_float(k_smooth), int(do_2lpt), int(prec64), int(keep_S), C.byref(r))
+    if st == 5:
+        raise RangeError("oracle pipeline: a halo mass outside the mass-function splines")
     if st:
         raise RuntimeError(f"oracle pipeline failed ({st})")
     nh, ng = r.nh, nd ** 3

@@ -60,7 +60,13 @@ int orc_halos_box_from_pk(const float *K, const float *P, int Nk, int nd, float 
   size_t nh = orc_find_halos(&p, res->delta, Btab, Ncells, M, Int, Nk, res->flag, res->hx,
                              res->hcount, res->Mh, np, &res->np);
   free(Sig); free(Btab); free(M); free(Int);
-  if (nh == (size_t)-1 || nh == (size_t)-2) { free(deltak); return 5; }
+  /* 5: a halo mass outside the mass-function splines (where the reference's
+   * gsl_spline_eval aborts, find_halos.c:472-474); 7: growth failed */
+  if (nh == (size_t)-2 || nh == (size_t)-1) {
+    free(deltak);
+    orc_result_free(res);
+    return nh == (size_t)-2 ? 5 : 7;
+  }
   res->nh = nh;
   double t2 = now_s();
 

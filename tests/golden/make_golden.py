@@ -1,7 +1,8 @@
 """Regenerates the golden fixtures in this directory from the reference tree.
 
-Run in a container that has the reference checkout (its path is the first
-argument, default /root/reference).  The reference's sphere table
+Run where the reference checkout exists, with its path as the one required
+argument:  python tests/golden/make_golden.py <reference tree>.  The
+reference's sphere table
 (src/exshalos/cells_in_spheres.c:4) is read as text and written as one
 integer per line; the oracle and the CUDA library must reproduce it.
 """
@@ -9,8 +10,8 @@ import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
 HERE = os.path.dirname(os.path.abspath(__file__))
+REF = None
 
 
 def cells_in_spheres():
@@ -25,4 +26,7 @@ def cells_in_spheres():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <reference tree>")
+    REF = sys.argv[1]
     print("cells_in_spheres:", cells_in_spheres())

@@ -63,3 +63,40 @@ def test_step_bytes_of_a_256_cube_realisation():
     # 2LPT 52N + 16Nc, CIC + P(k) 12 nh + 8N + 16Nc: about 7.09 GB with 1e6 halos
     b = bench.step_algorithmic_bytes(256, 50, 1.0e6)
     assert abs(b - 7.088e9) < 0.01e9
+
+
+class _Range(RuntimeError):
+    pass
+
+
+def test_seed_policy_skips_range_errors_and_counts_completed_steps():
+    def fn(s):
+        if s in (3, 8):
+            raise _Range()
+        return s * 10
+
+    out, done, skipped = bench.run_seeds(fn, 7, 1, _Range)
+    assert done == [1, 2, 4, 5, 6, 7, 9] and skipped == [3, 8]
+    assert out == [10, 20, 40, 50, 60, 70, 90]
+
+
+def test_seed_policy_gives_up_after_many_range_errors():
+    import pytest
+
+    def fn(s):
+        raise _Range()
+
+    with pytest.raises(RuntimeError):
+        bench.run_seeds(fn, 2, 1, _Range, max_skipped=3)
+
+
+def test_reference_realisation_with_range_error_is_reported(orc, pk):
+    """Seed 8 of the box_256 workload (taus field, barrier a=1 beta=0.12)
+    grows a halo of ~5000 cells whose mass lies beyond the mass-function
+    splines: the oracle raises its range error, which the benchmark's seed
+    policy skips (the reference's GSL spline would abort)."""
+    import pytest
+    k, P = pk
+    with pytest.raises(orc.RangeError):
+        orc.halos_box_from_pk(k, P, nd=256, Lc=2.0, seed=8, stream=0, do_2lpt=0, prec="f32", a=1.0, beta=0.12,
+                              alpha=0.0)

@@ -1,0 +1,104 @@
+"""The box_256 workload at its full size (GPU): nd = 256, Lc = 2 Mpc/h
+(L = 512), 2LPT, ellipsoidal barrier a = 1, beta = 0.12, alpha = 0, the
+kernels the benchmark runs (256-point four-step passes, the 2LPT Poisson x
+pass k_fft4_x_poisson<16,16>, the P(k) binning pass k_fft4_x_bin<16,16>), on
+two Philox seeds, one of them the benchmark's first timed seed.
+
+* catalogue (centre cells, member counts, mass bits, per-cell flags)
+  bit-identical to the oracle's Find_Halos on the GPU's float field
+  (find_halos.c:479-563);
+* field, particle displacements (2LPT, lpt.c:4-242) and halo displacements
+  against the FP64 oracle on the same labelling: relative rms <= 1e-5
+  (the reference's own float arithmetic sits at 1-2e-6 here) and at most
+  1e-3 Mpc/h anywhere;
+* CIC grid of the halos (gridmodule.c:21-53) against FP64 on the same
+  positions: relative rms <= 1e-5;
+* P(k) in 128 bins (powermodule.c:4-108) of that grid against FP64 on the
+  same grid: identical counts, every bin within 1e-5; and the whole chain's
+  P(k) (GPU field -> halos -> 2LPT -> CIC -> P(k)) within 1e-4 of the FP64
+  chain on the same catalogue.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_rms
+
+pytestmark = pytest.mark.gpu
+
+ND, LC, NK = 256, 2.0, 128
+L = ND * LC
+BARRIER = dict(a=1.0, beta=0.12, alpha=0.0)
+
+
+def _wrap(d):
+    return (d + L / 2) % L - L / 2
+
+
+@pytest.fixture(scope="module", params=[1, 7])
+def box(request, orc, pk):
+    from exshalos_gb300.lib import exshalos
+    k, P = pk
+    seed = request.param
+    r = exshalos.halos_box_from_pk(k, P, 1e5, ND, ND, ND, LC, seed, 1e4, 0.31, 0.0, -1.0, 1, BARRIER["a"],
+                                   BARRIER["beta"], BARRIER["alpha"], 0, 0.0, 1, 1, 0, 1, 1, 0, 0, 1,
+                                   _catalogue=True)
+    r = {key: np.array(v) for key, v in r.items()}        # out of the host-buffer pool
+    p = orc.make_params(ND, LC, seed=seed, **BARRIER)
+    ref = orc.find_halos(p, r["grid"], orc.sigma_tables(p, k, P))
+    return seed, p, r, ref
+
+
+def test_box256_catalogue_bit_exact(box):
+    seed, p, r, ref = box
+    assert ref["nh"] > 500000 and ref["np"] > 1000000
+    assert r["Mh"].size == ref["nh"]
+    np.testing.assert_array_equal(r["x"], ref["x"])
+    np.testing.assert_array_equal(r["count"], ref["count"])
+    np.testing.assert_array_equal(r["Mh"].view(np.uint32), ref["Mh"].view(np.uint32))
+    np.testing.assert_array_equal(r["flag"].reshape(-1), ref["flag"])
+
+
+def test_box256_field_and_displacements_vs_fp64(box, orc, pk):
+    seed, p, r, ref = box
+    k, P = pk
+    modes = orc.field_modes(p, k, P, stream=1)
+    want_field = orc.field_real(p, modes)
+    e_field = rel_rms(r["grid"], want_field)
+    lp = orc.lpt_posh(p, k, P, ref["flag"], ref["x"], ref["count"], do_2lpt=1, keep_pos=True, modes=modes)
+    q = (np.indices((ND, ND, ND), dtype=np.float64).reshape(3, -1).T + 0.5) * LC
+    S64 = _wrap(lp["pos"] - q)
+    dS = _wrap(r["pos"].astype(np.float64) - lp["pos"])
+    e_S = float(np.sqrt(np.mean(dS ** 2) / np.mean(S64 ** 2)))
+    centre = LC * (ref["x"] + 0.5)
+    D64 = _wrap(lp["posh"] - centre)
+    dD = _wrap(r["posh"].astype(np.float64) - lp["posh"])
+    e_D = float(np.sqrt(np.mean(dD ** 2) / np.mean(D64 ** 2)))
+    print(f"seed {seed}: field {e_field:.2e}, particles {e_S:.2e} (max {np.abs(dS).max():.2e} Mpc/h), "
+          f"halos {e_D:.2e} (max {np.abs(dD).max():.2e} Mpc/h)")
+    assert e_field < 1e-5
+    assert e_S < 1e-5 and np.abs(dS).max() < 1e-3
+    assert e_D < 1e-5 and np.abs(dD).max() < 1e-3
+
+
+def test_box256_cic_and_power_vs_fp64(box, orc, pk):
+    from exshalos_gb300 import simulation
+    seed, p, r, ref = box
+    k, P = pk
+    grid = simulation.Compute_Density_Grid(r["posh"], nd=ND, L=L, window="CIC")
+    want_grid = orc.cic(r["posh"].astype(np.float64), ND, L)
+    e_grid = rel_rms(grid, want_grid)
+    pk_gpu = simulation.Compute_Power_Spectrum(grid, L=L, window="CIC", Nk=NK)
+    kmin, kmax = np.float32(2 * np.pi / L), np.float32(np.pi / L * ND)
+    want = orc.power(np.asarray(grid, dtype=np.float64), L, window=2, Nk=NK, kmin=kmin, kmax=kmax)
+    np.testing.assert_array_equal(pk_gpu["Nk"], want["Nk"])
+    m = want["Nk"] > 0
+    e_bin = float(np.max(np.abs(pk_gpu["Pk"][m] / want["Pk"][m] - 1)))
+    # the whole chain in FP64 on the same catalogue
+    lp = orc.lpt_posh(p, k, P, ref["flag"], ref["x"], ref["count"], do_2lpt=1)
+    chain = orc.power(orc.cic(lp["posh"], ND, L), L, window=2, Nk=NK, kmin=kmin, kmax=kmax)
+    e_chain = float(np.max(np.abs(pk_gpu["Pk"][m] / chain["Pk"][m] - 1)))
+    print(f"seed {seed}: CIC {e_grid:.2e}, P(k) bins {e_bin:.2e}, chain P(k) {e_chain:.2e}")
+    assert e_grid < 1e-5
+    assert e_bin < 1e-5
+    assert np.max(np.abs(pk_gpu["k"][m] / want["k"][m] - 1)) < 1e-6
+    assert e_chain < 1e-4

@@ -1,6 +1,9 @@
 """Large box, nd = 512 (L = 1024 Mpc/h): halos, the 2LPT particle catalogue
 of 512^3 positions, their CIC grid and the 256-bin P(k), checked at full size
-through properties and against the FP64 oracle's P(k) of the same grid (GPU)."""
+through properties, against the FP64 oracle's P(k) of the same grid, and the
+particle positions (the 512-point passes, among them the 2LPT Poisson x pass
+k_fft8_x_poisson512) against the FP64 oracle's 2LPT (lpt.c:4-242) on the same
+Philox field (GPU)."""
 import ctypes as C
 
 import numpy as np
@@ -56,3 +59,26 @@ def test_box512_particles_cic_pk(orc, pk):
     m = want["Nk"] > 0
     assert np.max(np.abs(P_out[m] / want["Pk"][m] - 1)) < 1e-4
     assert np.max(np.abs(k_out[m] / want["k"][m] - 1)) < 1e-6
+    del g, grid, posh
+    # particle positions against the FP64 2LPT of the same field (no halo
+    # labelling needed for the particles), compared slab by slab
+    got = pos.cpu().numpy().reshape(nd, nd * nd, 3)
+    del pos
+    p = orc.make_params(nd, Lc, seed=1, a=1.0, beta=0.12, alpha=0.0)
+    lp = orc.lpt_posh(p, k, P, np.full(ng, ng, dtype=np.int64), np.zeros((0, 3), np.int32), np.zeros(0, np.int32),
+                      do_2lpt=1, keep_pos=True)
+    want_pos = lp["pos"].reshape(nd, nd * nd, 3)
+    num = den = worst = 0.0
+    jk = (np.indices((nd, nd), dtype=np.float64).reshape(2, -1).T + 0.5) * Lc
+    for i in range(nd):
+        a = got[i].astype(np.float64)
+        b = want_pos[i]
+        d = np.remainder(a - b + L / 2, L) - L / 2
+        q = np.concatenate([np.full((nd * nd, 1), (i + 0.5) * Lc), jk], axis=1)
+        s_ = np.remainder(b - q + L / 2, L) - L / 2
+        num += float(np.sum(d * d))
+        den += float(np.sum(s_ * s_))
+        worst = max(worst, float(np.abs(d).max()))
+    e = np.sqrt(num / den)
+    print(f"512^3 particles vs FP64: rel rms {e:.2e}, max {worst:.2e} Mpc/h")
+    assert e < 1e-5 and worst < 2e-3

@@ -13,7 +13,8 @@ def _dev(a):
 
 
 @pytest.mark.parametrize("shape", [(32, 32, 32), (48, 48, 48), (64, 64, 64), (96, 96, 96), (16, 24, 36),
-                                   (128, 128, 128), (64, 32, 16), (512, 512, 8), (16, 512, 36), (512, 24, 1024)])
+                                   (128, 128, 128), (64, 32, 16), (512, 512, 8), (16, 512, 36), (512, 24, 1024),
+                                   (256, 256, 256), (512, 512, 512)])
 def test_fft_roundtrip_vs_numpy(shape):
     import torch
     from exshalos_gb300 import _capi

@@ -70,3 +70,15 @@ def test_noalloc_rejects_sizes_beyond_its_limit():
     st = L_.exh_power_compute_noalloc(_capi.ptr(g), 32, C.c_float(100.0), 2, 300, C.c_float(0.1), C.c_float(1.0),
                                       _capi.ptr(out), _capi.ptr(out), _capi.ptr(cnt), None)
     assert st == _capi.EXH_E_INVALID
+    # windows beyond CIC are not built, as in the allocating entry point
+    st = L_.exh_power_compute_noalloc(_capi.ptr(g), 32, C.c_float(100.0), 3, 16, C.c_float(0.1), C.c_float(1.0),
+                                      _capi.ptr(out), _capi.ptr(out), _capi.ptr(cnt), None)
+    assert st == _capi.EXH_E_UNSUPPORTED
+    # kernel-class timing would create CUDA events: refused while it is on
+    _capi.timing_enable(True)
+    try:
+        st = L_.exh_power_compute_noalloc(_capi.ptr(g), 32, C.c_float(100.0), 2, 16, C.c_float(0.1),
+                                          C.c_float(1.0), _capi.ptr(out), _capi.ptr(out), _capi.ptr(cnt), None)
+    finally:
+        _capi.timing_enable(False)
+    assert st == _capi.EXH_E_UNSUPPORTED
