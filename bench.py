@@ -6,7 +6,8 @@ One step = one realisation of the single-box workload: Gaussian field
 with the ellipsoidal barrier (a = 1, beta = 0.12, alpha = 0), the top-hat
 smoothing ladder of 50 log-spaced radii from one cell to 30 Mpc/h with its
 per-cell first-crossing map, 2LPT displacement of the halos, CIC of the halo positions on a 256^3 grid and the
-power spectrum in 128 bins.  Every step draws a new Philox seed.
+power spectrum in 128 bins.  Every step takes the next seed of the reference's own field stream (GSL taus, polar
+deviates in its loop order), so both arms compute the same realisations.
 
   value   device-resident: C ABI calls with device buffers (k, P are the only
           inputs, 8 KB), halo positions and the grid stay in HBM
@@ -266,6 +267,7 @@ def run_reference(args, ws, rank):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "box_256 (nd=256, Lc=2, L=512, 2LPT, barrier a=1 beta=0.12 alpha=0, CIC 256^3, "
                                    "P(k) 128 bins, 50-radius ladder)", "sample": "one full 256^3 realisation per step",
+                       "field_stream": "the reference's (GSL taus seeded with the step's seed)",
                        "seeds": [done[0], done[-1]] if done else None, "skipped_seeds": skipped,
                        "skip_policy": "realisations whose halo masses leave the mass-function splines (the "
                                       "reference's GSL spline aborts there) are skipped and not timed"},
@@ -317,7 +319,7 @@ def accuracy_summary(k, P, seed):
                 np.array_equal(r["count"], ref["count"]) and
                 np.array_equal(r["Mh"].view(np.uint32), ref["Mh"].view(np.uint32)) and
                 np.array_equal(r["flag"].reshape(-1), ref["flag"]))
-    modes = orc.field_modes(p, k, P, stream=1)
+    modes = orc.field_modes(p, k, P, stream=0)
     e_field = _rel_rms(r["grid"], orc.field_real(p, modes))
     lp = orc.lpt_posh(p, k, P, ref["flag"], ref["x"], ref["count"], do_2lpt=1, modes=modes)
     centre = LC * (ref["x"] + 0.5)
@@ -345,6 +347,37 @@ def accuracy_summary(k, P, seed):
                    "field, halo displacements (same labelling), CIC (same positions), P(k) (same grid) and the "
                    "chain's P(k) (FP64 LPT -> CIC -> P(k) on the same catalogue) vs the FP64 oracle; flips vs the "
                    "FP64 ladder of the same modes"}
+
+
+def field_stream_summary(k, P, reps=5):
+    """The 256^3 Gaussian field alone (exh_density_grid_compute, device
+    output) with each random stream: Philox (one counter-based block per
+    mode, generated inside the first transform pass) and the reference's
+    taus stream (deviates drawn in its loop order beforehand, then read by
+    the same pass).  A new seed per call; CUDA events, median of reps."""
+    import torch
+    from exshalos_gb300 import _capi
+    L_ = _capi.load()
+    ctx = _capi.context()
+    out = torch.empty(ND ** 3, dtype=torch.float32, device="cuda")
+    res = {}
+    for name in ("philox", "taus"):
+        times = []
+        for r in range(reps + 2):
+            prm = _capi.default_params(ndx=ND, ndy=ND, ndz=ND, Lc=LC, seed=7000 + r,
+                                       field_stream=_capi.field_stream_code(name))
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            _capi.check(L_.exh_density_grid_compute(ctx, _capi.ptr(k), _capi.ptr(P), k.size, prm, _capi.ptr(out),
+                                                    _capi.EXH_MEM_DEVICE, None))
+            e1.record()
+            torch.cuda.synchronize()
+            if r >= 2:
+                times.append(e0.elapsed_time(e1))
+        res[name + "_ms"] = round(float(np.median(times)), 4)
+    res["workload"] = "field_256: the 256^3 Gaussian field (modes + inverse FFT), device output, new seed per call"
+    return res
 
 
 def batched_summary(k, P, lanes, seed0=0):
@@ -626,6 +659,7 @@ def run_ours(args, ws, rank, local):
     accuracy = None
     if rank == 0 and not args.no_accuracy:
         accuracy = accuracy_summary(k, P, done_seeds[0])
+    fields = field_stream_summary(k, P) if rank == 0 else None
     batched = None if args.no_batched else batched_summary(k, P, args.lanes, seed0=1000 * rank)
     differentiable = None if args.no_batched else diff_summary(k, P)
     galaxies = None if args.no_batched else galaxies_summary(k, P, reps=5, cpu=not args.no_cpu_baseline)
@@ -645,6 +679,8 @@ def run_ours(args, ws, rank, local):
         "config": {"workload": "box_256: nd=256, Lc=2 Mpc/h (L=512), synthetic BBKS P(k) sigma8=0.81, 2LPT, barrier "
                                "a=1 beta=0.12 alpha=0, 50-radius top-hat ladder + crossing map, CIC 256^3 of the halos, "
                                "P(k) 128 bins; new seed per step",
+                   "field_stream": "the reference's (GSL taus seeded with the step's seed): the reference arm's "
+                                   "realisations",
                    "l2": "inputs and intermediates (>1 GB per realisation) exceed L2",
                    "smoothing_ladder": f"{N_RADII} radii, Lc..{R_LADDER} Mpc/h, u8 first-crossing map",
                    "class_timing": "stage_ms_per_step, roofline_by_class and roofline from a second pass of the "
@@ -665,6 +701,7 @@ def run_ours(args, ws, rank, local):
         "clocks": clk,
         "cpu_baseline": cpu,
         "accuracy": accuracy,
+        "field_streams": fields,
         "batched": batched,
         "differentiable": differentiable,
         "galaxies": galaxies,

@@ -21,6 +21,20 @@ EXH_E_NO_DEVICE = 7
 EXH_MEM_HOST = 0
 EXH_MEM_DEVICE = 1
 EXH_FIELD_PHILOX = 1
+EXH_FIELD_TAUS = 2
+FIELD_STREAMS = {"philox": EXH_FIELD_PHILOX, "taus": EXH_FIELD_TAUS}
+
+
+def field_stream_code(name):
+    """EXH_FIELD_* code of a field stream name ("philox", "taus") or code."""
+    if isinstance(name, str):
+        try:
+            return FIELD_STREAMS[name.lower()]
+        except KeyError:
+            raise ValueError(f"unknown field stream {name!r}: 'philox' or 'taus'") from None
+    if int(name) not in FIELD_STREAMS.values():
+        raise ValueError(f"unknown field stream {name!r}")
+    return int(name)
 
 _lib = None
 _lock = threading.Lock()

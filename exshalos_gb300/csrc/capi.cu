@@ -90,6 +90,7 @@ int exh_ctx_destroy(exh_ctx* ctx) {
     cudaStreamDestroy(ctx->c.side);
   }
   for (int i = 0; i < B_COUNT; i++) ctx->c.buf[i].release();
+  if (ctx->c.taus_have_host) cudaFreeHost(ctx->c.taus_have_host);
   diff_state_release(ctx->c);
   halo_state_release(ctx->c);
   delete ctx;

@@ -82,6 +82,8 @@ enum BufId {
   B_HOD,          // galaxy population: per-halo work, stream, tables
   B_HODG,         // galaxy population: the galaxies of the last call
   B_SCRATCH,      // per-block partials, counters
+  B_GAUSS,        // taus field stream: deviates (or phases) in draw order
+  B_TAUS,         // taus field stream: jump matrices, per-chunk counts and scans
   B_HOSTIO,       // staging for host pointers
   B_HOSTIO2,
   B_COUNT
@@ -101,6 +103,13 @@ struct Ctx {
   HostTables tab_cache;
   // device tables reused while their inputs repeat
   std::string amp_key;                  // field amplitudes (B_TAB)
+  std::string taus_key;                 // taus field draws (B_GAUSS): box, seed, fixed
+  const void* taus_jump_at = nullptr;   // B_TAUS address the jump matrices were copied to
+  // accepted pairs of the last taus stream, copied to pinned host memory and
+  // checked against the draws needed at the caller's next synchronisation
+  unsigned* taus_have_host = nullptr;
+  long long taus_need = 0;
+  bool taus_pending = false;
   int shell_ncells = -1, shell_nmin = -1, shell_gmax = 0;   // shell offsets (B_HALO2)
   size_t shell_ncap = 0, shell_nall = 0;
   std::string mass_key;                 // mass-function splines (B_WORK2)

@@ -1,5 +1,6 @@
-// Gaussian field: Philox modes generated inside the first pass of the
-// inverse FFT, scaled by Normx in the last pass (density_grid.c:71-217).
+// Gaussian field: modes (Philox, or the reference's taus stream drawn
+// beforehand) generated inside the first pass of the inverse FFT, scaled by
+// Normx in the last pass (density_grid.c:71-217).
 #include <cmath>
 #include <string>
 #include <vector>
@@ -7,6 +8,7 @@
 #include "ctx.cuh"
 #include "fft4.cuh"
 #include "field.cuh"
+#include "lpt.cuh"
 #include "pipeline.cuh"
 
 namespace exh {
@@ -51,11 +53,23 @@ FieldModes make_modes(const BoxParams& b, const float* A_dev, int fixed, float p
   m.cph = (float)std::cos((double)phase);
   m.sph = (float)std::sin((double)phase);
   m.A = A_dev;
+  m.draws = nullptr;
   return m;
 }
 
-int field_real(Ctx& c, const BoxParams& b, const float* K, const float* P, int Nk, int fixed, float phase,
-               float* delta_dev, cudaStream_t st) {
+int make_field_modes(Ctx& c, const BoxParams& b, const float* A_dev, int stream, int fixed, float phase,
+                     cudaStream_t st, FieldModes* out) {
+  *out = make_modes(b, A_dev, fixed, phase);
+  if (stream == EXH_FIELD_TAUS) {
+    const float* d = nullptr;
+    EXH_TRY(taus_field_draws(c, b, fixed, st, &d));
+    out->draws = d;
+  }
+  return EXH_OK;
+}
+
+int field_real(Ctx& c, const BoxParams& b, const float* K, const float* P, int Nk, int stream, int fixed,
+               float phase, float* delta_dev, cudaStream_t st) {
   FFTPlan3D* p;
   EXH_TRY(c.get_plan(b.nd[0], b.nd[1], b.nd[2], &p));
   float* A_dev = nullptr;
@@ -63,7 +77,8 @@ int field_real(Ctx& c, const BoxParams& b, const float* K, const float* P, int N
   const size_t nk = (size_t)b.nd[0] * b.nd[1] * p->nc;
   EXH_TRY(c.buf[B_WORK].ensure(sizeof(float2) * nk));
   float2* work = c.buf[B_WORK].as<float2>();
-  FieldGen gen{make_modes(b, A_dev, fixed, phase)};
+  FieldGen gen;
+  EXH_TRY(make_field_modes(c, b, A_dev, stream, fixed, phase, st, &gen.m));
   EXH_CUDA_TRY(fft_c2r_3d(*p, gen, work, RealPairStore{delta_dev, b.nd[2], b.Normx}, st));
   return EXH_OK;
 }

@@ -1,14 +1,21 @@
 // Gaussian-field synthesis as a generator for the first pass of the inverse
 // FFT (Compute_Den, src/exshalos/density_grid.c:71-217).
 //
-// Each independent half-complex mode draws one Philox4x32-10 block keyed by
-// (seed, mode index); the Hermitian partners on the kz = 0 and kz = nz/2
-// planes are generated from their source mode and conjugated, following the
-// four copy rules of density_grid.c:109-150.  The amplitude sqrt(P(k)/2) is
-// read from a table indexed by the integer |n|^2 of the mode.  Nothing is
-// stored in k space: consumers regenerate the modes they need.
+// Two random streams:
+//  * Philox (EXH_FIELD_PHILOX): each independent half-complex mode draws one
+//    Philox4x32-10 block keyed by (seed, mode index);
+//  * the reference's own (EXH_FIELD_TAUS): the deviates of its sequential
+//    gsl_rng_taus stream, generated beforehand in loop order
+//    (taus_field.cu), which a mode reads at the index its position in the
+//    reference's loop gives (taus_draw_index).
+// In both, the Hermitian partners on the kz = 0 and kz = nz/2 planes come
+// from their source mode, conjugated, following the four copy rules of
+// density_grid.c:109-150.  The amplitude sqrt(P(k)/2) is read from a table
+// indexed by the integer |n|^2 of the mode.  Nothing is stored in k space:
+// consumers regenerate the modes they need.
 #pragma once
 #include "exh_common.cuh"
+#include "taus_index.h"
 
 namespace exh {
 
@@ -34,6 +41,9 @@ struct FieldModes {
   float cph, sph;              // cos/sin of the constant phase (0, 1 when unused)
   int use_phase;
   const float* __restrict__ A; // sqrt(P/2) by |n|^2
+  // taus stream: the field's deviates (phases with `fixed`) in draw order;
+  // nullptr for the Philox stream
+  const float* __restrict__ draws;
 
   // mode (i, j, k) of the half-complex grid
   __device__ __forceinline__ float2 mode(int i, int j, int k) const {
@@ -50,6 +60,7 @@ struct FieldModes {
     const int kk = (k == n2 / 2) ? n2 / 2 : k;
     const int q2 = ii * ii + jj * jj + kk * kk;
     const float a = A[q2];
+    if (draws) return taus_mode(si, sj, k, a, conj);
     const uint64_t ind = ((uint64_t)si * n1 + sj) * nc + k;
     uint32_t o[4];
     philox4x32_10((uint32_t)ind, (uint32_t)(ind >> 32), 0u, 0u, seed, PHILOX_KEY1, o);
@@ -72,6 +83,36 @@ struct FieldModes {
       else { re = a * (rad * c); im = a * (rad * s); }
     }
     if (use_phase) {   // density_grid.c:189-192, second line reads the rotated real part
+      const float r0 = re * cph - im * sph;
+      im = r0 * sph + im * cph;
+      re = r0;
+    }
+    return conj ? make_float2(re, -im) : make_float2(re, im);
+  }
+
+  // the reference's arithmetic (density_grid.c:169-186): A times the float
+  // deviate in float; the self-conjugate modes sqrt(2.0) A g in double;
+  // `fixed`: A cos(theta), A sin(theta) in double from the float phase
+  __device__ __forceinline__ float2 taus_mode(int si, int sj, int k, float a, bool conj) const {
+    const bool selfc = (si == 0 || si == n0 / 2) && (sj == 0 || sj == n1 / 2) && (k == 0 || k == n2 / 2);
+    const long long d = taus_draw_index(si, sj, k, n0, n1, n2, fixed);
+    float re, im;
+    if (fixed) {
+      if (selfc) { re = __double2float_rn(__dmul_rn(1.4142135623730951, (double)a)); im = 0.f; }
+      else {
+        double sn, cs;
+        sincos((double)draws[d], &sn, &cs);
+        re = __double2float_rn(__dmul_rn((double)a, cs));
+        im = __double2float_rn(__dmul_rn((double)a, sn));
+      }
+    } else if (selfc) {
+      re = __double2float_rn(__dmul_rn(__dmul_rn(1.4142135623730951, (double)a), (double)draws[d]));
+      im = 0.f;
+    } else {
+      re = __fmul_rn(a, draws[d]);
+      im = __fmul_rn(a, draws[d + 1]);
+    }
+    if (use_phase) {
       const float r0 = re * cph - im * sph;
       im = r0 * sph + im * cph;
       re = r0;

@@ -484,7 +484,8 @@ extern "C" int exh_smoothing_ladder(exh_ctx* ctx, const float* k, const float* P
   const std::vector<float>& B = c.ladder_B;
   float* A_dev = nullptr;
   EXH_TRY(upload_amplitudes(c, b, k, P, Nk, &A_dev, st));
-  const FieldModes modes = make_modes(b, A_dev, prm->fixed, prm->phase);
+  FieldModes modes;
+  EXH_TRY(make_field_modes(c, b, A_dev, prm->field_stream, prm->fixed, prm->phase, st, &modes));
   unsigned char* out = reinterpret_cast<unsigned char*>(cross);
   if (mem == EXH_MEM_HOST) {
     EXH_TRY(c.buf[B_CROSS].ensure(b.ng));
@@ -494,6 +495,7 @@ extern "C" int exh_smoothing_ladder(exh_ctx* ctx, const float* k, const float* P
   if (mem == EXH_MEM_HOST) {
     EXH_CUDA_TRY(cudaMemcpyAsync(cross, out, b.ng, cudaMemcpyDeviceToHost, st));
     EXH_CUDA_TRY(cudaStreamSynchronize(st));
+    EXH_TRY(taus_verify(c));
   }
   // a device map is complete when `stream` reaches this point (no host wait)
   for (int i = 0; i < n_radii; i++) {

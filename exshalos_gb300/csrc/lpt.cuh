@@ -29,6 +29,16 @@ int halo_displacements(Ctx& c, const BoxParams& b, const HaloDev& h, const Shell
 int particles(const BoxParams& b, const float* S, const float* V, const HaloOut& o, float* pos, float* vel,
               cudaStream_t st);
 FieldModes make_modes(const BoxParams& b, const float* A_dev, int fixed, float phase);
+// the modes of field stream `stream` (EXH_FIELD_PHILOX or EXH_FIELD_TAUS;
+// the taus stream's draws are generated on `st` first, taus_field.cu)
+int make_field_modes(Ctx& c, const BoxParams& b, const float* A_dev, int stream, int fixed, float phase,
+                     cudaStream_t st, FieldModes* out);
+// the draws of the reference's taus stream for box b and its seed into
+// context memory (*out): deviates, or with `fixed` phases, in draw order
+int taus_field_draws(Ctx& c, const BoxParams& b, int fixed, cudaStream_t st, const float** out);
+// after the stream of the last taus_field_draws has been synchronised: did
+// its stream hold every draw (EXH_E_RANGE if not)
+int taus_verify(Ctx& c);
 int upload_amplitudes(Ctx& c, const BoxParams& b, const float* K, const float* P, int Nk, float** A_dev,
                       cudaStream_t st);
 

@@ -35,7 +35,8 @@ static int check_common(const exh_halo_params* p, const float* k, const float* P
   REQUIRE((p->ndz % 2) == 0, EXH_E_INVALID, "ndz must be even");
   REQUIRE(p->Lc > 0.f && p->Lc < 100.f, EXH_E_INVALID, "cell size Lc must be in (0, 100) Mpc/h");
   REQUIRE(p->R_max >= 100000.f, EXH_E_UNSUPPORTED, "R_max < 1e5 (FFTLog truncation) is not built");
-  REQUIRE(p->field_stream == EXH_FIELD_PHILOX, EXH_E_UNSUPPORTED, "unknown field stream");
+  REQUIRE(p->field_stream == EXH_FIELD_PHILOX || p->field_stream == EXH_FIELD_TAUS, EXH_E_INVALID,
+          "unknown field stream");
   REQUIRE(p->OUT_PROF == 0, EXH_E_UNSUPPORTED, "Lagrangian profiles (OUT_PROF) are not built");
   for (int i = 0; i < Nk; i++) REQUIRE(k[i] > 0.f && P[i] >= 0.f, EXH_E_INVALID, "k must be > 0 and P >= 0");
   return EXH_OK;
@@ -173,7 +174,7 @@ void exh_halo_params_default(exh_halo_params* p) {
   p->beta = 0.f;
   p->alpha = 0.f;
   p->nthreads = 1;
-  p->field_stream = EXH_FIELD_PHILOX;
+  p->field_stream = EXH_FIELD_TAUS;      // the reference's realisation for a seed
   p->setup_fp64 = 0;
 }
 
@@ -192,10 +193,11 @@ int exh_density_grid_compute(exh_ctx* ctx, const float* k, const float* P, int N
     EXH_TRY(c.buf[B_DELTA].ensure(sizeof(float) * b.ng));
     d = c.buf[B_DELTA].as<float>();
   }
-  EXH_TRY(field_real(c, b, k, P, Nk, prm->fixed, prm->phase, d, st));
+  EXH_TRY(field_real(c, b, k, P, Nk, prm->field_stream, prm->fixed, prm->phase, d, st));
   if (mem == EXH_MEM_HOST) {
     EXH_CUDA_TRY(cudaMemcpyAsync(delta, d, sizeof(float) * b.ng, cudaMemcpyDeviceToHost, st));
     EXH_CUDA_TRY(cudaStreamSynchronize(st));
+    EXH_TRY(taus_verify(c));
   }
   return EXH_OK;
 }
@@ -218,11 +220,13 @@ int exh_halos_box_from_pk(exh_ctx* ctx, const float* k, const float* P, int Nk, 
   EXH_TRY(upload_amplitudes(c, b, k, P, Nk, &A_dev, st));
   EXH_TRY(c.buf[B_DELTA].ensure(sizeof(float) * ng));
   float* delta = c.buf[B_DELTA].as<float>();
+  FieldModes modes;
+  EXH_TRY(make_field_modes(c, b, A_dev, prm->field_stream, prm->fixed, prm->phase, st, &modes));
   {
     FFTPlan3D* p;
     EXH_TRY(c.get_plan(b.nd[0], b.nd[1], b.nd[2], &p));
     EXH_TRY(c.buf[B_WORK].ensure(sizeof(float2) * (size_t)b.nd[0] * b.nd[1] * p->nc));
-    FieldGen gen{make_modes(b, A_dev, prm->fixed, prm->phase)};
+    FieldGen gen{modes};
     EXH_CUDA_TRY(fft_c2r_3d(*p, gen, c.buf[B_WORK].as<float2>(), RealPairStore{delta, b.nd[2], b.Normx}, st));
   }
   // LPT (box.c:38-58) depends on the field's modes only: it is enqueued on the
@@ -231,7 +235,6 @@ int exh_halos_box_from_pk(exh_ctx* ctx, const float* k, const float* P, int Nk, 
   // halo sums wait for it.  The two share no buffer.
   cudaStream_t side;
   EXH_TRY(c.fork_stream(st, &side));
-  FieldModes modes = make_modes(b, A_dev, prm->fixed, prm->phase);
   EXH_TRY(c.buf[B_S].ensure(sizeof(float) * 3 * ng));
   EXH_TRY(c.buf[B_PHI1].ensure(sizeof(float) * ng));
   float* S = c.buf[B_S].as<float>();
@@ -255,9 +258,11 @@ int exh_halos_box_from_pk(exh_ctx* ctx, const float* k, const float* P, int Nk, 
   ShellTable t;
   const int hs = run_halo_finder(c, b, k, P, Nk, prm->setup_fp64, delta, &h, &t, st);
   EXH_CUDA_TRY(cudaStreamWaitEvent(st, c.ev_join, 0));
-  if (hs != EXH_OK) {
+  // the halo finder has synchronised the stream: the taus stream's count is in
+  const int tv = taus_verify(c);
+  if (hs != EXH_OK || tv != EXH_OK) {
     EXH_CUDA_TRY(cudaStreamSynchronize(side));      // nothing of this call left running on return
-    return hs;
+    return tv != EXH_OK ? tv : hs;
   }
   const size_t nh = std::max<int64_t>(h.nh, 1);
   EXH_TRY(c.buf[B_POSH].ensure(sizeof(float) * 6 * nh));

@@ -55,7 +55,7 @@ def _fetch_catalogue(nh, ng, want_vel=False, want_grid=False, want_pos=False, wa
 
 def halos_box_from_pk(k, P, R_max, Ndx, Ndy, Ndz, Lc, seed, k_smooth, Om0, redshift, dc, Nmin, a, beta, alpha,
                       fixed, phase, OUT_DEN, OUT_LPT, OUT_VEL, DO_2LPT, OUT_FLAG, OUT_PROF, verbose, nthreads,
-                      _catalogue=False):
+                      _catalogue=False, field_stream="taus"):
     """Halo catalogue from a linear P(k) (exshalos.c:710-940 / box.c:4-68).
 
     Returns the reference's dictionary: "posh", "Mh" always; "velh" with
@@ -63,7 +63,9 @@ def halos_box_from_pk(k, P, R_max, Ndx, Ndy, Ndz, Lc, seed, k_smooth, Om0, redsh
     "grid" with OUT_DEN.  The reference returns an empty dict for a few flag
     combinations it does not list (e.g. OUT_DEN alone); here every requested
     output is returned.  With _catalogue=True the Lagrangian centre cells "x"
-    and member counts "count" are added.
+    and member counts "count" are added.  field_stream: "taus" (default: the
+    reference's own gsl_rng_taus stream, the reference's realisation for this
+    seed) or "philox" (one counter-based block per Fourier mode).
     """
     k = np.ascontiguousarray(k, dtype=np.float32)
     P = np.ascontiguousarray(P, dtype=np.float32)
@@ -73,7 +75,8 @@ def halos_box_from_pk(k, P, R_max, Ndx, Ndy, Ndz, Lc, seed, k_smooth, Om0, redsh
                   k_smooth=float(k_smooth), Om0=float(Om0), redshift=float(redshift), dc=float(dc), Nmin=int(Nmin),
                   a=float(a), beta=float(beta), alpha=float(alpha), fixed=int(fixed), phase=float(phase),
                   OUT_DEN=int(OUT_DEN), OUT_LPT=int(OUT_LPT), OUT_VEL=int(OUT_VEL), DO_2LPT=int(DO_2LPT),
-                  OUT_FLAG=int(OUT_FLAG), OUT_PROF=int(OUT_PROF), verbose=int(verbose), nthreads=int(nthreads))
+                  OUT_FLAG=int(OUT_FLAG), OUT_PROF=int(OUT_PROF), verbose=int(verbose), nthreads=int(nthreads),
+                  field_stream=_capi.field_stream_code(field_stream))
     L = _capi.load()
     import ctypes as C
     nh = C.c_int64(0)
@@ -154,16 +157,18 @@ def find_halos(delta, k, P, Lc, Om0, redshift, dc, Nmin, a, beta, alpha, OUT_FLA
     return out
 
 
-def density_grid_compute(k, P, R_max, Ndx, Ndy, Ndz, Lc, outk, seed, fixed, phase, k_smooth, verbose, nthreads):
+def density_grid_compute(k, P, R_max, Ndx, Ndy, Ndz, Lc, outk, seed, fixed, phase, k_smooth, verbose, nthreads,
+                         field_stream="taus"):
     """Gaussian density grid (exshalos.c:46-121): {"grid"}.  The Fourier
     modes are regenerated where they are needed and are not returned
-    (outk raises NotImplementedError)."""
+    (outk raises NotImplementedError).  field_stream as halos_box_from_pk."""
     if int(outk):
         raise NotImplementedError("returning the Fourier-space grid (outk) is not built")
     k = np.ascontiguousarray(k, dtype=np.float32)
     P = np.ascontiguousarray(P, dtype=np.float32)
     prm = _params(R_max=float(R_max), ndx=int(Ndx), ndy=int(Ndy), ndz=int(Ndz), Lc=float(Lc), seed=int(seed),
-                  fixed=int(fixed), phase=float(phase), k_smooth=float(k_smooth))
+                  fixed=int(fixed), phase=float(phase), k_smooth=float(k_smooth),
+                  field_stream=_capi.field_stream_code(field_stream))
     grid = _capi.host_empty((int(Ndx), int(Ndy), int(Ndz)), np.float32)
     _capi.check(_capi.load().exh_density_grid_compute(_capi.context(), _capi.ptr(k), _capi.ptr(P), k.size, prm,
                                                       _capi.ptr(grid), _capi.EXH_MEM_HOST, None))
@@ -171,7 +176,8 @@ def density_grid_compute(k, P, R_max, Ndx, Ndy, Ndz, Lc, outk, seed, fixed, phas
 
 
 def smoothing_ladder(k, P, R_max, Ndx, Ndy, Ndz, Lc, seed=12345, n_radii=50, Om0=0.31, z=0.0, dc=1.686, a=1.0,
-                     beta=0.0, alpha=0.0, fixed=0, phase=0.0, k_smooth=100000.0, out=None, stream=None):
+                     beta=0.0, alpha=0.0, fixed=0, phase=0.0, k_smooth=100000.0, out=None, stream=None,
+                     field_stream="taus"):
     """First-crossing map of the top-hat smoothing ladder of the Gaussian
     field that density_grid_compute makes with the same arguments.
 
@@ -183,7 +189,8 @@ def smoothing_ladder(k, P, R_max, Ndx, Ndy, Ndz, Lc, seed=12345, n_radii=50, Om0
     P = np.ascontiguousarray(P, dtype=np.float32)
     prm = _params(R_max=float(R_max), ndx=int(Ndx), ndy=int(Ndy), ndz=int(Ndz), Lc=float(Lc), seed=int(seed),
                   Om0=float(Om0), redshift=float(z), dc=float(dc), a=float(a), beta=float(beta), alpha=float(alpha),
-                  fixed=int(fixed), phase=float(phase), k_smooth=float(k_smooth))
+                  fixed=int(fixed), phase=float(phase), k_smooth=float(k_smooth),
+                  field_stream=_capi.field_stream_code(field_stream))
     R = np.zeros(int(n_radii), dtype=np.float32)
     B = np.zeros(int(n_radii), dtype=np.float32)
     if out is None:
@@ -197,11 +204,12 @@ def smoothing_ladder(k, P, R_max, Ndx, Ndy, Ndz, Lc, seed=12345, n_radii=50, Om0
     return {"cross": cross, "R": R, "B": B}
 
 
-def batch_run(k, P, nds, seeds, Lc=2.0, Nk_pk=64, lanes=8, **params):
+def batch_run(k, P, nds, seeds, Lc=2.0, Nk_pk=64, lanes=8, field_stream="philox", **params):
     """Halos and the 64-bin (Nk_pk) CIC power spectrum of the halos for many
-    boxes of uneven size, each from its own Philox seed, scheduled over
-    ``lanes`` streams (1 = the plain loop).  ``params`` are fields of the
-    halo parameters shared by every box (Om0, DO_2LPT, a, beta, ...).
+    boxes of uneven size, each from its own Philox seed (field_stream
+    "taus": the reference's stream instead), scheduled over ``lanes``
+    streams (1 = the plain loop).  ``params`` are fields of the halo
+    parameters shared by every box (Om0, DO_2LPT, a, beta, ...).
 
     Returns {"nh": i64[n], "k": f32[n, Nk_pk], "Pk": f32[n, Nk_pk], "Nk": i64[n, Nk_pk],
     "status": i32[n]}: a box whose halo masses leave the mass-function
@@ -219,7 +227,7 @@ def batch_run(k, P, nds, seeds, Lc=2.0, Nk_pk=64, lanes=8, **params):
     for i in range(n):
         items[i].nd = int(nds[i])
         items[i].seed = int(seeds[i])
-    prm = _params(Lc=float(Lc), **params)
+    prm = _params(Lc=float(Lc), field_stream=_capi.field_stream_code(field_stream), **params)
     out = {"nh": np.zeros(n, dtype=np.int64), "k": np.zeros((n, Nk_pk), dtype=np.float32),
            "Pk": np.zeros((n, Nk_pk), dtype=np.float32), "Nk": np.zeros((n, Nk_pk), dtype=np.int64),
            "status": np.zeros(n, dtype=np.int32)}

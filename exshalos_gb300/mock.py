@@ -39,14 +39,17 @@ def Generate_Halos_Box_from_Pk(
     OUT_FLAG: bool = False,
     verbose: bool = False,
     nthreads: int = 1,
+    field_stream: str = "taus",
 ) -> Dict[str, np.ndarray]:
     """Halo catalogue in a periodic box from a linear power spectrum.
 
     Keys: "posh" (halo positions, Mpc/h), "Mh" (masses, Msun/h), and with the
-    flags "velh", "pos", "vel", "flag", "grid".  The Gaussian field is drawn
-    from a counter-based Philox stream keyed by `seed` (one block per Fourier
-    mode), so a realisation is reproducible and independent of the launch
-    shape; it is not the reference's GSL taus stream.
+    flags "velh", "pos", "vel", "flag", "grid".  field_stream picks the random
+    stream of the Gaussian field: "taus" (default: the reference's
+    gsl_rng_taus stream seeded with `seed`, drawn in its loop order, so the
+    reference's realisation for that seed, up to float rounding of the
+    transforms) or "philox" (a counter-based Philox block per Fourier mode
+    keyed by `seed`).
     """
     precision = _ext.check_precision()
     if precision == 4:
@@ -65,7 +68,7 @@ def Generate_Halos_Box_from_Pk(
         k, P, R_max, np.int32(ndx), np.int32(ndy), np.int32(ndz), Lc, np.int32(seed), k_smooth, Om0, z,
         delta_c, np.int32(Nmin), a, beta, alpha, np.int32(fixed), phase, np.int32(OUT_DEN), np.int32(OUT_LPT),
         np.int32(OUT_VEL), np.int32(DO_2LPT), np.int32(OUT_FLAG), np.int32(OUT_PROF), np.int32(verbose),
-        np.int32(nthreads))
+        np.int32(nthreads), field_stream=field_stream)
 
 
 def Generate_Halos_Box_from_Grid(

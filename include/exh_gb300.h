@@ -40,7 +40,11 @@ extern "C" {
 #define EXH_MEM_DEVICE 1
 
 /* Gaussian-field random streams */
-#define EXH_FIELD_PHILOX 1   /* counter-based Philox4x32-10 per Fourier mode (default) */
+#define EXH_FIELD_PHILOX 1   /* counter-based Philox4x32-10 per Fourier mode (batches) */
+#define EXH_FIELD_TAUS 2     /* the reference's own (default): one gsl_rng_taus stream
+                                seeded with `seed`, Marsaglia polar deviates in its
+                                mode-loop order (src/exshalos/density_grid.c:88-186); the
+                                reference's realisation for a given seed */
 
 typedef struct exh_ctx exh_ctx;
 
@@ -144,7 +148,7 @@ typedef struct {
   float phase;
   int OUT_DEN, OUT_LPT, OUT_VEL, DO_2LPT, OUT_FLAG, OUT_PROF;
   int verbose, nthreads;       /* nthreads is accepted and ignored (one GPU)             */
-  int field_stream;            /* EXH_FIELD_PHILOX                                       */
+  int field_stream;            /* EXH_FIELD_TAUS (default) or EXH_FIELD_PHILOX           */
   int setup_fp64;              /* 1: sigma(M) and mass-function tables in FP64;
                                   0: the reference's float arithmetic                    */
 } exh_halo_params;

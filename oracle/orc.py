@@ -261,7 +261,8 @@ def lpt_posh(p, k, P, flag, hx, hcount, do_2lpt=1, k_smooth=10000.0, stream=1, k
     rt = real_dtype(prec)
     if modes is None:
         modes = field_modes(p, k, P, stream=stream, prec=prec)
-    modes = np.ascontiguousarray(modes, dtype=rt)
+    # orc_lpt1 turns the modes into the potential in place: work on a copy
+    modes = np.array(modes, dtype=rt, order="C", copy=True)
     nh = int(hcount.size)
     ng = int(p.ng)
     flag = np.ascontiguousarray(flag, dtype=np.int64).reshape(-1)

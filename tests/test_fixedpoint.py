@@ -42,3 +42,11 @@ def test_fastdiv_matches_division(tmp_path):
 
 def test_fp32_restatements_match_fp64(tmp_path):
     _run_check(tmp_path, "fp32sum_check")
+
+
+def test_taus_draw_index_matches_the_reference_loop(tmp_path):
+    _run_check(tmp_path, "taus_index_check")
+
+
+def test_taus_chunked_polar_method_matches_sequential(tmp_path):
+    _run_check(tmp_path, "taus_chunk_check")

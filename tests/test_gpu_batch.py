@@ -31,7 +31,7 @@ def test_batch_equals_public_api_chain(pk, plain):
     k, P = pk
     for i in (0, 5, 7):
         nd, L = NDS[i], 2.0 * NDS[i]
-        h = mock.Generate_Halos_Box_from_Pk(k, P, nd=nd, Lc=2.0, seed=SEEDS[i])
+        h = mock.Generate_Halos_Box_from_Pk(k, P, nd=nd, Lc=2.0, seed=SEEDS[i], field_stream="philox")
         assert h["posh"].shape[0] == plain["nh"][i]
         g = simulation.Compute_Density_Grid(h["posh"], nd=nd, L=L, window="CIC")
         p = simulation.Compute_Power_Spectrum(g, L=L, window="CIC", Nk=64, k_min=2 * np.pi / L, k_max=np.pi * nd / L)
@@ -47,7 +47,7 @@ def test_batch_pk_vs_fp64_oracle(orc, pk, plain):
     k, P = pk
     for i in (1, 5):
         nd, L = NDS[i], 2.0 * NDS[i]
-        h = mock.Generate_Halos_Box_from_Pk(k, P, nd=nd, Lc=2.0, seed=SEEDS[i])
+        h = mock.Generate_Halos_Box_from_Pk(k, P, nd=nd, Lc=2.0, seed=SEEDS[i], field_stream="philox")
         g = orc.cic(h["posh"].astype(np.float64), nd, L)
         want = orc.power(g, L, window=2, Nk=64, kmin=2 * np.pi / L, kmax=np.pi * nd / L)
         m = want["Nk"] > 0

@@ -3,7 +3,7 @@ of 512^3 positions, their CIC grid and the 256-bin P(k), checked at full size
 through properties, against the FP64 oracle's P(k) of the same grid, and the
 particle positions (the 512-point passes, among them the 2LPT Poisson x pass
 k_fft8_x_poisson512) against the FP64 oracle's 2LPT (lpt.c:4-242) on the same
-Philox field (GPU)."""
+field stream (the reference's, GPU)."""
 import ctypes as C
 
 import numpy as np
@@ -66,7 +66,7 @@ def test_box512_particles_cic_pk(orc, pk):
     del pos
     p = orc.make_params(nd, Lc, seed=1, a=1.0, beta=0.12, alpha=0.0)
     lp = orc.lpt_posh(p, k, P, np.full(ng, ng, dtype=np.int64), np.zeros((0, 3), np.int32), np.zeros(0, np.int32),
-                      do_2lpt=1, keep_pos=True)
+                      do_2lpt=1, keep_pos=True, stream=0)
     want_pos = lp["pos"].reshape(nd, nd * nd, 3)
     num = den = worst = 0.0
     jk = (np.indices((nd, nd), dtype=np.float64).reshape(2, -1).T + 0.5) * Lc

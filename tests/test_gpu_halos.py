@@ -12,9 +12,12 @@ pytestmark = pytest.mark.gpu
 
 
 def _field(nd, Lc, seed, pk):
+    # the cases below were chosen on Philox fields (the reference's stream has
+    # its own tests, test_gpu_taus_field.py)
     from exshalos_gb300.lib import exshalos
     k, P = pk
-    return exshalos.density_grid_compute(k, P, 1e5, nd, nd, nd, Lc, 0, seed, 0, 0.0, 1e5, 0, 1)["grid"]
+    return exshalos.density_grid_compute(k, P, 1e5, nd, nd, nd, Lc, 0, seed, 0, 0.0, 1e5, 0, 1,
+                                         field_stream="philox")["grid"]
 
 
 def _compare(orc, delta, pk, Lc, Om0=0.31, z=0.0, dc=-1.0, Nmin=1, a=1.0, beta=0.0, alpha=0.0, fp64=0):
@@ -91,7 +94,7 @@ def test_halos_box_from_pk_vs_oracle(orc, pk, do2):
     r = exshalos.halos_box_from_pk(k, P, 1e5, nd, nd, nd, Lc, seed, 1e4, 0.31, 0.0, -1.0, 1, 1.0, 0.0, 0.0, 0, 0.0,
                                    1, 1, 1, do2, 1, 0, 0, 1, _catalogue=True)
     p = orc.make_params(nd, Lc, seed=seed)
-    want_field = orc.field_real(p, orc.field_modes(p, k, P, stream=1))
+    want_field = orc.field_real(p, orc.field_modes(p, k, P, stream=0))
     assert rel_rms(r["grid"], want_field) < 1e-5
     # the catalogue of the GPU field, bit for bit
     tab = orc.sigma_tables(p, k, P)
@@ -101,7 +104,7 @@ def test_halos_box_from_pk_vs_oracle(orc, pk, do2):
     np.testing.assert_array_equal(r["Mh"].view(np.uint32), ref["Mh"].view(np.uint32))
     np.testing.assert_array_equal(r["flag"].reshape(-1), ref["flag"])
     # displacements against the FP64 oracle on the same labelling
-    lp = orc.lpt_posh(p, k, P, ref["flag"], ref["x"], ref["count"], do_2lpt=do2, keep_pos=True)
+    lp = orc.lpt_posh(p, k, P, ref["flag"], ref["x"], ref["count"], do_2lpt=do2, keep_pos=True, stream=0)
     L = nd * Lc
     d = np.abs(r["posh"] - lp["posh"])
     d = np.minimum(d, L - d)

@@ -16,7 +16,7 @@ def test_ladder_matches_fp64_oracle(orc, pk, nd, Lc, n_radii, R_max):
     assert R[0] == pytest.approx(Lc, rel=1e-6) and R[-1] == pytest.approx(R_max, rel=1e-6)
     assert np.all(np.diff(B) <= 0) or n_radii == 1      # barrier falls with the radius
     p = orc.make_params(nd, Lc, seed=seed)
-    want = orc.ladder(p, orc.field_modes(p, k, P, stream=1), R, B)
+    want = orc.ladder(p, orc.field_modes(p, k, P, stream=0), R, B)
     got = r["cross"]
     crossed = np.mean(want != 255)
     assert 0.0 < crossed < 1.0

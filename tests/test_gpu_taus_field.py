@@ -1,0 +1,99 @@
+"""The reference's own field stream on the GPU (EXH_FIELD_TAUS, GPU): one
+gsl_rng_taus stream seeded with the seed, polar-method deviates consumed in
+Compute_Den's loop order (density_grid.c:88-186), against the oracle's
+restatement of that loop (oracle/orc_field.c, stream 0).
+
+* fields (Gaussian, fixed amplitudes, constant phase) within 1e-5 relative
+  rms of the oracle in the reference's float arithmetic and of the FP64
+  oracle (a single deviate read at a wrong index would move the field by
+  ~1e-4 at 64^3);
+* the box_256 workload's seed 8, whose largest halo leaves the mass-function
+  splines: the GPU returns EXH_E_RANGE on the oracle's field exactly where
+  the oracle reports its range error, and on its own taus field; the context
+  keeps working afterwards;
+* the catalogue of a taus-stream box bit-identical to the oracle's on the
+  GPU field, and its halo count within 1e-3 of the oracle's own realisation
+  of the same seed (the two fields differ by transform rounding only);
+* the smoothing ladder on the taus stream against the FP64 ladder.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_rms
+
+pytestmark = pytest.mark.gpu
+
+BAR = dict(a=1.0, beta=0.12, alpha=0.0)
+
+
+@pytest.mark.parametrize("nd,Lc,seed,fixed,phase", [(64, 4.0, 1, 0, 0.0), (32, 2.0, 12345, 0, 0.0),
+                                                     (48, 4.0, 3, 1, 0.0), (64, 4.0, 5, 0, 0.7),
+                                                     (96, 3.0, 0, 0, 0.0), (256, 2.0, 8, 0, 0.0)])
+def test_taus_field_matches_oracle(orc, pk, nd, Lc, seed, fixed, phase):
+    from exshalos_gb300.lib import exshalos
+    k, P = pk
+    got = exshalos.density_grid_compute(k, P, 1e5, nd, nd, nd, Lc, 0, seed, fixed, phase, 1e5, 0, 1,
+                                        field_stream="taus")["grid"]
+    p32 = orc.make_params(nd, Lc, seed=seed, prec="f32")
+    want32 = orc.field_real(p32, orc.field_modes(p32, k, P, stream=0, fixed=fixed, phase=phase, prec="f32"),
+                            prec="f32")
+    p = orc.make_params(nd, Lc, seed=seed)
+    want = orc.field_real(p, orc.field_modes(p, k, P, stream=0, fixed=fixed, phase=phase))
+    e32, e64 = rel_rms(got, want32), rel_rms(got, want)
+    print(f"taus field {nd}^3 seed {seed} fixed {fixed} phase {phase}: vs f32 {e32:.2e}, vs f64 {e64:.2e}")
+    assert e32 < 1e-5 and e64 < 1e-5
+
+
+def test_taus_range_error_where_the_oracle_fails(orc, pk):
+    from exshalos_gb300 import _capi
+    from exshalos_gb300.lib import exshalos
+    k, P = pk
+    nd, Lc, seed = 256, 2.0, 8
+    p = orc.make_params(nd, Lc, seed=seed, prec="f32", **BAR)
+    field = orc.field_real(p, orc.field_modes(p, k, P, stream=0, prec="f32"), prec="f32").astype(np.float32)
+    with pytest.raises(orc.RangeError):
+        orc.find_halos(p, field, orc.sigma_tables(p, k, P, prec="f32"), prec="f32")
+    # the GPU halo finder on the same grid (mass draws seeded 12345 as in the
+    # reference's Find_Halos hook) and the GPU pipeline on its own taus field
+    with pytest.raises(_capi.HaloRangeError):
+        exshalos.find_halos(field, k, P, Lc, 0.31, 0.0, -1.0, 1, BAR["a"], BAR["beta"], BAR["alpha"], 0, 0, 0)
+    args = (k, P, 1e5, nd, nd, nd, Lc, seed, 1e4, 0.31, 0.0, -1.0, 1, BAR["a"], BAR["beta"], BAR["alpha"], 0, 0.0,
+            0, 0, 0, 1, 0, 0, 0, 1)
+    with pytest.raises(_capi.HaloRangeError):
+        exshalos.halos_box_from_pk(*args, field_stream="taus")
+    # the context goes on: the next seed completes
+    args = args[:7] + (1,) + args[8:]
+    r = exshalos.halos_box_from_pk(*args, field_stream="taus")
+    assert r["Mh"].size > 500000 and np.all(np.isfinite(r["posh"]))
+
+
+@pytest.mark.parametrize("nd,Lc,seed", [(64, 4.0, 2), (256, 2.0, 1)])
+def test_taus_box_catalogue(orc, pk, nd, Lc, seed):
+    from exshalos_gb300.lib import exshalos
+    k, P = pk
+    r = exshalos.halos_box_from_pk(k, P, 1e5, nd, nd, nd, Lc, seed, 1e4, 0.31, 0.0, -1.0, 1, BAR["a"], BAR["beta"],
+                                   BAR["alpha"], 0, 0.0, 1, 0, 0, 1, 1, 0, 0, 1, _catalogue=True,
+                                   field_stream="taus")
+    r = {key: np.array(v) for key, v in r.items()}
+    p = orc.make_params(nd, Lc, seed=seed, **BAR)
+    ref = orc.find_halos(p, r["grid"], orc.sigma_tables(p, k, P))
+    np.testing.assert_array_equal(r["x"], ref["x"])
+    np.testing.assert_array_equal(r["count"], ref["count"])
+    np.testing.assert_array_equal(r["Mh"].view(np.uint32), ref["Mh"].view(np.uint32))
+    np.testing.assert_array_equal(r["flag"].reshape(-1), ref["flag"])
+    own = orc.halos_box_from_pk(k, P, nd=nd, Lc=Lc, seed=seed, stream=0, do_2lpt=1, prec="f32", **BAR)
+    print(f"taus box {nd}^3 seed {seed}: {ref['nh']} halos on the GPU field, {own['nh']} in the oracle's own "
+          f"realisation; field vs oracle {rel_rms(r['grid'], own['delta']):.2e}")
+    assert rel_rms(r["grid"], own["delta"]) < 1e-5
+    assert abs(int(ref["nh"]) - int(own["nh"])) <= 1e-3 * own["nh"]
+
+
+def test_taus_ladder_matches_fp64(orc, pk):
+    from exshalos_gb300.lib import exshalos as ex
+    k, P = pk
+    nd, Lc, seed = 64, 4.0, 31
+    r = ex.smoothing_ladder(k, P, 40.0, nd, nd, nd, Lc, seed=seed, n_radii=20, field_stream="taus", **BAR)
+    p = orc.make_params(nd, Lc, seed=seed)
+    want = orc.ladder(p, orc.field_modes(p, k, P, stream=0), r["R"], r["B"])
+    assert 0.0 < np.mean(want != 255) < 1.0
+    assert np.mean(r["cross"] != want) < 1e-3
