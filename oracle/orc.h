@@ -14,10 +14,13 @@
  * The halo finder (peaks, quicksort, sphere growth, masses) always runs in the
  * reference's types (float density, double sums) in both builds.
  *
- * Parity status: the FFTW and GSL arithmetic the reference links against is
- * absent from this tree and from the build image.  The GSL pieces (taus
- * generator, polar Gaussian, natural cubic spline) are restated from their
- * published algorithms; their bit-equality with a real GSL build is unpinned.
+ * Parity status: the reference's own C for this path is compiled unmodified
+ * from its tree (oracle/ref_build.py) against stand-ins for the FFTW3 and GSL
+ * entry points it calls, which use this oracle's FFT, taus stream, polar
+ * Gaussian and spline; every stage of this restatement equals it bit for bit
+ * (tests/test_oracle_ref.py).  What stays unpinned is FFTW's and GSL's own
+ * arithmetic (both absent from the build image): the GSL pieces are restated
+ * from their published algorithms and the FFT is a mixed-radix Stockham.
  * The sphere table (CELLS_IN_SPHERES) is pinned against the reference's own
  * table (tests/golden/cells_in_spheres.txt).
  */
