@@ -81,6 +81,17 @@ def max_over_ranks(x, ws):
     return float(t.item())
 
 
+def sum_over_ranks(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def aggregate_value(ws, steps, t_max):
     """Whole-job realisations per second: every rank runs `steps` of its own
     realisations, the job takes the slowest rank's time."""
@@ -380,36 +391,47 @@ def field_stream_summary(k, P, reps=5):
     return res
 
 
-def batched_summary(k, P, lanes, seed0=0):
-    """Batched workload: 256 realisations with Philox seeds seed0..seed0+255
-    and box sizes drawn uniformly from {64, 96, 128, 192, 256} (fixed draw),
-    cell size 2 Mpc/h, halos (2LPT, barrier a=1 beta=0.12 alpha=0) and the
-    64-bin CIC P(k) of each; the lanes runner against the plain loop (one
-    lane) on the same items.  Throughput in 256^3 equivalents (sum nd^3 / 256^3)."""
+def batched_summary(k, P, lanes, ws=1, rank=0):
+    """Batched workload: 256 realisations with Philox seeds 0..255 and box
+    sizes drawn uniformly from {64, 96, 128, 192, 256} (fixed draw), cell
+    size 2 Mpc/h, halos (2LPT, barrier a=1 beta=0.12 alpha=0) and the 64-bin
+    CIC P(k) of each; the lanes runner against the plain loop (one lane) on
+    the same items.  Throughput in 256^3 equivalents (sum nd^3 / 256^3).
+    With several ranks the box list is split by cell-count-balanced greedy
+    bin packing (exshalos_gb300.shard), each rank runs its share on its own
+    GPU and the slowest rank's time counts (weak scaling of the list)."""
     import torch
+    from exshalos_gb300 import shard
     from exshalos_gb300.lib import exshalos as exl
     rng = np.random.default_rng(2024)
-    nds = rng.choice([64, 96, 128, 192, 256], size=256)
-    seeds = np.arange(seed0, seed0 + 256)
-    eq = float(np.sum(nds.astype(np.float64) ** 3) / 256.0 ** 3)
+    nds_all = rng.choice([64, 96, 128, 192, 256], size=256)
+    seeds_all = np.arange(256)
+    parts, loads = shard.partition(nds_all, ws)
+    mine = np.asarray(parts[rank], dtype=np.int64)
+    nds, seeds = nds_all[mine], seeds_all[mine]
+    eq = float(np.sum(nds_all.astype(np.float64) ** 3) / 256.0 ** 3)
     kw = dict(Lc=LC, Nk_pk=64, DO_2LPT=1, **BARRIER)
     exl.batch_run(k, P, nds, seeds + 1000, lanes=lanes, **kw)       # warm-up: buffers and plans of every lane
     exl.batch_run(k, P, nds[:8], seeds[:8] + 2000, lanes=1, **kw)
     out = {}
     res = {}
     for name, nl in (("plain", 1), ("batched", lanes)):
+        barrier(ws)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         res[name] = exl.batch_run(k, P, nds, seeds, lanes=nl, **kw)
         torch.cuda.synchronize()
-        out[name] = eq / (time.perf_counter() - t0)
+        out[name] = eq / max_over_ranks(time.perf_counter() - t0, ws)
     same = all(np.array_equal(res["plain"][x], res["batched"][x]) for x in ("nh", "Pk", "Nk", "status"))
+    same = max_over_ranks(0.0 if same else 1.0, ws) == 0.0
+    failed = int(sum_over_ranks(float((res["batched"]["status"] != 0).sum()), ws))
     return {"workload": "batch_256: 256 boxes, nd ~ U{64,96,128,192,256} (seeded draw), Lc=2, Philox seeds 0..255, "
                         "2LPT, barrier a=1 beta=0.12, halos + CIC + 64-bin P(k) each",
             "unit": "256^3-equivalent realisations/s", "equivalents": round(eq, 3), "lanes": lanes,
             "value": out["batched"], "plain_loop_value": out["plain"], "speedup_vs_plain": out["batched"] / out["plain"],
-            "identical_to_plain": bool(same), "failed_items": int((res["batched"]["status"] != 0).sum()),
-            "timing": "host wall clock around the synchronous batch call"}
+            "identical_to_plain": bool(same), "failed_items": failed,
+            "ranks": ws, "cells_per_rank": loads,
+            "timing": "host wall clock around the synchronous batch call, slowest rank"}
 
 
 def diff_summary(k, P, reps=3):
@@ -660,7 +682,7 @@ def run_ours(args, ws, rank, local):
     if rank == 0 and not args.no_accuracy:
         accuracy = accuracy_summary(k, P, done_seeds[0])
     fields = field_stream_summary(k, P) if rank == 0 else None
-    batched = None if args.no_batched else batched_summary(k, P, args.lanes, seed0=1000 * rank)
+    batched = None if args.no_batched else batched_summary(k, P, args.lanes, ws=ws, rank=rank)
     differentiable = None if args.no_batched else diff_summary(k, P)
     galaxies = None if args.no_batched else galaxies_summary(k, P, reps=5, cpu=not args.no_cpu_baseline)
     if rank != 0:
