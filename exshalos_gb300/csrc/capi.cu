@@ -84,6 +84,13 @@ int exh_ctx_destroy(exh_ctx* ctx) {
   }
   for (auto& kv : ctx->c.plans) fft_plan_destroy(&kv.second);
   if (ctx->c.ladder_graph) cudaGraphExecDestroy(ctx->c.ladder_graph);
+  if (ctx->c.sort_graph) cudaGraphExecDestroy(ctx->c.sort_graph);
+  if (ctx->c.sort_graph_src) cudaGraphDestroy(ctx->c.sort_graph_src);
+  for (auto& e : ctx->c.grow_graphs) {
+    cudaGraphExecDestroy(e.exec);
+    cudaGraphDestroy(e.src);
+  }
+  if (ctx->c.capture) cudaStreamDestroy(ctx->c.capture);
   if (ctx->c.side) {
     cudaEventDestroy(ctx->c.ev_fork);
     cudaEventDestroy(ctx->c.ev_join);

@@ -1,6 +1,7 @@
 // Library context: cached FFT plans, device work buffers and the results of
 // the last halo call.  One context per host thread.
 #pragma once
+#include <functional>
 #include <map>
 #include <tuple>
 #include <vector>
@@ -117,6 +118,20 @@ struct Ctx {
   std::string ladder_tab_key;           // ladder radii and barriers (host)
   std::string ladder_seen_key, ladder_graph_key;
   cudaGraphExec_t ladder_graph = nullptr;   // captured radius loop
+  // the halo finder's level loop (sort) and round loop (growth) as graphs
+  // whose while node the kernels end on the device; rebuilt when their
+  // arguments change
+  cudaGraph_t sort_graph_src = nullptr;
+  cudaGraphExec_t sort_graph = nullptr;
+  std::string sort_graph_key;
+  struct GraphEntry {
+    std::string key;
+    cudaGraph_t src = nullptr;
+    cudaGraphExec_t exec = nullptr;
+  };
+  std::vector<GraphEntry> grow_graphs;
+  cudaStream_t capture = nullptr;           // stream used only to capture graph bodies
+  int capture_stream(cudaStream_t* out);
   std::vector<float> ladder_R, ladder_B;
   // sorted peaks of the last grid given to exh_find_halos (B_PEAKS2), by digest
   unsigned long long peak_hash = 0;
@@ -145,6 +160,13 @@ struct Ctx {
 };
 
 void diff_state_release(Ctx& c);
+
+// A graph of one while node.  `body` enqueues the loop body on the stream it
+// is given (captured into the node's body graph); its kernels end the loop
+// with cudaGraphSetConditional(handle, 0).  The condition is 1 at every
+// launch, so the body runs at least once.
+int build_while_graph(Ctx& c, const std::function<int(cudaStream_t, cudaGraphConditionalHandle)>& body,
+                      cudaGraph_t* src_out, cudaGraphExec_t* exec_out);
 
 }  // namespace exh
 

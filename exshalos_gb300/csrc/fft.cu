@@ -78,6 +78,53 @@ void fft_plan_destroy(FFTPlan3D* p) {
   p->twx = p->twy = p->twm = p->twn = nullptr;
 }
 
+int Ctx::capture_stream(cudaStream_t* out) {
+  if (!capture) EXH_CUDA_TRY(cudaStreamCreateWithFlags(&capture, cudaStreamNonBlocking));
+  *out = capture;
+  return EXH_OK;
+}
+
+int build_while_graph(Ctx& c, const std::function<int(cudaStream_t, cudaGraphConditionalHandle)>& body,
+                      cudaGraph_t* src_out, cudaGraphExec_t* exec_out) {
+  cudaStream_t cs;
+  EXH_TRY(c.capture_stream(&cs));
+  cudaGraph_t g = nullptr;
+  EXH_CUDA_TRY(cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle h;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+  cudaGraphNodeParams np{};
+  cudaGraphNode_t node;
+  if (e == cudaSuccess) {
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+  }
+  if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(cs, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                          cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    exh_set_error_msg(cudaGetErrorString(e), __FILE__, __LINE__);
+    return EXH_E_CUDA;
+  }
+  const int bs = body(cs, h);
+  cudaGraph_t captured = nullptr;
+  e = cudaStreamEndCapture(cs, &captured);
+  cudaGraphExec_t ex = nullptr;
+  if (bs == EXH_OK && e == cudaSuccess) e = cudaGraphInstantiate(&ex, g, 0);
+  if (bs != EXH_OK || e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (bs != EXH_OK) return bs;
+    exh_set_error_msg(cudaGetErrorString(e), __FILE__, __LINE__);
+    return EXH_E_CUDA;
+  }
+  *src_out = g;
+  *exec_out = ex;
+  return EXH_OK;
+}
+
 int Ctx::side_stream(cudaStream_t* out) {
   if (!side) {
     EXH_CUDA_TRY(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));

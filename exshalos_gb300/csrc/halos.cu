@@ -225,6 +225,12 @@ k_peak_write(const float* __restrict__ d, size_t ng, unsigned ngroups, const uns
   }
 }
 
+// peaks the B_PEAKS buffer holds: its sets of keys and cell ids are laid out
+// by the allocation's capacity, not the peak count, so buffer addresses
+// (and the sort's captured graph) stay the same from one realisation to the
+// next while the buffer does not grow
+size_t peak_cap(const Ctx& c) { return c.buf[B_PEAKS].cap / ((sizeof(float) + sizeof(unsigned)) * 3); }
+
 int find_peaks(Ctx& c, const float* delta, const BoxParams& b, HaloDev* h, cudaStream_t st) {
   const size_t ng = b.ng;
   const unsigned nb = exh_div_up(ng, PK_T);
@@ -253,8 +259,8 @@ int find_peaks(Ctx& c, const float* delta, const BoxParams& b, HaloDev* h, cudaS
   EXH_CUDA_TRY(cudaMemcpyAsync(&np, total, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
   EXH_CUDA_TRY(cudaStreamSynchronize(st));
   h->np = np;
-  const size_t cap = std::max<size_t>(np, 1);
-  EXH_TRY(c.buf[B_PEAKS].ensure((sizeof(float) + sizeof(unsigned)) * cap * 3));
+  EXH_TRY(c.buf[B_PEAKS].ensure((sizeof(float) + sizeof(unsigned)) * std::max<size_t>(np, 1) * 3));
+  const size_t cap = peak_cap(c);
   h->key = c.buf[B_PEAKS].as<float>();
   h->id = reinterpret_cast<unsigned*>(h->key + cap);
   { KTimer kt(KC_PEAKS, st, ng / 8.0 + 12.0 * np);
@@ -470,6 +476,7 @@ k_qs_jump(const Seg* __restrict__ segs, const int* __restrict__ cseg, const int*
 // level bookkeeping on the device: counters of the level loop
 struct SortCtl {
   int nseg, nch, nnext, nsmall, nsingle, err;
+  int iters;                   // iterations of the graph's level loop
   unsigned long long elems;    // elements partitioned by the level kernels (timing)
 };
 
@@ -505,11 +512,17 @@ __global__ void k_qs_children(const Seg* __restrict__ segs, const int* __restric
   }
 }
 
-// next level's segment list and chunk tables (one block)
+// next level's segment list and chunk tables (one block).  Inside the level
+// loop's graph (cond_on), the last level of the loop body also decides
+// whether the loop goes on: while large segments remain, no list
+// overflowed, and at most SORT_ITERS_PER_LAUNCH iterations per launch (the
+// host then launches the graph again).
 constexpr int QS_CHUNK_T = 1024;
+constexpr int SORT_ITERS_PER_LAUNCH = 64;
 __global__ void __launch_bounds__(QS_CHUNK_T)
 k_qs_chunks(SortCtl* ctl, const Seg* __restrict__ next, Seg* __restrict__ segs, int* __restrict__ cfirst,
-            int* __restrict__ cseg, int* __restrict__ coff, int cap_chunks) {
+            int* __restrict__ cseg, int* __restrict__ coff, int cap_chunks, cudaGraphConditionalHandle cond,
+            int cond_on) {
   __shared__ int ws[32];
   __shared__ int carry;
   const int nseg = ctl->nnext;
@@ -543,6 +556,10 @@ k_qs_chunks(SortCtl* ctl, const Seg* __restrict__ next, Seg* __restrict__ segs, 
     ctl->nseg = nseg;
     ctl->nch = min(carry, cap_chunks);
     ctl->nnext = 0;
+    if (cond_on) {
+      const int it = ++ctl->iters;
+      cudaGraphSetConditional(cond, (nseg > 0 && ctl->err == 0 && it % SORT_ITERS_PER_LAUNCH != 0) ? 1u : 0u);
+    }
   }
 }
 
@@ -767,16 +784,15 @@ k_qs_small(const Seg* __restrict__ segs, int nseg, SmallSortBuffers bufs, float*
 }
 int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
   const int np = (int)h->np;
-  const size_t cap = std::max<size_t>(np, 1);
+  const size_t cap = peak_cap(c);          // find_peaks laid the keys out by this capacity
   float* k0 = h->key;
   unsigned* i0 = h->id;
   float* k1 = reinterpret_cast<float*>(i0 + cap);
   unsigned* i1 = reinterpret_cast<unsigned*>(k1 + cap);
-  float* fk = reinterpret_cast<float*>(i1 + cap);
   // final arrays live in B_PEAKS2
   EXH_TRY(c.buf[B_PEAKS2].ensure((sizeof(float) + sizeof(unsigned)) * cap + sizeof(int) * (cap + 1) +
-                                  sizeof(int2) * cap + sizeof(int) * cap));
-  fk = c.buf[B_PEAKS2].as<float>();
+                                  sizeof(int2) * cap + sizeof(int) * cap + 16));
+  float* fk = c.buf[B_PEAKS2].as<float>();
   unsigned* fi = reinterpret_cast<unsigned*>(fk + cap);
   int* lam = reinterpret_cast<int*>(fi + cap);
   int2* chain = reinterpret_cast<int2*>(lam + cap + (cap & 1));     // 8-byte aligned
@@ -793,11 +809,11 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
   float* kb[2] = {k0, k1};
   unsigned* ib[2] = {i0, i1};
   // device-side level loop: segment lists, chunk tables and counters live
-  // on the device; the host launches levels and reads the counters back
-  // every few levels only
-  const int max_segs = np / SORT_SMALL + 8;
-  const int max_chunks = np / CH + max_segs + 8;
-  const int cap_small = np / 2 + 8;
+  // on the device, sized by the capacity
+  const int ncap = (int)std::min<size_t>(cap, (size_t)1 << 30);
+  const int max_segs = ncap / SORT_SMALL + 8;
+  const int max_chunks = ncap / CH + max_segs + 8;
+  const int cap_small = ncap / 2 + 8;
   const size_t need = sizeof(SortCtl) + sizeof(Seg) * (2 * (size_t)max_segs + cap_small) +
                       sizeof(int2) * (size_t)cap_small +
                       sizeof(int) * (3 * (size_t)max_chunks + 2 * (size_t)max_segs + 8) + 64;
@@ -818,48 +834,96 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
   EXH_TRY(upload_small(np > SORT_SMALL ? d_next : d_small, &whole, sizeof(Seg), st));
   EXH_TRY(upload_small(ctl, &h0, sizeof(SortCtl), st));
   SortCtl hc = h0;
+  // one level: the large segments of buffer `buf` are partitioned into the
+  // other buffer (or, finished, into the final arrays)
+  auto level = [&](int buf, cudaStream_t s, cudaGraphConditionalHandle cond, int cond_on) -> int {
+    k_qs_count<<<max_chunks, CH_T, 0, s>>>(kb[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL);
+    k_qs_seg_scan<<<max_segs, 256, 0, s>>>(d_cfirst, &ctl->nseg, d_cL, d_nl);
+    k_qs_place<1><<<max_chunks, CH_T, 0, s>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL, d_nl, lam,
+                                              chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi, j2);
+    k_qs_place<3><<<max_chunks, CH_T, 0, s>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL, d_nl, lam,
+                                              chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi, j2);
+    k_qs_jump<<<max_chunks, CH_T, 0, s>>>(d_segs, d_cseg, d_coff, &ctl->nch, d_nl, chain, j2);
+    k_qs_place<2><<<max_chunks, CH_T, 0, s>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL, d_nl, lam,
+                                              chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi, j2);
+    k_qs_children<<<exh_div_up(max_segs, 128), 128, 0, s>>>(d_segs, d_nl, ctl, d_next, d_small, d_single, max_segs,
+                                                            cap_small);
+    k_qs_chunks<<<1, QS_CHUNK_T, 0, s>>>(ctl, d_next, d_segs, d_cfirst, d_cseg, d_coff, max_chunks, cond, cond_on);
+    EXH_CUDA_TRY(cudaGetLastError());
+    return EXH_OK;
+  };
   if (np > SORT_SMALL) {
-    k_qs_chunks<<<1, QS_CHUNK_T, 0, st>>>(ctl, d_next, d_segs, d_cfirst, d_cseg, d_coff, max_chunks);
+    k_qs_chunks<<<1, QS_CHUNK_T, 0, st>>>(ctl, d_next, d_segs, d_cfirst, d_cseg, d_coff, max_chunks, 0, 0);
     count_launch(1);
-    constexpr int LEVELS_PER_CHECK = 4;
-    // the level loop is one timed unit; its algorithmic bytes are one read
-    // and one write of key and id (16 B) per element partitioned
-    KTimer kt(KC_SORT, st, 0.0);
-    for (int level = 0;; level++) {
-      const int buf = level & 1;       // every large segment of a level sits in the same buffer
-      {
-        k_qs_count<<<max_chunks, CH_T, 0, st>>>(kb[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL);
-        k_qs_seg_scan<<<max_segs, 256, 0, st>>>(d_cfirst, &ctl->nseg, d_cL, d_nl);
-        k_qs_place<1><<<max_chunks, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL, d_nl,
-                                                   lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi, j2);
-        k_qs_place<3><<<max_chunks, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL, d_nl,
-                                                   lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi, j2);
-        k_qs_jump<<<max_chunks, CH_T, 0, st>>>(d_segs, d_cseg, d_coff, &ctl->nch, d_nl, chain, j2);
-        k_qs_place<2><<<max_chunks, CH_T, 0, st>>>(kb[buf], ib[buf], d_segs, d_cseg, d_coff, &ctl->nch, d_cL, d_nl,
-                                                   lam, chain, kb[buf ^ 1], ib[buf ^ 1], fk, fi, j2);
-        k_qs_children<<<exh_div_up(max_segs, 128), 128, 0, st>>>(d_segs, d_nl, ctl, d_next, d_small, d_single,
-                                                                 max_segs, cap_small);
-        k_qs_chunks<<<1, QS_CHUNK_T, 0, st>>>(ctl, d_next, d_segs, d_cfirst, d_cseg, d_coff, max_chunks);
+    if (timing_on()) {
+      // kernel-class timing: the levels launched one by one, the host checks
+      // the counters every few levels; the level loop is one timed unit whose
+      // algorithmic bytes are one read and one write of key and id (16 B) per
+      // element partitioned
+      constexpr int LEVELS_PER_CHECK = 4;
+      KTimer kt(KC_SORT, st, 0.0);
+      for (int lv = 0;; lv++) {
+        EXH_TRY(level(lv & 1, st, 0, 0));
         count_launch(8);
-        EXH_CUDA_TRY(cudaGetLastError());
+        if ((lv + 1) % LEVELS_PER_CHECK == 0) {
+          EXH_CUDA_TRY(cudaMemcpyAsync(&hc, ctl, sizeof(SortCtl), cudaMemcpyDeviceToHost, st));
+          EXH_CUDA_TRY(cudaStreamSynchronize(st));
+          if (hc.err) break;
+          if (hc.nseg == 0) {
+            kt.bytes = 16.0 * (double)hc.elems;
+            break;
+          }
+        }
+        if (lv > np) break;
       }
-      if ((level + 1) % LEVELS_PER_CHECK == 0) {
+    } else {
+      // the level loop as a graph: a while node over two levels (even and
+      // odd buffer) that the last kernel ends on the device; captured once
+      // per set of buffers and sizes, launched again only when it stopped at
+      // its iteration cap
+      std::string key;
+      const void* ptrs[16] = {k0, i0, k1, i1, fk, fi, lam, chain, j2, ctl, d_segs, d_next, d_small, d_single, d_cseg,
+                              d_cL};
+      const int sizes[4] = {max_segs, max_chunks, cap_small, SORT_ITERS_PER_LAUNCH};
+      key.append(reinterpret_cast<const char*>(ptrs), sizeof(ptrs));
+      key.append(reinterpret_cast<const char*>(sizes), sizeof(sizes));
+      if (!c.sort_graph || key != c.sort_graph_key) {
+        if (c.sort_graph) cudaGraphExecDestroy(c.sort_graph);
+        if (c.sort_graph_src) cudaGraphDestroy(c.sort_graph_src);
+        c.sort_graph = nullptr;
+        c.sort_graph_src = nullptr;
+        c.sort_graph_key.clear();
+        EXH_TRY(build_while_graph(
+            c,
+            [&](cudaStream_t s, cudaGraphConditionalHandle h) -> int {
+              EXH_TRY(level(0, s, h, 0));
+              return level(1, s, h, 1);
+            },
+            &c.sort_graph_src, &c.sort_graph));
+        c.sort_graph_key = key;
+      }
+      int done_iters = 0;
+      for (int launch = 0;; launch++) {
+        EXH_CUDA_TRY(cudaGraphLaunch(c.sort_graph, st));
         EXH_CUDA_TRY(cudaMemcpyAsync(&hc, ctl, sizeof(SortCtl), cudaMemcpyDeviceToHost, st));
         EXH_CUDA_TRY(cudaStreamSynchronize(st));
-        if (c.verbose) { printf("  sort level %d: %d large, %d small, %d single\n", level, hc.nseg, hc.nsmall, hc.nsingle); fflush(stdout); }
-        if (hc.err) {
-          exh_set_error_msg("peak sort: segment lists overflowed", __FILE__, __LINE__);
-          return EXH_E_RANGE;
-        }
-        if (hc.nseg == 0) {
-          kt.bytes = 16.0 * (double)hc.elems;
-          break;
-        }
+        count_launch(16 * (hc.iters - done_iters));
+        done_iters = hc.iters;
+        if (hc.err || hc.nseg == 0) break;
+        if ((size_t)launch * 2 * SORT_ITERS_PER_LAUNCH > (size_t)np + 4) break;
       }
-      if (level > np) {
-        exh_set_error_msg("peak sort made no progress", __FILE__, __LINE__);
-        return EXH_E_TIMEOUT;
-      }
+    }
+    if (c.verbose) {
+      printf("  sort levels done: %d small segments, %d single\n", hc.nsmall, hc.nsingle);
+      fflush(stdout);
+    }
+    if (hc.err) {
+      exh_set_error_msg("peak sort: segment lists overflowed", __FILE__, __LINE__);
+      return EXH_E_RANGE;
+    }
+    if (hc.nseg != 0) {
+      exh_set_error_msg("peak sort made no progress", __FILE__, __LINE__);
+      return EXH_E_TIMEOUT;
     }
   }
   SortBufs sb{{kb[0], kb[1]}, {ib[0], ib[1]}};
@@ -895,8 +959,6 @@ struct GrowArgs {
   const float* delta;
   const float* key;        // sorted peaks (ascending)
   const unsigned* id;
-  int64_t np;
-  int nproc;
   HaloScalars hs;
   const float* Btab;
   ShellTable t;
@@ -1199,7 +1261,10 @@ struct RoundArgs {
   int* flag;
   unsigned* resv;
   unsigned* claimed;   // one bit per cell: flag != FLAG_FREE
-  int tag;
+  // device words: the round's reservation tag and the number of peaks (so
+  // that the arguments, and a captured round loop, do not change with them)
+  const int* tag;
+  const long long* np;
   int* cnt;
   int* gtmp;
   int* gexit;
@@ -1234,7 +1299,7 @@ k_tentative(GrowArgs A, const int* __restrict__ list, const int* __restrict__ nl
   const int stride = (int)(gridDim.x * blockDim.x);
   for (int t = (int)(blockIdx.x * (size_t)blockDim.x + threadIdx.x); t < n; t += stride) {
     const int r = list[t];
-    const int64_t l = A.np - 1 - r;
+    const int64_t l = *R.np - 1 - r;
     const unsigned cell0 = A.id[l];
     if (cell_claimed(R.claimed, cell0)) {    // find_halos.c:233: the peak is already inside a halo
       R.state[r] = 1;
@@ -1252,7 +1317,7 @@ k_tentative(GrowArgs A, const int* __restrict__ list, const int* __restrict__ nl
     }
     R.cnt[r] = count; R.gtmp[r] = gt; R.gexit[r] = ge; R.gst[r] = st;
     if (R.nwords) R.nwords[r] += tentative_words(A, ge);
-    const unsigned key = resv_key(R.tag, r);
+    const unsigned key = resv_key(*R.tag, r);
     const int e = A.t.start_all[ge];          // cells it may flag: r^2 < gexit
     for (int q = 0; q < e; q++) {
       unsigned* pr = &R.resv[cell_at(x, y, z, A.t.off_all[q], A.hs)];
@@ -1270,7 +1335,7 @@ k_tentative_warp(GrowArgs A, RoundArgs R) {
   const int n = *R.nw;
   for (int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5); w < n; w += nwarps) {
     const int r = R.wlist[w];
-    const int64_t l = A.np - 1 - r;
+    const int64_t l = *R.np - 1 - r;
     const unsigned cell0 = A.id[l];
     int x, y, z;
     peak_coords(cell0, A.hs, x, y, z);
@@ -1279,7 +1344,7 @@ k_tentative_warp(GrowArgs A, RoundArgs R) {
     if (st == 3) st = grow_warp(A, R.claimed, x, y, z, A.key[l], lane, wb[threadIdx.x >> 5], count, gt, ge);
     if (lane == 0) { R.cnt[r] = count; R.gtmp[r] = gt; R.gexit[r] = ge; R.gst[r] = st; }
     if (lane == 0 && R.nwords) R.nwords[r] += tentative_words(A, ge);
-    const unsigned key = resv_key(R.tag, r);
+    const unsigned key = resv_key(*R.tag, r);
     const int e = A.t.start_all[ge];
     for (int q = lane; q < e; q += 32) {
       unsigned* pr = &R.resv[cell_at(x, y, z, A.t.off_all[q], A.hs)];
@@ -1320,10 +1385,10 @@ k_commit(GrowArgs A, const int* __restrict__ list, const int* __restrict__ nlist
       list_push(R.clist, R.nc, r);
       continue;
     }
-    const unsigned cell0 = A.id[A.np - 1 - r];
+    const unsigned cell0 = A.id[*R.np - 1 - r];
     int x, y, z;
     peak_coords(cell0, A.hs, x, y, z);
-    const unsigned key = resv_key(R.tag, r);
+    const unsigned key = resv_key(*R.tag, r);
     bool mine = true;
     for (int q = 0; q < e && mine; q++) mine = R.resv[cell_at(x, y, z, A.t.off_all[q], A.hs)] <= key;
     if (R.nwords) R.nwords[r] += (unsigned)e;
@@ -1352,10 +1417,10 @@ k_commit_warp(GrowArgs A, RoundArgs R) {
   const int n = *R.nc;
   for (int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5); w < n; w += nwarps) {
     const int r = R.clist[w];
-    const unsigned cell0 = A.id[A.np - 1 - r];
+    const unsigned cell0 = A.id[*R.np - 1 - r];
     int x, y, z;
     peak_coords(cell0, A.hs, x, y, z);
-    const unsigned key = resv_key(R.tag, r);
+    const unsigned key = resv_key(*R.tag, r);
     const int e = A.t.start_all[R.gexit[r] + 1];
     bool mine = true;
     for (int q = lane; q < e && mine; q += 32) mine = R.resv[cell_at(x, y, z, A.t.off_all[q], A.hs)] <= key;
@@ -1380,6 +1445,31 @@ k_commit_warp(GrowArgs A, RoundArgs R) {
       claim_cell(R.claimed, cell0);
     }
   }
+}
+
+// round bookkeeping on the device: counters of the growth loop in B_HOSTIO2
+// ([0] grown, [1] error, [2] [3] the two list lengths, [4] warp growth list,
+// [5] warp commit list, [6..7] byte total, [16] tag, [18..19] peak count)
+constexpr int GROW_TAG = 16, GROW_NP = 18;
+constexpr int GROW_ROUNDS_PER_LAUNCH = 250;     // reservation tags 1..250 (8 bits of the key)
+
+// start of a round with current list `cur`: its next list and the warp
+// lists empty, the next reservation tag
+__global__ void k_round_begin(int* dcnt, int cur) {
+  if (threadIdx.x == 0) {
+    dcnt[3 - cur] = 0;
+    dcnt[4] = 0;
+    dcnt[5] = 0;
+    dcnt[GROW_TAG] += 1;
+  }
+}
+
+// end of the round loop's body (current list 1): go on while peaks are left,
+// no growth failed and the tags last
+__global__ void k_round_end(const int* dcnt, cudaGraphConditionalHandle cond) {
+  if (threadIdx.x == 0)
+    cudaGraphSetConditional(cond, (dcnt[2] > 0 && dcnt[1] == 0 && dcnt[GROW_TAG] < GROW_ROUNDS_PER_LAUNCH - 1) ? 1u
+                                                                                                               : 0u);
 }
 
 __global__ void k_sum_words(const unsigned* __restrict__ w, int n, unsigned long long* __restrict__ out) {
@@ -1454,16 +1544,19 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   h->flag = c.buf[B_FLAG].as<int>();
   h->resv = reinterpret_cast<unsigned*>(h->flag + ng);
   unsigned* claimed = h->resv + ng;
+  // per processed peak arrays, laid out by the buffer's capacity (stable
+  // addresses from one realisation to the next)
   EXH_TRY(c.buf[B_HALO].ensure(npr * (sizeof(int) * 8 + 1) + 64));
+  const size_t hcap = (c.buf[B_HALO].cap - 64) / (sizeof(int) * 8 + 1);
   h->gfree = c.buf[B_HALO].as<int>();
-  h->gfin = h->gfree + npr;
-  h->cnt = h->gfin + npr;
-  h->hid = h->cnt + npr;
-  h->hpeak = h->hid + npr;
-  int* kept = h->hpeak + npr;
-  int* misc = kept + npr;             // npr ints: scan scratch / counters
-  h->words = reinterpret_cast<unsigned*>(misc + npr);
-  h->state = reinterpret_cast<unsigned char*>(h->words + npr);
+  h->gfin = h->gfree + hcap;
+  h->cnt = h->gfin + hcap;
+  h->hid = h->cnt + hcap;
+  h->hpeak = h->hid + hcap;
+  int* kept = h->hpeak + hcap;
+  int* misc = kept + hcap;            // hcap ints: scan scratch / counters
+  h->words = reinterpret_cast<unsigned*>(misc + hcap);
+  h->state = reinterpret_cast<unsigned char*>(h->words + hcap);
   EXH_CUDA_TRY(cudaMemsetAsync(h->flag, 0xff, sizeof(int) * ng, st));      // FLAG_FREE
   EXH_CUDA_TRY(cudaMemsetAsync(h->resv, 0, sizeof(unsigned) * ng, st));
   EXH_CUDA_TRY(cudaMemsetAsync(claimed, 0, sizeof(unsigned) * nclaim, st));
@@ -1471,17 +1564,14 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   EXH_CUDA_TRY(cudaMemsetAsync(h->cnt, 0, sizeof(int) * npr, st));
   h->nh = 0;
   if (nproc == 0) return EXH_OK;
-  GrowArgs A{delta, h->key, h->id, np, (int)nproc, hs, Btab_dev, t};
+  GrowArgs A{delta, h->key, h->id, hs, Btab_dev, t};
   const unsigned nb = exh_div_up(nproc, 128);
-  const unsigned nbw = exh_div_up((size_t)nproc * 32, GROW_T);
   if (c.verbose) { printf("  %lld peaks above the barrier\n", (long long)nproc); fflush(stdout); }
   // per processed peak during the rounds: gfree = last shell read,
   // kept = growth status; both are rewritten after the rounds
   int* gexit = h->gfree;
   int* gst = kept;
-  // device counters: [0] pending this round, [1] error, [2] next list,
-  // [3] warp growth list, [4] warp commit list, [6..7] byte total (timing)
-  EXH_TRY(c.buf[B_HOSTIO2].ensure(64));
+  EXH_TRY(c.buf[B_HOSTIO2].ensure(128));
   int* dcnt = c.buf[B_HOSTIO2].as<int>();
   // pending peaks as a compacted list (misc and hid serve as the two lists
   // during the rounds; both are rewritten afterwards); the warp passes'
@@ -1489,59 +1579,124 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   int* lists[2] = {misc, h->hid};
   EXH_TRY(c.buf[B_HALO3].ensure(sizeof(int) * 2 * npr));
   int* wlist = c.buf[B_HALO3].as<int>();
-  int* clist = wlist + npr;
-  // device counters: [0] grown this round, [1] error, [2] [3] the two list
-  // lengths, [4] warp growth list, [5] warp commit list, [6..7] byte total
+  int* clist = wlist + c.buf[B_HALO3].cap / (2 * sizeof(int));
   k_iota<<<nb, 128, 0, st>>>(lists[0], (int)nproc);
   count_launch(1);
   {
-    const int init[6] = {0, 0, (int)nproc, 0, 0, 0};
+    int init[20] = {0, 0, (int)nproc, 0, 0, 0};
+    const long long npl = np;
+    std::memcpy(&init[GROW_NP], &npl, sizeof(npl));
     EXH_TRY(upload_small(dcnt, init, sizeof(init), st));
   }
-  (void)nbw;
   if (timing_on()) EXH_CUDA_TRY(cudaMemsetAsync(h->words, 0, sizeof(unsigned) * npr, st));
   KTimer kt(KC_GROW, st, 0.0);   // the whole growth phase is one timed unit
-  // the rounds run without host round trips: list lengths stay on the device
-  // and the persistent grids read them; the host checks every few rounds
-  const unsigned nbl = std::min<unsigned>(exh_div_up((size_t)nproc, GROW_T), GROW_PERSIST);
-  constexpr int ROUNDS_PER_CHECK = 3;
-  int cur = 0;
-  for (int round = 0;; round++) {
-    const int tag = (round % 255) + 1;
-    if (round > 0 && tag == 1) EXH_CUDA_TRY(cudaMemsetAsync(h->resv, 0, sizeof(unsigned) * ng, st));
-    EXH_CUDA_TRY(cudaMemsetAsync(dcnt + 3 - cur, 0, sizeof(int), st));      // next list
-    EXH_CUDA_TRY(cudaMemsetAsync(dcnt + 4, 0, sizeof(int) * 2, st));        // warp lists
+  // persistent grids, sized by the peak buffers' capacity (stable from one
+  // realisation to the next)
+  const unsigned nbl = std::min<unsigned>(exh_div_up(std::max<size_t>(peak_cap(c), 1), GROW_T), GROW_PERSIST);
+  auto round = [&](int cur, cudaStream_t s) -> int {
     RoundArgs R;
-    R.state = h->state; R.flag = h->flag; R.resv = h->resv; R.claimed = claimed; R.tag = tag;
+    R.state = h->state; R.flag = h->flag; R.resv = h->resv; R.claimed = claimed;
+    R.tag = dcnt + GROW_TAG;
+    R.np = reinterpret_cast<const long long*>(dcnt + GROW_NP);
     R.cnt = h->cnt; R.gtmp = h->gfin; R.gexit = gexit; R.gst = gst; R.gfin = h->gfin;
     R.npend = dcnt; R.err = dcnt + 1; R.next = lists[cur ^ 1]; R.nnext = dcnt + 3 - cur;
     R.wlist = wlist; R.nw = dcnt + 4; R.clist = clist; R.nc = dcnt + 5;
     R.nwords = timing_on() ? h->words : nullptr;
     const int* ncur = dcnt + 2 + cur;
-    k_tentative<<<nbl, GROW_T, 0, st>>>(A, lists[cur], ncur, R);
-    k_tentative_warp<<<nbl, GROW_T, 0, st>>>(A, R);
-    k_commit<<<nbl, GROW_T, 0, st>>>(A, lists[cur], ncur, R);
-    k_commit_warp<<<nbl, GROW_T, 0, st>>>(A, R);
-    count_launch(4);
+    k_round_begin<<<1, 32, 0, s>>>(dcnt, cur);
+    k_tentative<<<nbl, GROW_T, 0, s>>>(A, lists[cur], ncur, R);
+    k_tentative_warp<<<nbl, GROW_T, 0, s>>>(A, R);
+    k_commit<<<nbl, GROW_T, 0, s>>>(A, lists[cur], ncur, R);
+    k_commit_warp<<<nbl, GROW_T, 0, s>>>(A, R);
     EXH_CUDA_TRY(cudaGetLastError());
-    cur ^= 1;
-    if ((round + 1) % ROUNDS_PER_CHECK == 0) {
-      int hc[6];
-      EXH_CUDA_TRY(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
-      EXH_CUDA_TRY(cudaStreamSynchronize(st));
-      if (hc[1]) {
-        exh_set_error_msg(hc[1] == 1 ? "a halo grew past the sigma(M) table (find_halos.c:316 would read past Sig_Grid)"
-                                     : "a halo grew past every shell of the box",
-                          __FILE__, __LINE__);
-        return EXH_E_RANGE;
+    return EXH_OK;
+  };
+  int hc[6] = {0, 0, 0, 0, 0, 0};
+  if (timing_on()) {
+    // kernel-class timing: rounds launched one by one, the host checks every
+    // few rounds
+    constexpr int ROUNDS_PER_CHECK = 3;
+    int cur = 0;
+    for (int rd = 0;; rd++) {
+      if (rd > 0 && rd % GROW_ROUNDS_PER_LAUNCH == 0) {
+        EXH_CUDA_TRY(cudaMemsetAsync(h->resv, 0, sizeof(unsigned) * ng, st));
+        EXH_CUDA_TRY(cudaMemsetAsync(dcnt + GROW_TAG, 0, sizeof(int), st));
       }
-      if (c.verbose > 1) { printf("  growth round %d: %d left\n", round, hc[2 + cur]); fflush(stdout); }
-      if (hc[2 + cur] == 0) break;
+      EXH_TRY(round(cur, st));
+      count_launch(5);
+      cur ^= 1;
+      if ((rd + 1) % ROUNDS_PER_CHECK == 0) {
+        EXH_CUDA_TRY(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
+        EXH_CUDA_TRY(cudaStreamSynchronize(st));
+        if (c.verbose > 1) { printf("  growth round %d: %d left\n", rd, hc[2 + cur]); fflush(stdout); }
+        if (hc[1] || hc[2 + cur] == 0) break;
+      }
+      if (rd > nproc + 2) {
+        exh_set_error_msg("halo growth made no progress", __FILE__, __LINE__);
+        return EXH_E_TIMEOUT;
+      }
     }
-    if (round > nproc + 2) {
-      exh_set_error_msg("halo growth made no progress", __FILE__, __LINE__);
-      return EXH_E_TIMEOUT;
+  } else {
+    // the round loop as a graph: a while node over two rounds (list 0, then
+    // list 1) that k_round_end ends on the device; one graph per set of
+    // arguments, a few kept (batches alternate box sizes), launched again
+    // with fresh reservation tags only if it stopped at its round cap
+    std::string key;
+    const void* ptrs[16] = {delta, h->key, h->id, Btab_dev, h->state, h->flag, h->resv, claimed, h->cnt, h->gfin,
+                            gexit, gst, dcnt, lists[0], lists[1], wlist};
+    key.append(reinterpret_cast<const char*>(ptrs), sizeof(ptrs));
+    key.append(reinterpret_cast<const char*>(&clist), sizeof(clist));
+    key.append(reinterpret_cast<const char*>(&hs), sizeof(hs));
+    key.append(reinterpret_cast<const char*>(&t), sizeof(t));
+    key.append(reinterpret_cast<const char*>(&nbl), sizeof(nbl));
+    cudaGraphExec_t ex = nullptr;
+    for (auto& e : c.grow_graphs)
+      if (e.key == key) ex = e.exec;
+    if (!ex) {
+      if (c.grow_graphs.size() >= 6) {
+        cudaGraphExecDestroy(c.grow_graphs.front().exec);
+        cudaGraphDestroy(c.grow_graphs.front().src);
+        c.grow_graphs.erase(c.grow_graphs.begin());
+      }
+      Ctx::GraphEntry e;
+      EXH_TRY(build_while_graph(
+          c,
+          [&](cudaStream_t s, cudaGraphConditionalHandle cond) -> int {
+            EXH_TRY(round(0, s));
+            EXH_TRY(round(1, s));
+            k_round_end<<<1, 32, 0, s>>>(dcnt, cond);
+            EXH_CUDA_TRY(cudaGetLastError());
+            return EXH_OK;
+          },
+          &e.src, &e.exec));
+      e.key = key;
+      c.grow_graphs.push_back(e);
+      ex = e.exec;
     }
+    for (int launch = 0;; launch++) {
+      if (launch > 0) {          // a new set of tags: stale reservations cleared
+        EXH_CUDA_TRY(cudaMemsetAsync(h->resv, 0, sizeof(unsigned) * ng, st));
+        EXH_CUDA_TRY(cudaMemsetAsync(dcnt + GROW_TAG, 0, sizeof(int), st));
+      }
+      EXH_CUDA_TRY(cudaGraphLaunch(ex, st));
+      int tag = 0;
+      EXH_CUDA_TRY(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
+      EXH_CUDA_TRY(cudaMemcpyAsync(&tag, dcnt + GROW_TAG, sizeof(int), cudaMemcpyDeviceToHost, st));
+      EXH_CUDA_TRY(cudaStreamSynchronize(st));
+      count_launch(11 * (tag / 2));
+      if (c.verbose > 1) { printf("  growth: %d rounds, %d left\n", tag, hc[2]); fflush(stdout); }
+      if (hc[1] || hc[2] == 0) break;
+      if ((size_t)launch * GROW_ROUNDS_PER_LAUNCH > (size_t)nproc + 2) {
+        exh_set_error_msg("halo growth made no progress", __FILE__, __LINE__);
+        return EXH_E_TIMEOUT;
+      }
+    }
+  }
+  if (hc[1]) {
+    exh_set_error_msg(hc[1] == 1 ? "a halo grew past the sigma(M) table (find_halos.c:316 would read past Sig_Grid)"
+                                 : "a halo grew past every shell of the box",
+                      __FILE__, __LINE__);
+    return EXH_E_RANGE;
   }
   if (timing_on()) {
     // algorithmic bytes of the growth rounds: one reduction over the peaks
