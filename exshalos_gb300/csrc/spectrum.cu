@@ -173,6 +173,166 @@ __device__ __forceinline__ void bin_tile(const float2* res, int W, int n, int nb
   }
 }
 
+// ---------------------------------------------------------------------------
+// Binning epilogue of the four-step x passes (k_fft4_x_bin, k_fft8_x_bin512;
+// Nk <= BINW_MAX_NK).  Same modes, wave numbers, |k| and bins as bin_tile,
+// bit for bit, with only float work per mode:
+// * rows i and nd - i have the same kx^2, hence the same |k|, bin and window
+//   for every column: one lane takes the entry q = |kx| / kn, both its rows;
+// * for a fixed column the bin is monotone in q (every step from q to the
+//   bin is a monotone rounded operation), and the modes the reference skips
+//   (powermodule.c:50-51) or that fall outside the bins sit at the ends of the
+//   q order, so among 32 consecutive entries equal bins are contiguous: a warp
+//   takes one column of 32 entries per step and sums each run of equal bins
+//   with a segmented shuffle reduction; the run's first lane adds the sums to
+//   the warp's histogram (float pairs (s, c) per bin, distinct bins within a
+//   warp, no atomics) and the mode count to the block's (integer atomics);
+// * the bin floor((|k| - kmin) / dk) is taken from (|k| - kmin) * (1/dk),
+//   whose relative distance to the correctly rounded quotient is below 2^-22;
+//   within BIN_EDGE of an integer the quotient is formed exactly (__fdiv_rn);
+// * the window is separable: Normk / W = (Normk / wx) * (1 / (wy wz)), a
+//   factor per entry and one per column, instead of two divisions per mode
+//   (a few float ulps from the reference's gridk = out Normk / W);
+// * the warps' histograms are combined per bin in float pairs (fixed order)
+//   and turned into double once per bin and block.
+// The tile is read as res[i * PW + b] with a padded row stride PW = W + 1, so
+// the 32 entries of one column fall in distinct bank pairs.
+constexpr int BINW_MAX_NK = 256;
+constexpr float BIN_EDGE = 1.f / 2048.f;     // covers the 2^-22 relative gap for quotients below 2048
+
+// (s, c) += hi + lo, s updated by an error-free TwoSum
+__device__ __forceinline__ void pair_add(float& s, float& c, float hi, float lo) {
+  const float t = __fadd_rn(s, hi);
+  const float bb = __fsub_rn(t, s);
+  const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(hi, bb));
+  s = t;
+  c = __fadd_rn(c, __fadd_rn(e, lo));
+}
+
+// shared memory of the epilogue: a float4 per column (ky, kz, column factor,
+// skip flags), 4 NW Nk floats (warp histograms), a float per entry (entry
+// factor), 16 bytes of alignment slack
+__host__ __device__ __forceinline__ size_t binw_smem(int NW, int Nk, int nd, int W) {
+  return 16 + 16 * (size_t)W + sizeof(float) * (4 * (size_t)NW * Nk + (size_t)(nd / 2 + 2));
+}
+
+__device__ void bin_tile_mirror(const float2* res, int PW, int W, int nb, int i0, int nd, int nc,
+                                const BinParams& bp, void* scratch, double* hP, double* hK, unsigned* hN) {
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, NW = blockDim.x >> 5;
+  const int Nk = bp.Nk, h = nd / 2, E = h + 1, G = (E + 31) >> 5;
+  const int wq = bp.window == 2 ? 2 : (bp.window == 1 ? 1 : 0);     // W = (wx wy wz)^wq
+  float4* colt = reinterpret_cast<float4*>((reinterpret_cast<uintptr_t>(scratch) + 15) & ~(uintptr_t)15);
+  float* ws = reinterpret_cast<float*>(colt + W);
+  const size_t stride = (size_t)NW * Nk;
+  float* Ps = ws + (size_t)warp * Nk;
+  float* Pc = Ps + stride;
+  float* Ks = Pc + stride;
+  float* Kc = Ks + stride;
+  float* rowt = ws + 4 * stride;
+  for (int b = lane; b < Nk; b += 32) { Ps[b] = 0.f; Pc[b] = 0.f; Ks[b] = 0.f; Kc[b] = 0.f; }
+  for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+    const int col = i0 + t, j = col / nc, k = col % nc;
+    const float ky = (float)((2 * j < nd) ? j : j - nd) * bp.kn;
+    const float kz = (float)((2 * k < nd) ? k : k - nd) * bp.kn;
+    float cf = 1.f;
+    if (wq) {
+      float s = __fmul_rn(sinc_f(ky * bp.Lb * 0.5f), sinc_f(kz * bp.Lb * 0.5f));
+      if (wq == 2) s = __fmul_rn(s, s);
+      cf = __frcp_rn(s);
+    }
+    const int flag = ((k == 0 || k == h) ? 1 : 0) | ((j == 0 || j == h) ? 2 : 0);
+    colt[t] = make_float4(ky, kz, cf, __int_as_float(flag));
+  }
+  for (int q = threadIdx.x; q < E; q += blockDim.x) {
+    float rf = bp.Normk;
+    if (wq) {
+      float s = sinc_f((float)q * bp.kn * bp.Lb * 0.5f);             // sinc is even: both rows of the entry
+      if (wq == 2) s = __fmul_rn(s, s);
+      rf = __fdiv_rn(bp.Normk, s);
+    }
+    rowt[q] = rf;
+  }
+  __syncthreads();
+  const float inv_dk = __frcp_rn(bp.dk);
+  const int units = G * nb;
+  for (int u = warp; u < units; u += NW) {              // warp-uniform: (entry group, column)
+    const int g = u / nb, b = u - g * nb;
+    const int q = (g << 5) + lane;
+    int key = -1, two = 0;
+    float pw = 0.f, kk = 0.f;
+    if (q < E) {
+      const float4 cq = colt[b];
+      const int fl = __float_as_int(cq.w);
+      const bool fk = fl & 1, fj = fl & 2;
+      const int r2 = nd - q;                            // the mirror row, when it is a row other than q
+      const bool keep1 = !fk || (!fj && q > 0 && q < h);
+      const bool keep2 = q > 0 && r2 > h && !fk;        // rows past nd/2 are skipped on the kz = 0, nd/2 planes
+      if (keep1 || keep2) {
+        const float kx = (float)q * bp.kn;              // (-q kn)^2 = (q kn)^2: the mirror row's kx^2
+        const float k2 = __fadd_rn(__fadd_rn(__fmul_rn(kx, kx), __fmul_rn(cq.x, cq.x)), __fmul_rn(cq.y, cq.y));
+        const float kmod = __fsqrt_rn(k2);
+        const float d = __fsub_rn(kmod, bp.kmin);
+        const float qf = __fmul_rn(d, inv_dk);
+        float fb = floorf(qf);
+        const float fr = __fsub_rn(qf, fb);
+        if (fr <= BIN_EDGE || fr >= 1.f - BIN_EDGE) fb = floorf(__fdiv_rn(d, bp.dk));
+        if (fb >= 0.f && fb < (float)Nk) {
+          key = (int)fb;
+          const float sc = __fmul_rn(rowt[q], cq.z);
+          float p = 0.f;
+          if (keep1) {
+            const float2 v = res[q * PW + b];
+            const float re = __fmul_rn(v.x, sc), im = __fmul_rn(v.y, sc);
+            p = __fadd_rn(__fmul_rn(re, re), __fmul_rn(im, im));
+          }
+          if (keep2) {
+            const float2 v = res[r2 * PW + b];
+            const float re = __fmul_rn(v.x, sc), im = __fmul_rn(v.y, sc);
+            p = __fadd_rn(p, __fadd_rn(__fmul_rn(re, re), __fmul_rn(im, im)));
+          }
+          pw = p;
+          two = keep1 && keep2;
+          kk = two ? __fadd_rn(kmod, kmod) : kmod;
+        }
+      }
+    }
+    const unsigned vmask = __ballot_sync(FULL, key >= 0);
+    if (vmask == 0u) continue;
+    const int kprev = __shfl_up_sync(FULL, key, 1);
+    const bool start = key >= 0 && (lane == 0 || kprev != key);
+    const unsigned bmask = __ballot_sync(FULL, start) | ~vmask;        // lanes where a run begins or breaks
+    const unsigned above = bmask & (0xfffffffeu << lane);
+    const int end = above ? __ffs(above) - 1 : 32;                    // one past this lane's run
+    const unsigned tmask = __ballot_sync(FULL, two);
+#pragma unroll
+    for (int dd = 1; dd < 32; dd <<= 1) {                             // suffix sums within the run
+      const float tp = __shfl_down_sync(FULL, pw, dd), tk = __shfl_down_sync(FULL, kk, dd);
+      if (lane + dd < end) {
+        pw = __fadd_rn(pw, tp);
+        kk = __fadd_rn(kk, tk);
+      }
+    }
+    if (start) {
+      const unsigned run = (end == 32 ? FULL : ((1u << end) - 1u)) & (FULL << lane);
+      pair_add(Ps[key], Pc[key], pw, 0.f);
+      pair_add(Ks[key], Kc[key], kk, 0.f);
+      atomicAdd(&hN[key], (unsigned)(end - lane) + (unsigned)__popc(tmask & run));
+    }
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < Nk; b += blockDim.x) {
+    float ps = 0.f, pc = 0.f, ks = 0.f, kc = 0.f;
+    for (int w = 0; w < NW; w++) {
+      const size_t o = (size_t)w * Nk + b;
+      pair_add(ps, pc, ws[o], ws[stride + o]);
+      pair_add(ks, kc, ws[2 * stride + o], ws[3 * stride + o]);
+    }
+    hP[b] = (double)ps + (double)pc;
+    hK[b] = (double)ks + (double)kc;
+  }
+}
+
 // x pass of the forward transform with the binning epilogue.
 // Tile: all nx modes of FFT_W adjacent (y, kz) columns.
 __global__ void __launch_bounds__(FFT_THREADS)
@@ -216,7 +376,7 @@ k_fft4_x_bin(const float2* __restrict__ work, const float2* __restrict__ tw, int
   constexpr int W = S::W, n = S::n;
   extern __shared__ float2 dsm[];
   float2* sm = dsm;
-  double* hP = reinterpret_cast<double*>(sm + n * W);
+  double* hP = reinterpret_cast<double*>(sm + n * (W + 1));
   double* hK = hP + bp.Nk;
   unsigned int* hN = reinterpret_cast<unsigned int*>(hK + bp.Nk);
   const int inner = nd * nc;
@@ -247,10 +407,11 @@ k_fft4_x_bin(const float2* __restrict__ work, const float2* __restrict__ tw, int
   __syncthreads();
   if (jj < N1) {
 #pragma unroll
-    for (int k2 = 0; k2 < N2; k2++) sm[(jj + N1 * k2) * W + c] = u[k2];
+    for (int k2 = 0; k2 < N2; k2++) sm[(jj + N1 * k2) * (W + 1) + c] = u[k2];
   }
   __syncthreads();
-  bin_tile(sm, W, n, nb, i0, nd, nc, bp, hP, hK, hN);
+  if (bp.Nk <= BINW_MAX_NK) bin_tile_mirror(sm, W + 1, W, nb, i0, nd, nc, bp, hN + bp.Nk, hP, hK, hN);
+  else bin_tile(sm, W + 1, n, nb, i0, nd, nc, bp, hP, hK, hN);
   __syncthreads();
   for (int b = threadIdx.x; b < bp.Nk; b += blockDim.x) {
     partP[(size_t)blockIdx.x * bp.Nk + b] = hP[b];
@@ -282,10 +443,11 @@ k_fft8_x_bin512(const float2* __restrict__ work, const float2* __restrict__ tw, 
   {
     const int k1 = q >> 3, k2a = q & 7;
 #pragma unroll
-    for (int k2b = 0; k2b < 8; k2b++) sm[(k1 + 8 * k2a + 64 * k2b) * W + c] = v[k2b];
+    for (int k2b = 0; k2b < 8; k2b++) sm[(k1 + 8 * k2a + 64 * k2b) * (W + 1) + c] = v[k2b];
   }
   __syncthreads();
-  bin_tile(sm, W, n, nb, i0, nd, nc, bp, hP, hK, hN);
+  if (bp.Nk <= BINW_MAX_NK) bin_tile_mirror(sm, W + 1, W, nb, i0, nd, nc, bp, hN + bp.Nk, hP, hK, hN);
+  else bin_tile(sm, W + 1, n, nb, i0, nd, nc, bp, hP, hK, hN);
   __syncthreads();
   for (int b = threadIdx.x; b < bp.Nk; b += blockDim.x) {
     partP[(size_t)blockIdx.x * bp.Nk + b] = hP[b];
@@ -304,7 +466,8 @@ static cudaError_t launch_fs_x_bin(const float2* work, const float2* tw, int nd,
   if (nd == 512) {
     const int nb = (int)exh_div_up(inner, F512_W);
     if (nb > nblk_cap) return cudaSuccess;
-    const size_t sm = sizeof(float2) * (512 + 64) * F512_W + (size_t)bp.Nk * (2 * sizeof(double) + sizeof(unsigned)) + 16;
+    size_t sm = sizeof(float2) * (512 + 64) * F512_W + (size_t)bp.Nk * (2 * sizeof(double) + sizeof(unsigned)) + 16;
+    if (bp.Nk <= BINW_MAX_NK) sm += binw_smem(F512_T / 32, bp.Nk, 512, F512_W);
     cudaError_t e = set_smem(k_fft8_x_bin512, sm);
     if (e != cudaSuccess) return e;
     k_fft8_x_bin512<<<nb, F512_T, sm, st>>>(work, tw, nd, nc, bp, partP, partK, partN);
@@ -317,7 +480,8 @@ static cudaError_t launch_fs_x_bin(const float2* work, const float2* tw, int nd,
     using S = FsShape<A_, B_>;                                                                           \
     const int nb = (int)exh_div_up(inner, S::W);                                                         \
     if (nb > nblk_cap) return cudaSuccess;                                                               \
-    const size_t sm = sizeof(float2) * S::n * S::W + (size_t)bp.Nk * (2 * sizeof(double) + sizeof(unsigned)) + 16; \
+    size_t sm = sizeof(float2) * S::n * (S::W + 1) + (size_t)bp.Nk * (2 * sizeof(double) + sizeof(unsigned)) + 16; \
+    if (bp.Nk <= BINW_MAX_NK) sm += binw_smem(FS_THREADS / 32, bp.Nk, S::n, S::W);                      \
     cudaError_t e = set_smem(k_fft4_x_bin<A_, B_>, sm);                                                  \
     if (e != cudaSuccess) return e;                                                                      \
     k_fft4_x_bin<A_, B_><<<nb, FS_THREADS, sm, st>>>(work, tw, nd, nc, bp, partP, partK, partN);          \
