@@ -231,15 +231,27 @@ k_peak_write(const float* __restrict__ d, size_t ng, unsigned ngroups, const uns
 // next while the buffer does not grow
 size_t peak_cap(const Ctx& c) { return c.buf[B_PEAKS].cap / ((sizeof(float) + sizeof(unsigned)) * 3); }
 
+// B_SORT after find_peaks: the peak bitmask (one bit per cell), the peak
+// count and the first peak (in cell order) of every group of PK_T cells.
+// Only find_peaks writes the buffer, so it describes the peaks of the last
+// grid searched, which are the peaks in use (a reused sort belongs to that
+// grid too).
+static void peak_mask_layout(Ctx& c, size_t ng, unsigned** mask, unsigned** cnt, unsigned** off) {
+  const unsigned nb = exh_div_up(ng, PK_T);
+  const size_t words = (size_t)nb * (PK_T / 32);
+  *mask = c.buf[B_SORT].as<unsigned>();
+  *cnt = *mask + words;
+  *off = *cnt + nb;
+}
+
 int find_peaks(Ctx& c, const float* delta, const BoxParams& b, HaloDev* h, cudaStream_t st) {
   const size_t ng = b.ng;
   const unsigned nb = exh_div_up(ng, PK_T);
   const size_t words = (size_t)nb * (PK_T / 32);
   // scratch: mask words, block counts, block offsets, scan sums, total
   EXH_TRY(c.buf[B_SORT].ensure(sizeof(unsigned) * (words + 3 * (size_t)nb + 64)));
-  unsigned* mask = c.buf[B_SORT].as<unsigned>();
-  unsigned* cnt = mask + words;
-  unsigned* off = cnt + nb;
+  unsigned *mask, *cnt, *off;
+  peak_mask_layout(c, ng, &mask, &cnt, &off);
   unsigned* sums = off + nb;
   unsigned* total = sums + nb + 32;
   const unsigned grid = std::min<unsigned>(nb, EXH_NUM_SMS * PK_BLOCKS_PER_SM);
@@ -578,134 +590,113 @@ struct SmallSortBuffers {
   unsigned* ib[2];
 };
 
-// One block sorts one segment of at most SORT_SMALL elements, level by
-// level: in each level every warp partitions its share of the pending
-// sub-segments (Lomuto, computed as in k_qs_place), then the block
-// collects the children for the next level.  No locks and no waits other
-// than block barriers; at most n levels.
-__device__ __forceinline__ void warp_partition(float* ka, unsigned* ia, float* kb, unsigned* ib, int* lam, int* posl, int lo,
-                                               int hi, int lane, int& nL_out) {
-  const float pv = ka[hi];
-  const int s = hi - lo + 1;
-  int run = 0;
-  for (int b0 = lo; b0 < hi; b0 += 32) {
-    const int p = b0 + lane;
-    const bool L = p < hi && ka[p] <= pv;
-    const unsigned msk = __ballot_sync(0xffffffffu, L);
-    const int r = run + __popc(msk & ((1u << lane) - 1u));
-    if (p < hi) {
-      if (L) { kb[lo + r] = ka[p]; ib[lo + r] = ia[p]; posl[lo + r] = p - lo; }
-      else lam[lo + (p - lo - r)] = r;
-    }
-    run += __popc(msk);
-  }
-  const int nL = run, m = s - 1 - nL;
-  __syncwarp();
-  for (int b0 = lo; b0 < hi; b0 += 32) {
-    const int p = b0 + lane;
-    if (p < hi && !(ka[p] <= pv)) {
-      const int* ls = lam + lo;
-      const int* ps = posl + lo;
-      const int a = lomuto_g_dest(p - lo, nL, m, [ls](int i) { return ls[i]; }, [ps](int i) { return ps[i]; });
-      const int dest = (a == nL) ? (s - 1) : a;
-      kb[lo + dest] = ka[p];
-      ib[lo + dest] = ia[p];
-    }
-  }
-  if (lane == 0) { kb[lo + nL] = ka[hi]; ib[lo + nL] = ia[hi]; }
-  __syncwarp();
-  for (int p = lo + lane; p <= hi; p += 32) { ka[p] = kb[p]; ia[p] = ib[p]; }
-  __syncwarp();
-  nL_out = nL;
-}
-
-// The same partition of one sub-segment [lo, hi] by the whole block (for
-// the first levels, where a block has one or two sub-segments): each thread
-// classifies SORT_SMALL / SORT_T consecutive elements, a block scan gives the
-// L ranks, and the > elements follow their chains.  Returns nL.
-__device__ __forceinline__ int block_partition(float* ka, unsigned* ia, float* kb, unsigned* ib, int* lam, int* posl,
-                                               int lo, int hi, int* ws) {
-  constexpr int IT = SORT_SMALL / SORT_T;
-  const float pv = ka[hi];
-  const int n = hi - lo;                     // elements before the pivot, <= SORT_SMALL - 1
-  const int base = lo + threadIdx.x * IT;
-  bool isL[IT];
-  int c = 0;
-#pragma unroll
-  for (int q = 0; q < IT; q++) {
-    const int p = base + q;
-    isL[q] = p < hi && ka[p] <= pv;
-    c += isL[q];
-  }
-  int nL;
-  int r = block_exclusive_scan<int>(c, ws, nL);
-#pragma unroll
-  for (int q = 0; q < IT; q++) {
-    const int p = base + q;
-    if (p >= hi) break;
-    if (isL[q]) { kb[lo + r] = ka[p]; ib[lo + r] = ia[p]; posl[lo + r] = p - lo; r++; }
-    else lam[lo + (p - lo - r)] = r;
-  }
-  __syncthreads();
-  const int m = n - nL;
-  const int* ls = lam + lo;
-  const int* ps = posl + lo;
-#pragma unroll
-  for (int q = 0; q < IT; q++) {
-    const int p = base + q;
-    if (p < hi && !isL[q]) {
-      const int a = lomuto_g_dest(p - lo, nL, m, [ls](int i) { return ls[i]; }, [ps](int i) { return ps[i]; });
-      const int dest = (a == nL) ? n : a;
-      kb[lo + dest] = ka[p];
-      ib[lo + dest] = ia[p];
-    }
-  }
-  if (threadIdx.x == 0) { kb[lo + nL] = ka[hi]; ib[lo + nL] = ia[hi]; }
-  __syncthreads();
-  for (int p = lo + threadIdx.x; p <= hi; p += blockDim.x) { ka[p] = kb[p]; ia[p] = ib[p]; }
-  __syncthreads();
-  return nL;
-}
-
-// Sub-segments of at most SORT_TINY elements are finished by one thread with
-// the literal Lomuto quicksort (find_halos.c:175-197: pivot at hi, keys
-// <= pivot to the front, then both sides), an explicit stack instead of the
-// recursion (the order in which independent sides are sorted does not change
-// the result; pushing the larger side keeps the depth below log2 n).
+// Sub-segments of at most SORT_TINY elements are finished by one warp, one
+// element per lane, with the literal Lomuto quicksort's result
+// (find_halos.c:175-197: pivot at hi, keys <= pivot to the front in their
+// order, then both sides).  A quicksort leaves distinct keys in ascending
+// order whatever its pivots, so a pending sub-segment without two equal keys
+// is finished at once (each lane's place is the number of smaller keys);
+// the others partition, all at once per level: each is a run of lanes
+// [a, b] (pivot in lane b), L ranks come from the warp's ballot, and a >
+// element's place follows the same chain as in k_qs_place, with posl(r) (the
+// r-th L lane) and lam(c) (L lanes before the c-th > lane) read off the two
+// ballots.  At most 31 levels.
 constexpr int SORT_TINY = 32;
 
-__device__ __forceinline__ void tiny_quicksort(float* k, unsigned* id, int lo, int hi) {
-  int stk[16];
-  int sp = 0;
-  for (;;) {
-    while (lo < hi) {
-      const float pv = k[hi];
-      int i = lo - 1;
-      for (int j = lo; j < hi; j++) {
-        const float kj = k[j];
-        if (kj <= pv) {
-          i++;
-          const float tk = k[i]; k[i] = kj; k[j] = tk;
-          const unsigned ti = id[i]; id[i] = id[j]; id[j] = ti;
-        }
-      }
-      {
-        const float tk = k[i + 1]; k[i + 1] = k[hi]; k[hi] = tk;
-        const unsigned ti = id[i + 1]; id[i + 1] = id[hi]; id[hi] = ti;
-      }
-      const int pi = i + 1;
-      if (pi - lo < hi - pi) { stk[sp++] = pi + 1; stk[sp++] = hi; hi = pi - 1; }
-      else { stk[sp++] = lo; stk[sp++] = pi - 1; lo = pi + 1; }
+// position of the n-th (0-based) set bit of m (m has more than n set bits)
+__device__ __forceinline__ int nth_set(unsigned m, int n) {
+  int pos = 0;
+#pragma unroll
+  for (int w = 16; w > 0; w >>= 1) {
+    const int c = __popc(m & ((1u << w) - 1u));
+    if (n >= c) {
+      n -= c;
+      m >>= w;
+      pos += w;
     }
-    if (sp == 0) break;
-    hi = stk[--sp];
-    lo = stk[--sp];
   }
+  return pos;
 }
 
+__device__ __forceinline__ void warp_tiny_sort(float* ka, unsigned* ia, float* kb, unsigned* ib, int lo, int hi,
+                                               int lane) {
+  constexpr unsigned FULL = 0xffffffffu;
+  const int s = hi - lo + 1;                       // 2 .. SORT_TINY
+  const bool act = lane < s;
+  float k = act ? ka[lo + lane] : 0.f;
+  unsigned id = act ? ia[lo + lane] : 0u;
+  unsigned start = 1u;                             // lanes that begin a sub-segment
+  unsigned pend = s >= 2 ? 1u : 0u;                // sub-segments (by first lane) still to partition
+  while (pend) {
+    const int a = 31 - __clz(start & ((2u << lane) - 1u));
+    const unsigned above = start & ~((2u << lane) - 1u);
+    const int b = (above ? __ffs(above) - 1 : s) - 1;
+    const bool inpend = act && ((pend >> a) & 1u);
+    // equal keys (-0 and +0 compare equal) within the pending sub-segment;
+    // lanes outside the segment carry distinct NaN patterns
+    const unsigned ab = ((2u << b) - 1u) & ~((1u << a) - 1u);       // lanes a .. b
+    const unsigned same = __match_any_sync(FULL, act ? __float_as_uint(k == 0.f ? 0.f : k) : 0x7fc00000u + lane);
+    const unsigned tiem = __ballot_sync(FULL, inpend && __popc(same & ab) > 1);
+    const bool ranked = inpend && (tiem & ab) == 0u;
+    int dest = lane;
+    if (__any_sync(FULL, ranked)) {
+      int rk = 0;
+      for (int j = 0; j < 32; j++) {
+        const float kj = __shfl_sync(FULL, k, j);
+        rk += (j >= a && j <= b && kj < k) ? 1 : 0;
+      }
+      if (ranked) dest = a + rk;
+    }
+    const bool lom = inpend && !ranked;
+    const float pv = __shfl_sync(FULL, k, b & 31);
+    const bool isL = lom && lane < b && k <= pv;
+    const bool isG = lom && lane < b && !(k <= pv);
+    const unsigned Lm = __ballot_sync(FULL, isL), Gm = __ballot_sync(FULL, isG);
+    unsigned add_start = 0u, add_pend = 0u;
+    if (lom) {
+      const unsigned seg = ((1u << b) - 1u) & ~((1u << a) - 1u);
+      const int nL = __popc(Lm & seg), m = (b - a) - nL;
+      if (isL) {
+        dest = a + __popc(Lm & seg & ((1u << lane) - 1u));
+      } else if (lane == b) {
+        dest = a + nL;
+      } else {
+        const unsigned Lr = (Lm & seg) >> a, Gr = (Gm & seg) >> a;
+        const int g = lomuto_g_dest(lane - a, nL, m, [Gr](int c) { return nth_set(Gr, c) - c; },
+                                    [Lr](int r) { return nth_set(Lr, r); });
+        dest = a + (g == nL ? b - a : g);
+      }
+      if (lane == a) {
+        add_start = 1u << (a + nL);
+        if (a + nL + 1 <= b) add_start |= 1u << (a + nL + 1);
+        if (nL >= 2) add_pend |= 1u << a;
+        if (m >= 2) add_pend |= 1u << (a + nL + 1);
+      }
+    }
+    if (act) { kb[lo + dest] = k; ib[lo + dest] = id; }
+    __syncwarp();
+    if (act) { k = kb[lo + lane]; id = ib[lo + lane]; }
+    __syncwarp();
+    start |= __reduce_or_sync(FULL, add_start);
+    pend = __reduce_or_sync(FULL, add_pend);
+  }
+  if (act) { ka[lo + lane] = k; ia[lo + lane] = id; }
+}
+
+// One block sorts one segment of at most SORT_SMALL elements, level by
+// level.  Each level partitions every pending sub-segment (more than
+// SORT_TINY elements) at once with the whole block (Lomuto, as k_qs_place):
+// thread t owns positions IT t .. IT t + IT - 1; one block scan of the L
+// flags over all positions gives every L element its rank (the scan value
+// minus the value at its sub-segment's first position), and the > elements
+// follow their chains.  The pending list stays ordered by position, so a
+// position finds its sub-segment by a binary search of the list.  Children
+// of at most SORT_TINY elements go to the warp sort.  No locks and no waits
+// other than block barriers; at most n levels.
 __global__ void __launch_bounds__(SORT_T)
 k_qs_small(const Seg* __restrict__ segs, int nseg, SmallSortBuffers bufs, float* __restrict__ fkey,
            unsigned* __restrict__ fid, int* __restrict__ err) {
+  constexpr int IT = SORT_SMALL / SORT_T;
   extern __shared__ unsigned char sm_raw[];
   float* ka = reinterpret_cast<float*>(sm_raw);
   unsigned* ia = reinterpret_cast<unsigned*>(ka + SORT_SMALL);
@@ -716,11 +707,13 @@ k_qs_small(const Seg* __restrict__ segs, int nseg, SmallSortBuffers bufs, float*
   // pending sub-segments have more than SORT_TINY elements: at most
   // SORT_SMALL / (SORT_TINY + 1) of them; tiny ones at most SORT_SMALL / 2
   constexpr int PEND = 2 * (SORT_SMALL / (SORT_TINY + 1) + 1);
-  static_assert(2 * PEND + 4 * PEND + SORT_SMALL <= 3 * SORT_SMALL, "lists fit the allocation");
-  int* cur = posl + SORT_SMALL;             // pending (lo, hi) pairs of this level
+  static_assert(2 * PEND + 4 * PEND + 2 * PEND + SORT_SMALL <= 3 * SORT_SMALL, "lists fit the allocation");
+  int* cur = posl + SORT_SMALL;             // pending (lo, hi) pairs of this level, by position
   int* nxt = cur + 2 * PEND;                // two child slots per pending segment
-  int* tiny = nxt + 4 * PEND;               // (lo, hi) pairs finished by one thread each
+  int* sbase = nxt + 4 * PEND;              // L flags before each pending segment's first / last position
+  int* tiny = sbase + 2 * PEND;             // (lo, hi) pairs finished by one warp each
   __shared__ int ncur, ntiny;
+  __shared__ int ws[32];
   if (blockIdx.x >= nseg) return;
   const Seg sg = segs[blockIdx.x];
   const int n = sg.hi - sg.lo + 1;
@@ -735,50 +728,115 @@ k_qs_small(const Seg* __restrict__ segs, int nseg, SmallSortBuffers bufs, float*
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  __shared__ int ws[32];
+  const int base = threadIdx.x * IT;
   for (int level = 0; level <= n && ncur > 0; level++) {
     const int nc = ncur;
-    if (nc <= 2) {                           // few large sub-segments: the whole block on each
-      for (int q = 0; q < nc; q++) {
-        const int lo = cur[2 * q], hi = cur[2 * q + 1];
-        const int nL = block_partition(ka, ia, kb, ib, lam, posl, lo, hi, ws);
-        if (threadIdx.x == 0) {
-          const int m = hi - lo - nL;
-          nxt[4 * q + 0] = nL >= 2 ? lo : -1;
-          nxt[4 * q + 1] = lo + nL - 1;
-          nxt[4 * q + 2] = m >= 2 ? lo + nL + 1 : -1;
-          nxt[4 * q + 3] = hi;
-        }
+    // sub-segment of each owned position (-1: none pending) and its L flag
+    int sq[IT];
+    bool isL[IT];
+    int c = 0;
+#pragma unroll
+    for (int u = 0; u < IT; u++) {
+      const int p = base + u;
+      int lo = 0, hi = nc;                      // last q with cur[2q] <= p
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (cur[2 * mid] <= p) lo = mid; else hi = mid;
       }
-    } else
-    for (int q = w; q < nc; q += nw) {
-      const int lo = cur[2 * q], hi = cur[2 * q + 1];
-      int nL;
-      warp_partition(ka, ia, kb, ib, lam, posl, lo, hi, lane, nL);
-      if (lane == 0) {
-        const int m = hi - lo - nL;
-        nxt[4 * q + 0] = nL >= 2 ? lo : -1;
-        nxt[4 * q + 1] = lo + nL - 1;
-        nxt[4 * q + 2] = m >= 2 ? lo + nL + 1 : -1;
-        nxt[4 * q + 3] = hi;
+      sq[u] = (p < n && cur[2 * lo] <= p && p <= cur[2 * lo + 1]) ? lo : -1;
+      isL[u] = sq[u] >= 0 && p < cur[2 * lo + 1] && ka[p] <= ka[cur[2 * lo + 1]];
+      c += isL[u];
+    }
+    int tot;
+    const int r0 = block_exclusive_scan<int>(c, ws, tot);
+    {
+      int r = r0;
+#pragma unroll
+      for (int u = 0; u < IT; u++) {
+        const int p = base + u, q = sq[u];
+        if (q >= 0) {
+          if (p == cur[2 * q]) sbase[2 * q] = r;
+          if (p == cur[2 * q + 1]) sbase[2 * q + 1] = r;
+        }
+        r += isL[u];
       }
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      int k = 0, t = ntiny;
-      for (int q = 0; q < 2 * nc; q++) {
-        const int clo = nxt[2 * q], chi = nxt[2 * q + 1];
-        if (clo < 0) continue;
-        if (chi - clo + 1 > SORT_TINY) { cur[2 * k] = clo; cur[2 * k + 1] = chi; k++; }
-        else { tiny[2 * t] = clo; tiny[2 * t + 1] = chi; t++; }
+    // L elements to the front in order, lam and posl
+    {
+      int r = r0;
+#pragma unroll
+      for (int u = 0; u < IT; u++) {
+        const int p = base + u, q = sq[u];
+        if (q >= 0 && p < cur[2 * q + 1]) {
+          const int lo = cur[2 * q], rel = r - sbase[2 * q];
+          if (isL[u]) { kb[lo + rel] = ka[p]; ib[lo + rel] = ia[p]; posl[lo + rel] = p - lo; }
+          else lam[lo + (p - lo - rel)] = rel;
+        }
+        r += isL[u];
       }
-      ncur = k;
-      ntiny = t;
+    }
+    __syncthreads();
+    // > elements along their chains, pivots after the L elements
+#pragma unroll
+    for (int u = 0; u < IT; u++) {
+      const int p = base + u, q = sq[u];
+      if (q < 0) continue;
+      const int lo = cur[2 * q], hi = cur[2 * q + 1];
+      const int nL = sbase[2 * q + 1] - sbase[2 * q];
+      if (p == hi) {
+        kb[lo + nL] = ka[p];
+        ib[lo + nL] = ia[p];
+      } else if (!isL[u]) {
+        const int* ls = lam + lo;
+        const int* ps = posl + lo;
+        const int a = lomuto_g_dest(p - lo, nL, (hi - lo) - nL, [ls](int i) { return ls[i]; },
+                                    [ps](int i) { return ps[i]; });
+        const int dest = (a == nL) ? hi - lo : a;
+        kb[lo + dest] = ka[p];
+        ib[lo + dest] = ia[p];
+      }
+    }
+    if (threadIdx.x < nc) {
+      const int q = threadIdx.x, lo = cur[2 * q], hi = cur[2 * q + 1];
+      const int nL = sbase[2 * q + 1] - sbase[2 * q], m = hi - lo - nL;
+      nxt[4 * q + 0] = nL >= 2 ? lo : -1;
+      nxt[4 * q + 1] = lo + nL - 1;
+      nxt[4 * q + 2] = m >= 2 ? lo + nL + 1 : -1;
+      nxt[4 * q + 3] = hi;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < IT; u++) {
+      const int p = base + u;
+      if (sq[u] >= 0) { ka[p] = kb[p]; ia[p] = ib[p]; }
+    }
+    {
+      // children in slot order (left, right of each pending segment): large
+      // ones to the next level, the others to the tiny list; one thread per
+      // slot, places by a block scan of packed (large << 16 | tiny) counts
+      const int nt0 = ntiny;
+      const int q = threadIdx.x;
+      int clo = -1, chi = -1, cnt = 0;
+      if (q < 2 * nc) {
+        clo = nxt[2 * q];
+        chi = nxt[2 * q + 1];
+        if (clo >= 0) cnt = (chi - clo + 1 > SORT_TINY) ? (1 << 16) : 1;
+      }
+      int ctot;
+      const int ex = block_exclusive_scan<int>(cnt, ws, ctot);
+      if (cnt == (1 << 16)) { cur[2 * (ex >> 16)] = clo; cur[2 * (ex >> 16) + 1] = chi; }
+      else if (cnt == 1) { tiny[2 * (nt0 + (ex & 0xffff))] = clo; tiny[2 * (nt0 + (ex & 0xffff)) + 1] = chi; }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        ncur = ctot >> 16;
+        ntiny = nt0 + (ctot & 0xffff);
+      }
     }
     __syncthreads();
   }
   if (ncur > 0 && threadIdx.x == 0) atomicExch(err, 1);
-  for (int q = threadIdx.x; q < ntiny; q += blockDim.x) tiny_quicksort(ka, ia, tiny[2 * q], tiny[2 * q + 1]);
+  for (int q = w; q < ntiny; q += nw) warp_tiny_sort(ka, ia, kb, ib, tiny[2 * q], tiny[2 * q + 1], lane);
   __syncthreads();
   for (int t = threadIdx.x; t < n; t += blockDim.x) { fkey[sg.lo + t] = ka[t]; fid[sg.lo + t] = ia[t]; }
 }
@@ -1125,6 +1183,7 @@ __device__ int grow_warp_f32(const GrowArgs& A, const unsigned* __restrict__ cla
     float s = 0.f, sa = 0.f;
     bool foreign = false;
     int steps = 0;
+#pragma unroll 4
     for (int q = s0 + lane; q < s1; q += 32) {
       const size_t cell = cell_at(x0, y0, z0, A.t.off_cap[q], hs);
       if (cell_claimed(claimed, cell)) foreign = true;
@@ -1149,6 +1208,7 @@ __device__ int grow_warp_f32(const GrowArgs& A, const unsigned* __restrict__ cla
     count_tmp = count;
     const int s0 = A.t.start_cap[grows], s1 = A.t.start_cap[grows + 1];
     float s = 0.f, sa = 0.f;
+#pragma unroll 4
     for (int q = s0 + lane; q < s1; q += 32) {
       const float v = A.delta[cell_at(x0, y0, z0, A.t.off_cap[q], hs)];
       s += v;
@@ -1186,11 +1246,6 @@ __device__ __forceinline__ void list_push(int* list, int* n, int v) {
   list[base + __popc(m & ((1u << lane) - 1u))] = v;
 }
 
-__device__ __forceinline__ void count_push(int* n) {
-  const unsigned m = __activemask();
-  if ((threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(n, __popc(m));
-}
-
 // grow_warp_f32 by one thread for the small spheres that most peaks grow:
 // the shell sums are sequential (bound depth = cells in the shell).  Returns
 // 3 when a comparison is undecided or the growth would pass shell LANE_GMAX;
@@ -1219,6 +1274,7 @@ __device__ int grow_lane_f32(const GrowArgs& A, const unsigned* __restrict__ cla
     const int s0 = A.t.start_cap[grows_tmp], s1 = A.t.start_cap[grows_tmp + 1];
     float sm = 0.f, sa = 0.f;
     bool foreign = false;
+#pragma unroll 8
     for (int q = s0; q < s1; q++) {
       const size_t cell = cell_at(x0, y0, z0, A.t.off_cap[q], hs);
       foreign |= cell_claimed(claimed, cell);
@@ -1239,6 +1295,7 @@ __device__ int grow_lane_f32(const GrowArgs& A, const unsigned* __restrict__ cla
     count_tmp = count;
     const int s0 = A.t.start_cap[grows], s1 = A.t.start_cap[grows + 1];
     float sm = 0.f, sa = 0.f;
+#pragma unroll 8
     for (int q = s0; q < s1; q++) {
       const float v = A.delta[cell_at(x0, y0, z0, A.t.off_cap[q], hs)];
       sm += v;
@@ -1270,7 +1327,6 @@ struct RoundArgs {
   int* gexit;
   int* gst;
   int* gfin;
-  int* npend;       // peaks grown this round (progress output only)
   int* err;
   int* next;        // peaks left for the next round
   int* nnext;
@@ -1280,6 +1336,49 @@ struct RoundArgs {
   int* nc;
   unsigned* nwords; // 4-byte words touched per peak (timing only) or null
 };
+
+// Reservation of the cells off_all[q0, q1) (step dq) around (x, y, z) with
+// key: the current values are read in batches of RB before any atomic, so a
+// thread has RB loads in flight instead of one.  Values only grow during a
+// round (atomicMax), so a value read early that is already >= key stays so
+// and the skipped atomic would not have changed it.
+constexpr int RB = 8;
+__device__ __forceinline__ void reserve_cells(const GrowArgs& A, unsigned* resv, int x, int y, int z, int q0, int q1,
+                                              int dq, unsigned key) {
+  for (int qb = q0; qb < q1; qb += RB * dq) {
+    size_t cells[RB];
+    unsigned v[RB];
+#pragma unroll
+    for (int u = 0; u < RB; u++) {
+      const int q = qb + u * dq;
+      cells[u] = q < q1 ? cell_at(x, y, z, A.t.off_all[q], A.hs) : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < RB; u++) v[u] = qb + u * dq < q1 ? resv[cells[u]] : 0xffffffffu;
+#pragma unroll
+    for (int u = 0; u < RB; u++)
+      if (v[u] < key) atomicMax(&resv[cells[u]], key);
+  }
+}
+
+// true when no cell off_all[q0, q1) (step dq) holds a reservation above key;
+// RB loads in flight per batch, the test after each batch
+__device__ __forceinline__ bool cells_mine(const GrowArgs& A, const unsigned* resv, int x, int y, int z, int q0, int q1,
+                                           int dq, unsigned key) {
+  for (int qb = q0; qb < q1; qb += RB * dq) {
+    unsigned v[RB];
+#pragma unroll
+    for (int u = 0; u < RB; u++) {
+      const int q = qb + u * dq;
+      v[u] = q < q1 ? resv[cell_at(x, y, z, A.t.off_all[q], A.hs)] : 0u;
+    }
+    bool ok = true;
+#pragma unroll
+    for (int u = 0; u < RB; u++) ok &= v[u] <= key;
+    if (!ok) return false;
+  }
+  return true;
+}
 
 __device__ __forceinline__ unsigned tentative_words(const GrowArgs& A, int ge) {
   // cells read by the growth (density + label) and reserved (read + atomic)
@@ -1299,6 +1398,7 @@ k_tentative(GrowArgs A, const int* __restrict__ list, const int* __restrict__ nl
   const int stride = (int)(gridDim.x * blockDim.x);
   for (int t = (int)(blockIdx.x * (size_t)blockDim.x + threadIdx.x); t < n; t += stride) {
     const int r = list[t];
+    if (r < 0) continue;                     // first round: a peak below the barrier
     const int64_t l = *R.np - 1 - r;
     const unsigned cell0 = A.id[l];
     if (cell_claimed(R.claimed, cell0)) {    // find_halos.c:233: the peak is already inside a halo
@@ -1306,7 +1406,6 @@ k_tentative(GrowArgs A, const int* __restrict__ list, const int* __restrict__ nl
       R.cnt[r] = 0;
       continue;
     }
-    count_push(R.npend);
     int x, y, z;
     peak_coords(cell0, A.hs, x, y, z);
     int count, gt, ge;
@@ -1318,11 +1417,7 @@ k_tentative(GrowArgs A, const int* __restrict__ list, const int* __restrict__ nl
     R.cnt[r] = count; R.gtmp[r] = gt; R.gexit[r] = ge; R.gst[r] = st;
     if (R.nwords) R.nwords[r] += tentative_words(A, ge);
     const unsigned key = resv_key(*R.tag, r);
-    const int e = A.t.start_all[ge];          // cells it may flag: r^2 < gexit
-    for (int q = 0; q < e; q++) {
-      unsigned* pr = &R.resv[cell_at(x, y, z, A.t.off_all[q], A.hs)];
-      if (*pr < key) atomicMax(pr, key);
-    }
+    reserve_cells(A, R.resv, x, y, z, 0, A.t.start_all[ge], 1, key);   // cells it may flag: r^2 < gexit
   }
 }
 
@@ -1345,11 +1440,7 @@ k_tentative_warp(GrowArgs A, RoundArgs R) {
     if (lane == 0) { R.cnt[r] = count; R.gtmp[r] = gt; R.gexit[r] = ge; R.gst[r] = st; }
     if (lane == 0 && R.nwords) R.nwords[r] += tentative_words(A, ge);
     const unsigned key = resv_key(*R.tag, r);
-    const int e = A.t.start_all[ge];
-    for (int q = lane; q < e; q += 32) {
-      unsigned* pr = &R.resv[cell_at(x, y, z, A.t.off_all[q], A.hs)];
-      if (*pr < key) atomicMax(pr, key);
-    }
+    reserve_cells(A, R.resv, x, y, z, lane, A.t.start_all[ge], 32, key);
   }
 }
 
@@ -1379,7 +1470,7 @@ k_commit(GrowArgs A, const int* __restrict__ list, const int* __restrict__ nlist
   const int stride = (int)(gridDim.x * blockDim.x);
   for (int t = (int)(blockIdx.x * (size_t)blockDim.x + threadIdx.x); t < n; t += stride) {
     const int r = list[t];
-    if (R.state[r]) continue;              // resolved by the centre test this round
+    if (r < 0 || R.state[r]) continue;     // below the barrier; resolved by the centre test this round
     const int e = A.t.start_all[R.gexit[r] + 1];
     if (e > LANE_COMMIT_MAX) {
       list_push(R.clist, R.nc, r);
@@ -1389,8 +1480,7 @@ k_commit(GrowArgs A, const int* __restrict__ list, const int* __restrict__ nlist
     int x, y, z;
     peak_coords(cell0, A.hs, x, y, z);
     const unsigned key = resv_key(*R.tag, r);
-    bool mine = true;
-    for (int q = 0; q < e && mine; q++) mine = R.resv[cell_at(x, y, z, A.t.off_all[q], A.hs)] <= key;
+    const bool mine = cells_mine(A, R.resv, x, y, z, 0, e, 1, key);
     if (R.nwords) R.nwords[r] += (unsigned)e;
     if (!mine) {
       list_push(R.next, R.nnext, r);
@@ -1423,9 +1513,10 @@ k_commit_warp(GrowArgs A, RoundArgs R) {
     const unsigned key = resv_key(*R.tag, r);
     const int e = A.t.start_all[R.gexit[r] + 1];
     bool mine = true;
-    for (int q = lane; q < e && mine; q += 32) mine = R.resv[cell_at(x, y, z, A.t.off_all[q], A.hs)] <= key;
+    for (int qb = 0; qb < e && mine; qb += 32 * RB)          // warp-uniform: all lanes leave together
+      mine = __all_sync(0xffffffffu, cells_mine(A, R.resv, x, y, z, qb + lane, min(qb + 32 * RB, e), 32, key));
     if (lane == 0 && R.nwords) R.nwords[r] += (unsigned)e;
-    if (!__all_sync(0xffffffffu, mine)) {
+    if (!mine) {
       if (lane == 0) R.next[atomicAdd(R.nnext, 1)] = r;
       continue;
     }
@@ -1448,7 +1539,7 @@ k_commit_warp(GrowArgs A, RoundArgs R) {
 }
 
 // round bookkeeping on the device: counters of the growth loop in B_HOSTIO2
-// ([0] grown, [1] error, [2] [3] the two list lengths, [4] warp growth list,
+// ([0] unused, [1] error, [2] [3] the two list lengths, [4] warp growth list,
 // [5] warp commit list, [6..7] byte total, [16] tag, [18..19] peak count)
 constexpr int GROW_TAG = 16, GROW_NP = 18;
 constexpr int GROW_ROUNDS_PER_LAUNCH = 250;     // reservation tags 1..250 (8 bits of the key)
@@ -1480,9 +1571,24 @@ __global__ void k_sum_words(const unsigned* __restrict__ w, int n, unsigned long
   if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
 }
 
-__global__ void k_iota(int* __restrict__ a, int n) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) a[i] = i;
+// The first round's list in cell order: the processed peak of rank r
+// (sorted index np - 1 - r >= L0) at its position among the peaks in cell
+// order (group offset + the mask bits before it), -1 at the others.  Which
+// peak a thread grows does not change any result (reservations decide by
+// rank); in cell order the threads of a warp grow neighbouring peaks, so
+// their shells share sectors in L1 and L2.
+__global__ void k_spatial_list(const unsigned* __restrict__ id, long long np, long long L0,
+                               const unsigned* __restrict__ mask, const unsigned* __restrict__ off,
+                               int* __restrict__ list) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long l = L0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; l < np; l += stride) {
+    const unsigned cell = id[l];
+    const unsigned w = cell >> 5;
+    unsigned p = off[cell / PK_T];
+    for (unsigned q = (cell / PK_T) * (PK_T / 32); q < w; q++) p += __popc(__ldg(&mask[q]));
+    p += __popc(__ldg(&mask[w]) & ((1u << (cell & 31)) - 1u));
+    list[p] = (int)(np - 1 - l);
+  }
 }
 
 __global__ void k_kept(const int* __restrict__ cnt, const unsigned char* __restrict__ state, int nproc, int Nmin,
@@ -1573,17 +1679,26 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   int* gst = kept;
   EXH_TRY(c.buf[B_HOSTIO2].ensure(128));
   int* dcnt = c.buf[B_HOSTIO2].as<int>();
-  // pending peaks as a compacted list (misc and hid serve as the two lists
-  // during the rounds; both are rewritten afterwards); the warp passes'
-  // lists live in the hand-off buffer
-  int* lists[2] = {misc, h->hid};
-  EXH_TRY(c.buf[B_HALO3].ensure(sizeof(int) * 2 * npr));
+  // pending peaks as lists: the first round's in cell order with gaps
+  // (np entries), then compacted lists (hid serves as the second list during
+  // the rounds and is rewritten afterwards); the warp passes' lists and the
+  // first list live in the hand-off buffer, in thirds of its capacity
+  const size_t lcap = std::max<size_t>(npr, (size_t)np);
+  EXH_TRY(c.buf[B_HALO3].ensure(sizeof(int) * 3 * lcap));
+  const size_t third = c.buf[B_HALO3].cap / (3 * sizeof(int));
   int* wlist = c.buf[B_HALO3].as<int>();
-  int* clist = wlist + c.buf[B_HALO3].cap / (2 * sizeof(int));
-  k_iota<<<nb, 128, 0, st>>>(lists[0], (int)nproc);
-  count_launch(1);
+  int* clist = wlist + third;
+  int* lists[2] = {clist + third, h->hid};
   {
-    int init[20] = {0, 0, (int)nproc, 0, 0, 0};
+    unsigned *pmask, *pcnt, *poff;
+    peak_mask_layout(c, ng, &pmask, &pcnt, &poff);
+    EXH_CUDA_TRY(cudaMemsetAsync(lists[0], 0xff, sizeof(int) * (size_t)np, st));
+    k_spatial_list<<<exh_div_up(nproc, 256), 256, 0, st>>>(h->id, np, np - nproc, pmask, poff, lists[0]);
+    count_launch(1);
+    EXH_CUDA_TRY(cudaGetLastError());
+  }
+  {
+    int init[20] = {0, 0, (int)np, 0, 0, 0};
     const long long npl = np;
     std::memcpy(&init[GROW_NP], &npl, sizeof(npl));
     EXH_TRY(upload_small(dcnt, init, sizeof(init), st));
@@ -1599,7 +1714,7 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
     R.tag = dcnt + GROW_TAG;
     R.np = reinterpret_cast<const long long*>(dcnt + GROW_NP);
     R.cnt = h->cnt; R.gtmp = h->gfin; R.gexit = gexit; R.gst = gst; R.gfin = h->gfin;
-    R.npend = dcnt; R.err = dcnt + 1; R.next = lists[cur ^ 1]; R.nnext = dcnt + 3 - cur;
+    R.err = dcnt + 1; R.next = lists[cur ^ 1]; R.nnext = dcnt + 3 - cur;
     R.wlist = wlist; R.nw = dcnt + 4; R.clist = clist; R.nc = dcnt + 5;
     R.nwords = timing_on() ? h->words : nullptr;
     const int* ncur = dcnt + 2 + cur;
@@ -1747,12 +1862,24 @@ int flags_to_reference(const HaloDev& h, size_t ng, int64_t* out_dev, cudaStream
 }
 
 // ------------------------------------------------------------------ masses
+// Compute_Mass (find_halos.c:455-476): halo h takes the h-th draw of the
+// taus stream seeded with the seed; its mass interpolates I(M) between the
+// member count and the next sphere count and inverts I.  Everything that
+// depends on the count alone is tabulated on the host once per set of tables
+// (same double operations as the per-halo evaluation): I at every sphere
+// count, the first sphere-table entry of every count, and the inverse
+// spline's interval coefficients.
 constexpr int MASS_CHUNK = 8;
 
+struct MassTables {
+  const double* Itab;     // I(count * Mcell) per sphere-table entry, NaN outside the spline
+  const int* first;       // count -> first sphere-table entry with that count (< min(nsph, Ncells)), or -1
+  int nsph, Ncells;
+  DevSplineCoef inv;      // M(I)
+};
 
-__global__ void k_masses(const TausJump* __restrict__ J, TausState s0, DevSpline sI, DevSpline sInv, const int* __restrict__ hpeak,
-                         const int* __restrict__ cnt, const unsigned* __restrict__ pid, int64_t np,
-                         const int* __restrict__ spheres, int nsph, int Ncells, float Mcell, int64_t nh,
+__global__ void k_masses(const TausJump* __restrict__ J, TausState s0, MassTables T, const int* __restrict__ hpeak,
+                         const int* __restrict__ cnt, const unsigned* __restrict__ pid, int64_t np, int64_t nh,
                          HaloScalars hs, float* __restrict__ Mh, int* __restrict__ count_out, int* __restrict__ xc,
                          int* __restrict__ err) {
   const int64_t h0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * MASS_CHUNK;
@@ -1766,22 +1893,20 @@ __global__ void k_masses(const TausJump* __restrict__ J, TausState s0, DevSpline
     const double u = taus_u01(taus_next(s));
     const int r = hpeak[h];
     const int count = cnt[r];
-    // Next_Count (find_halos.c:442-452): first table entry equal to count
-    int lo = 0, hi = min(nsph, Ncells);
-    while (lo < hi) {
-      const int mid = (lo + hi) >> 1;
-      if (spheres[mid] < count) lo = mid + 1; else hi = mid;
-    }
-    const int nx = lo + 1;
-    float m;
-    if (lo >= min(nsph, Ncells) || spheres[lo] != count || nx >= nsph) {
+    // Next_Count (find_halos.c:442-452): the first table entry equal to
+    // count, and the entry after it
+    const int lo = (count >= 0 && count <= T.Ncells) ? __ldg(&T.first[count]) : -1;
+    float m = __int_as_float(0x7fc00000);
+    if (lo < 0 || lo + 1 >= T.nsph) {
       bad = 1;
-      m = __int_as_float(0x7fc00000);
     } else {
-      const float m0 = __fmul_rn((float)count, Mcell), m1 = __fmul_rn((float)spheres[nx], Mcell);
-      const double i0 = sI.eval((double)m0, &bad), i1 = sI.eval((double)m1, &bad);
-      const float dt = (float)__dadd_rn(i0, __dmul_rn(__dsub_rn(i1, i0), u));
-      m = (float)sInv.eval((double)dt, &bad);
+      const double i0 = __ldg(&T.Itab[lo]), i1 = __ldg(&T.Itab[lo + 1]);
+      if (isnan(i0) || isnan(i1)) {
+        bad = 1;
+      } else {
+        const float dt = (float)__dadd_rn(i0, __dmul_rn(__dsub_rn(i1, i0), u));
+        m = (float)T.inv.eval((double)dt, &bad);
+      }
     }
     Mh[h] = m;
     count_out[h] = count;
@@ -1800,39 +1925,61 @@ int halo_masses(Ctx& c, const BoxParams& b, const HaloDev& h, const HostTables& 
   TausState s0;
   taus_seed_state((unsigned long)b.seed, s0.s);
   const std::vector<int>& sph = cells_in_spheres();
-  const int Nr = tab.Nr;
-  const size_t bytes = sizeof(TausJump) + sizeof(double) * 6 * Nr + sizeof(int) * sph.size() + 64;
-  // device copies of the jump matrices, the I(M) splines and the sphere
-  // table: uploaded once per distinct set of tables
+  const int Nr = tab.Nr, nsph = (int)sph.size(), Ncells = tab.Ncells;
+  const size_t dbl = 5 * (size_t)Nr + nsph;
+  const size_t bytes = sizeof(TausJump) + 16 + sizeof(double) * dbl + sizeof(int) * ((size_t)Ncells + 1) + 64;
+  // device copies of the jump matrices and the count tables: uploaded once
+  // per distinct set of tables and cell mass
   std::string key(reinterpret_cast<const char*>(tab.M.data()), sizeof(double) * Nr);
   key.append(reinterpret_cast<const char*>(tab.Int.data()), sizeof(double) * Nr);
+  key.append(reinterpret_cast<const char*>(&b.Mcell), sizeof(float));
+  key.append(reinterpret_cast<const char*>(&Ncells), sizeof(int));
   const bool cached = key == c.mass_key && c.buf[B_WORK2].p && c.buf[B_WORK2].cap >= bytes;
   if (!cached) c.mass_key.clear();
   EXH_TRY(c.buf[B_WORK2].ensure(bytes));
   char* base = c.buf[B_WORK2].as<char>();
   TausJump* dJ = reinterpret_cast<TausJump*>(base);
   double* dd = reinterpret_cast<double*>(base + ((sizeof(TausJump) + 15) & ~size_t(15)));
-  int* dsph = reinterpret_cast<int*>(dd + 6 * Nr);
+  int* dfirst = reinterpret_cast<int*>(dd + dbl);
   if (!cached) {
     Spline sI, sInv;
     if (sI.init(tab.M.data(), tab.Int.data(), Nr) != EXH_OK || sInv.init(tab.Int.data(), tab.M.data(), Nr) != EXH_OK) {
       exh_set_error_msg("mass-function integral is not increasing", __FILE__, __LINE__);
       return EXH_E_RANGE;
     }
-    std::vector<double> hd(6 * Nr);
-    std::memcpy(&hd[0], sI.x.data(), sizeof(double) * Nr);
-    std::memcpy(&hd[Nr], sI.y.data(), sizeof(double) * Nr);
-    std::memcpy(&hd[2 * Nr], sI.c.data(), sizeof(double) * Nr);
-    std::memcpy(&hd[3 * Nr], sInv.x.data(), sizeof(double) * Nr);
-    std::memcpy(&hd[4 * Nr], sInv.y.data(), sizeof(double) * Nr);
-    std::memcpy(&hd[5 * Nr], sInv.c.data(), sizeof(double) * Nr);
+    std::vector<double> hd(dbl);
+    std::memcpy(&hd[0], sInv.x.data(), sizeof(double) * Nr);
+    std::memcpy(&hd[Nr], sInv.y.data(), sizeof(double) * Nr);
+    std::memcpy(&hd[2 * Nr], sInv.c.data(), sizeof(double) * Nr);
+    for (int i = 0; i + 1 < Nr; i++) {       // Spline::eval's bb and dd of interval i
+      const double xl = sInv.x[i], dx = sInv.x[i + 1] - xl, dy = sInv.y[i + 1] - sInv.y[i];
+      const double c0 = sInv.c[i], c1 = sInv.c[i + 1];
+      hd[3 * Nr + i] = dy / dx - dx * (c1 + 2.0 * c0) / 3.0;
+      hd[4 * Nr + i] = (c1 - c0) / (3.0 * dx);
+    }
+    hd[4 * Nr - 1] = 0.0;
+    hd[5 * Nr - 1] = 0.0;
+    for (int j = 0; j < nsph; j++) {         // I at each sphere count, as m0 / m1 of the reference
+      int bad = 0;
+      const float m = (float)sph[j] * b.Mcell;
+      const double v = sI.eval((double)m, &bad);
+      hd[5 * Nr + j] = bad ? NAN : v;
+    }
+    std::vector<int> first((size_t)Ncells + 1, -1);
+    for (int j = std::min(nsph, Ncells) - 1; j >= 0; j--)
+      if (sph[j] >= 0 && sph[j] <= Ncells) first[sph[j]] = j;
     EXH_CUDA_TRY(cudaMemcpyAsync(dJ, &J, sizeof(J), cudaMemcpyHostToDevice, st));
     EXH_CUDA_TRY(cudaMemcpyAsync(dd, hd.data(), sizeof(double) * hd.size(), cudaMemcpyHostToDevice, st));
-    EXH_CUDA_TRY(cudaMemcpyAsync(dsph, sph.data(), sizeof(int) * sph.size(), cudaMemcpyHostToDevice, st));
+    EXH_CUDA_TRY(cudaMemcpyAsync(dfirst, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice, st));
     EXH_CUDA_TRY(cudaStreamSynchronize(st));   // the host vectors die here
     c.mass_key = key;
   }
-  DevSpline dI{dd, dd + Nr, dd + 2 * Nr, Nr}, dInv{dd + 3 * Nr, dd + 4 * Nr, dd + 5 * Nr, Nr};
+  MassTables T;
+  T.Itab = dd + 5 * Nr;
+  T.first = dfirst;
+  T.nsph = nsph;
+  T.Ncells = Ncells;
+  T.inv = DevSplineCoef{dd, dd + Nr, dd + 2 * Nr, dd + 3 * Nr, dd + 4 * Nr, Nr};
   EXH_TRY(c.buf[B_HOSTIO2].ensure(64));
   int* derr = c.buf[B_HOSTIO2].as<int>();
   EXH_CUDA_TRY(cudaMemsetAsync(derr, 0, sizeof(int), st));
@@ -1840,8 +1987,8 @@ int halo_masses(Ctx& c, const BoxParams& b, const HaloDev& h, const HostTables& 
   hs.n0 = b.nd[0]; hs.n1 = b.nd[1]; hs.n2 = b.nd[2];
   const int64_t nchunk = (h.nh + MASS_CHUNK - 1) / MASS_CHUNK;
   { KTimer kt(KC_MASS, st, 0.0);
-  k_masses<<<exh_div_up(nchunk, 128), 128, 0, st>>>(dJ, s0, dI, dInv, h.hpeak, h.cnt, h.id, h.np, dsph, (int)sph.size(),
-                                                   tab.Ncells, b.Mcell, h.nh, hs, Mh_dev, count_dev, xc_dev, derr); }
+  k_masses<<<exh_div_up(nchunk, 128), 128, 0, st>>>(dJ, s0, T, h.hpeak, h.cnt, h.id, h.np, h.nh, hs, Mh_dev,
+                                                   count_dev, xc_dev, derr); }
   count_launch(1);
   EXH_CUDA_TRY(cudaGetLastError());
   int herr = 0;

@@ -2,6 +2,7 @@
 // (src/exshalos/box.c:4-68, binding exshalos.c:710-940), Find_Halos on a
 // given grid (exshalos.c:509-610), the Gaussian field alone
 // (exshalos.c:46-121) and the result fetch.
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -81,6 +82,19 @@ int grid_digest(Ctx& c, const float* d, size_t n, cudaStream_t st, unsigned long
 int run_halo_finder(Ctx& c, const BoxParams& b, const float* k, const float* P, int Nk, int setup_fp64,
                     const float* delta, HaloDev* h, ShellTable* t, cudaStream_t st, unsigned long long grid_hash = 0) {
   HostTables& tab = c.halos.tab;
+  // verbose >= 2: wall-clock milliseconds of each stage, the stream
+  // synchronised at every mark (the stages wait on their counters anyway)
+  auto t_mark = std::chrono::steady_clock::now();
+  auto mark = [&](const char* what) -> int {
+    if (c.verbose < 2) return EXH_OK;
+    EXH_CUDA_TRY(cudaStreamSynchronize(st));
+    const auto now = std::chrono::steady_clock::now();
+    printf("  [%s: %.3f ms]\n", what, std::chrono::duration<double, std::milli>(now - t_mark).count());
+    fflush(stdout);
+    t_mark = now;
+    return EXH_OK;
+  };
+  EXH_TRY(mark("before the halo finder"));
   // the tables depend on P(k), the cosmology, the cell and the barrier only:
   // reuse them across realisations (the key holds every input bit)
   std::string key;
@@ -112,10 +126,13 @@ int run_halo_finder(Ctx& c, const BoxParams& b, const float* k, const float* P, 
     h->id = c.peak_id;
   } else {
     c.peak_hash = 0;
+    EXH_TRY(mark("tables"));
     EXH_TRY(find_peaks(c, delta, b, h, st));
     if (c.verbose) { printf("There are %lld peaks\n", (long long)h->np); fflush(stdout); }
+    EXH_TRY(mark("peaks"));
     EXH_TRY(sort_peaks(c, h, st));
     if (c.verbose) { printf("peaks sorted\n"); fflush(stdout); }
+    EXH_TRY(mark("sort"));
     if (grid_hash != 0) {
       c.peak_hash = grid_hash;
       c.peak_nd[0] = b.nd[0]; c.peak_nd[1] = b.nd[1]; c.peak_nd[2] = b.nd[2];
@@ -133,12 +150,14 @@ int run_halo_finder(Ctx& c, const BoxParams& b, const float* k, const float* P, 
   hs.n0 = b.nd[0]; hs.n1 = b.nd[1]; hs.n2 = b.nd[2];
   EXH_TRY(grow_halos(c, delta, b, hs, Btab_dev, *t, h, st));
   if (c.verbose) { printf("There are %lld halos\n", (long long)h->nh); fflush(stdout); }
+  EXH_TRY(mark("growth"));
   const size_t nh = std::max<int64_t>(h->nh, 1);
   EXH_TRY(c.buf[B_MH].ensure((sizeof(float) + 4 * sizeof(int)) * nh));
   float* Mh = c.buf[B_MH].as<float>();
   int* cnt = reinterpret_cast<int*>(Mh + nh);
   int* xc = cnt + nh;
   EXH_TRY(halo_masses(c, b, *h, tab, Mh, cnt, xc, st));
+  EXH_TRY(mark("masses"));
   HaloState& s = c.halos;
   s.nh = h->nh; s.np = h->np; s.nproc = h->nproc;
   s.nd[0] = b.nd[0]; s.nd[1] = b.nd[1]; s.nd[2] = b.nd[2];

@@ -117,4 +117,26 @@ struct DevSpline {
   }
 };
 
+// The same spline with the per-interval coefficients bb, dd formed once on
+// the host (Spline::eval's expressions, the same double operations), so an
+// evaluation is the knot search and the Horner steps only
+struct DevSplineCoef {
+  const double* x;
+  const double* y;
+  const double* c;
+  const double* bb;
+  const double* dd;
+  int n;
+  __device__ double eval(double q, int* bad) const {
+    if (!(q >= x[0] && q <= x[n - 1])) { *bad = 1; return 0.0; }
+    int lo = 0, hi = n - 1;
+    while (hi > lo + 1) {
+      const int mid = (hi + lo) >> 1;
+      if (x[mid] > q) hi = mid; else lo = mid;
+    }
+    const double t = __dsub_rn(q, x[lo]);
+    return __dadd_rn(y[lo], __dmul_rn(t, __dadd_rn(bb[lo], __dmul_rn(t, __dadd_rn(c[lo], __dmul_rn(t, dd[lo]))))));
+  }
+};
+
 }  // namespace exh
