@@ -22,7 +22,7 @@ def _params(**kw):
     return _capi.default_params(**kw)
 
 
-def _fetch_catalogue(nh, ng, want_vel=False, want_grid=False, want_pos=False, want_flag=False, nd=None):
+def _fetch_catalogue(nh, ng, want_vel=False, want_grid=False, want_pos=False, want_flag=False, nd=None, stream=None):
     L = _capi.load()
     # every array is filled completely by exh_halos_fetch
     he = _capi.host_empty
@@ -39,7 +39,7 @@ def _fetch_catalogue(nh, ng, want_vel=False, want_grid=False, want_pos=False, wa
     flag = he(nd, np.int64) if want_flag else None
     _capi.check(L.exh_halos_fetch(_capi.context(), _capi.ptr(out["posh"]), _capi.ptr(velh), _capi.ptr(out["Mh"]),
                                   _capi.ptr(out["x"]), _capi.ptr(out["count"]), _capi.ptr(grid), _capi.ptr(pos),
-                                  _capi.ptr(vel), _capi.ptr(flag), _capi.EXH_MEM_HOST, None))
+                                  _capi.ptr(vel), _capi.ptr(flag), _capi.EXH_MEM_HOST, stream))
     if velh is not None:
         out["velh"] = velh
     if grid is not None:
@@ -55,7 +55,7 @@ def _fetch_catalogue(nh, ng, want_vel=False, want_grid=False, want_pos=False, wa
 
 def halos_box_from_pk(k, P, R_max, Ndx, Ndy, Ndz, Lc, seed, k_smooth, Om0, redshift, dc, Nmin, a, beta, alpha,
                       fixed, phase, OUT_DEN, OUT_LPT, OUT_VEL, DO_2LPT, OUT_FLAG, OUT_PROF, verbose, nthreads,
-                      _catalogue=False, field_stream="taus"):
+                      _catalogue=False, field_stream="taus", stream=None):
     """Halo catalogue from a linear P(k) (exshalos.c:710-940 / box.c:4-68).
 
     Returns the reference's dictionary: "posh", "Mh" always; "velh" with
@@ -65,7 +65,9 @@ def halos_box_from_pk(k, P, R_max, Ndx, Ndy, Ndz, Lc, seed, k_smooth, Om0, redsh
     output is returned.  With _catalogue=True the Lagrangian centre cells "x"
     and member counts "count" are added.  field_stream: "taus" (default: the
     reference's own gsl_rng_taus stream, the reference's realisation for this
-    seed) or "philox" (one counter-based block per Fourier mode).
+    seed) or "philox" (one counter-based block per Fourier mode).  stream: a
+    CUDA stream handle (int) for the device work, None for the default
+    stream; the call returns with the host outputs filled either way.
     """
     k = np.ascontiguousarray(k, dtype=np.float32)
     P = np.ascontiguousarray(P, dtype=np.float32)
@@ -80,11 +82,12 @@ def halos_box_from_pk(k, P, R_max, Ndx, Ndy, Ndz, Lc, seed, k_smooth, Om0, redsh
     L = _capi.load()
     import ctypes as C
     nh = C.c_int64(0)
-    _capi.check(L.exh_halos_box_from_pk(_capi.context(), _capi.ptr(k), _capi.ptr(P), k.size, prm, C.byref(nh), None))
+    _capi.check(L.exh_halos_box_from_pk(_capi.context(), _capi.ptr(k), _capi.ptr(P), k.size, prm, C.byref(nh),
+                                        stream))
     nd = (int(Ndx), int(Ndy), int(Ndz))
     ng = nd[0] * nd[1] * nd[2]
     out = _fetch_catalogue(nh.value, ng, want_vel=bool(OUT_VEL), want_grid=bool(OUT_DEN), want_pos=bool(OUT_LPT),
-                           want_flag=bool(OUT_FLAG), nd=nd)
+                           want_flag=bool(OUT_FLAG), nd=nd, stream=stream)
     if not _catalogue:
         out.pop("x")
         out.pop("count")

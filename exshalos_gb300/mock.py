@@ -40,6 +40,7 @@ def Generate_Halos_Box_from_Pk(
     verbose: bool = False,
     nthreads: int = 1,
     field_stream: str = "taus",
+    stream: Optional[int] = None,
 ) -> Dict[str, np.ndarray]:
     """Halo catalogue in a periodic box from a linear power spectrum.
 
@@ -49,7 +50,8 @@ def Generate_Halos_Box_from_Pk(
     gsl_rng_taus stream seeded with `seed`, drawn in its loop order, so the
     reference's realisation for that seed, up to float rounding of the
     transforms) or "philox" (a counter-based Philox block per Fourier mode
-    keyed by `seed`).
+    keyed by `seed`).  stream: a CUDA stream handle (int) for the device work
+    (None: the default stream); the call returns with the outputs filled.
     """
     precision = _ext.check_precision()
     if precision == 4:
@@ -68,7 +70,7 @@ def Generate_Halos_Box_from_Pk(
         k, P, R_max, np.int32(ndx), np.int32(ndy), np.int32(ndz), Lc, np.int32(seed), k_smooth, Om0, z,
         delta_c, np.int32(Nmin), a, beta, alpha, np.int32(fixed), phase, np.int32(OUT_DEN), np.int32(OUT_LPT),
         np.int32(OUT_VEL), np.int32(DO_2LPT), np.int32(OUT_FLAG), np.int32(OUT_PROF), np.int32(verbose),
-        np.int32(nthreads), field_stream=field_stream)
+        np.int32(nthreads), field_stream=field_stream, stream=stream)
 
 
 def Generate_Halos_Box_from_Grid(

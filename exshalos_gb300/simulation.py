@@ -50,13 +50,15 @@ def Compute_Density_Grid(
     folds: int = 1,
     verbose: bool = False,
     nthreads: int = 1,
+    stream: Optional[int] = None,
 ) -> np.ndarray:
     """Density contrast of a tracer set on an nd^3 grid (simulation.py:9-166).
 
     Windows NGP, CIC, SPHERICAL (R), EXPONENTIAL (R, R_times); masses;
     several tracer types; interlacing; redshift-space shifts along x/y/z;
     folds.  Returns [nd, nd, nd] float32 for one type without interlacing,
-    else [ntypes, interlacing + 1, nd, nd, nd]."""
+    else [ntypes, interlacing + 1, nd, nd, nd].  stream: a CUDA stream handle
+    (int) for the device work, None for the default stream."""
     pos = np.asarray(pos, dtype=np.float32)
     L, R, R_times = np.float32(L), np.float32(R), np.float32(R_times)
     Om0, z = np.float32(Om0), np.float32(z)
@@ -76,7 +78,7 @@ def Compute_Density_Grid(
         return None
     grid = _spec.grid_compute(pos, vel, mass, np.int32(nmass), types, np.int32(ntypes), np.int32(nd), L, Om0, z,
                               np.int32(direction), np.int32(window), R, R_times, np.int32(interlacing),
-                              np.int32(folds), np.int32(verbose), np.int32(nthreads))
+                              np.int32(folds), np.int32(verbose), np.int32(nthreads), stream=stream)
     if not interlacing and ntypes == 1:
         grid = grid.reshape([nd, nd, nd])
     return grid
@@ -96,9 +98,11 @@ def Compute_Power_Spectrum(
     verbose: bool = False,
     nthreads: int = 1,
     ntypes: int = 1,
+    stream: Optional[int] = None,
 ) -> Dict[str, np.ndarray]:
     """Shell-binned power spectrum of a grid (simulation.py:170-311):
-    {"k": mean |k| per bin, "Pk": P(k), "Nk": modes per bin}."""
+    {"k": mean |k| per bin, "Pk": P(k), "Nk": modes per bin}.  stream: a
+    CUDA stream handle (int) for the device work, None for the default stream."""
     if grid.ndim == 3:
         interlacing, ntypes = 0, 1
     elif grid.ndim == 5:
@@ -120,7 +124,7 @@ def Compute_Power_Spectrum(
     direction = _direction_code(direction)
     x = _spec.power_compute(grid, np.int32(ntypes), np.int32(nd), L, np.int32(window), R, np.int32(interlacing),
                             np.int32(Nk), k_min, k_max, np.int32(l_max), np.int32(direction), np.int32(verbose),
-                            np.int32(nthreads))
+                            np.int32(nthreads), stream=stream)
     if ntypes == 1 and l_max == 0:
         x["Pk"] = x["Pk"].reshape([Nk])
     return x
