@@ -552,18 +552,26 @@ k_qs_chunks(SortCtl* ctl, const Seg* __restrict__ next, Seg* __restrict__ segs, 
     }
     int tot;
     const int ex = block_exclusive_scan<int>(n, ws, tot) + carry;
-    if (i < nseg) {
-      cfirst[i] = ex;
-      for (int o = 0; o < n; o++) {
-        if (ex + o < cap_chunks) { cseg[ex + o] = i; coff[ex + o] = o * CH; }
-      }
-    }
+    if (i < nseg) cfirst[i] = ex;
     __syncthreads();
     if (threadIdx.x == 0) carry += tot;
     __syncthreads();
   }
+  if (threadIdx.x == 0) cfirst[nseg] = carry;
+  __syncthreads();
+  // chunk table: every chunk finds its segment by a binary search of the
+  // segments' first chunks
+  const int nch = min(carry, cap_chunks);
+  for (int c = threadIdx.x; c < nch; c += blockDim.x) {
+    int lo = 0, hi = nseg;                        // last segment whose first chunk is <= c
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (cfirst[mid] <= c) lo = mid; else hi = mid;
+    }
+    cseg[c] = lo;
+    coff[c] = (c - cfirst[lo]) * CH;
+  }
   if (threadIdx.x == 0) {
-    cfirst[nseg] = carry;
     if (carry > cap_chunks) ctl->err = 1;
     ctl->nseg = nseg;
     ctl->nch = min(carry, cap_chunks);
@@ -735,16 +743,21 @@ k_qs_small(const Seg* __restrict__ segs, int nseg, SmallSortBuffers bufs, float*
     int sq[IT];
     bool isL[IT];
     int c = 0;
+    int q = 0;
+    {
+      int qh = nc;                              // first q whose last position is >= base
+      while (q < qh) {
+        const int mid = (q + qh) >> 1;
+        if (cur[2 * mid + 1] < base) q = mid + 1; else qh = mid;
+      }
+    }
 #pragma unroll
     for (int u = 0; u < IT; u++) {
       const int p = base + u;
-      int lo = 0, hi = nc;                      // last q with cur[2q] <= p
-      while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (cur[2 * mid] <= p) lo = mid; else hi = mid;
-      }
-      sq[u] = (p < n && cur[2 * lo] <= p && p <= cur[2 * lo + 1]) ? lo : -1;
-      isL[u] = sq[u] >= 0 && p < cur[2 * lo + 1] && ka[p] <= ka[cur[2 * lo + 1]];
+      while (q < nc && cur[2 * q + 1] < p) q++;
+      const bool in = p < n && q < nc && cur[2 * q] <= p;
+      sq[u] = in ? q : -1;
+      isL[u] = in && p < cur[2 * q + 1] && ka[p] <= ka[cur[2 * q + 1]];
       c += isL[u];
     }
     int tot;
@@ -1159,14 +1172,243 @@ __device__ __forceinline__ int fb_ge(FBound b, float t) {
   return -1;
 }
 
-__device__ int grow_warp_f32(const GrowArgs& A, const unsigned* __restrict__ claimed, int x0, int y0, int z0, float pden,
-                             int lane, int& count_out, int& gtmp_out, int& gexit_out) {
+// The same growth with FP64 sums and a bound on the distance to the
+// reference's sequential FP64 loop (its sums are formed in another order):
+// used where the FP32 bound could not decide, so that the exact sequential
+// replay (grow_warp) runs only for a comparison within about 1e-15 of the
+// barrier.  Reference and own roundings of the product, the sums (the
+// reference's n sequential additions, our depth) and the division, at
+// u = 2^-53 (taken as 1.2e-16).
+struct DBound {
+  double f, e;
+};
+__device__ __forceinline__ DBound db_update(DBound prev, int c, double S, double sabs, int depth, int n, int cn,
+                                            double sign) {
+  const double u = 1.2e-16;
+  const double fc = (double)c, fcn = (double)cn;
+  const double prod = __dmul_rn(prev.f, fc);
+  const double res = __ddiv_rn(__dadd_rn(prod, sign * S), fcn);
+  const double mag = fabs(prod) + sabs;
+  double e = prev.e * fc + 2.0 * u * fabs(prod) + (double)(depth + n + 2) * u * mag;
+  e = e / fcn + 2.0 * u * fabs(res);
+  return DBound{res, e * 1.01 + 1e-300};
+}
+__device__ __forceinline__ int db_ge(DBound b, double t) {
+  const double slack = b.e + 2.4e-16 * (fabs(b.f) + fabs(t));
+  if (b.f - t >= slack) return 1;
+  if (t - b.f > slack) return 0;
+  return -1;
+}
+
+// the two bound tiers behind one interface
+template <typename T> struct Tier;
+template <> struct Tier<float> {
+  using B = FBound;
+  __device__ static B init(float v) { return FBound{v, 0.f}; }
+  __device__ static B update(B p, int c, float S, float sa, int depth, int n, int cn, float sign) {
+    return fb_update(p, c, S, sa, depth, n, cn, sign);
+  }
+  __device__ static int ge(B b, float t) { return fb_ge(b, t); }
+};
+template <> struct Tier<double> {
+  using B = DBound;
+  __device__ static B init(float v) { return DBound{(double)v, 0.0}; }
+  __device__ static B update(B p, int c, double S, double sa, int depth, int n, int cn, double sign) {
+    return db_update(p, c, S, sa, depth, n, cn, sign);
+  }
+  __device__ static int ge(B b, float t) { return db_ge(b, (double)t); }
+};
+
+template <typename T> __device__ __forceinline__ T warp_sum_t(T v) {
+#pragma unroll
+  for (int w = 16; w > 0; w >>= 1) v += __shfl_xor_sync(0xffffffffu, v, w);
+  return v;
+}
+
+// Shell sums of the warp growth, kept per warp in shared memory (shell g <
+// GW_CACHE at slot g): the growth loads up to GW_CHUNK cells of consecutive
+// whole shells in one round trip instead of one round trip per shell, and
+// the shrink re-reads nothing.  The sums are of type T (float for the FP32
+// tier, double for the FP64 one) in the same storage.
+constexpr int GW_U = 4;                  // consecutive cells per lane in a chunk
+constexpr int GW_CHUNK = 32 * GW_U;      // cells loaded per round trip
+constexpr int GW_CACHE = 128;            // shells a warp keeps
+struct ShellCache {
+  double sbuf[GW_CACHE], sabuf[GW_CACHE];   // sum and sum of |.| of the shell's densities (T)
+  unsigned short nf[GW_CACHE];              // claimed cells in the shell
+  unsigned char depth[GW_CACHE];            // longest chain of additions that formed the sum
+  int bnd[32];                              // chunk: first cell of each shell, relative
+  template <typename T> __device__ T* s() { return reinterpret_cast<T*>(sbuf); }
+  template <typename T> __device__ T* sa() { return reinterpret_cast<T*>(sabuf); }
+};
+
+// shell g by lane-strided loads (a shell of more than GW_CHUNK cells, or one
+// the cache does not hold)
+template <typename T>
+__device__ __forceinline__ void shell_direct(const GrowArgs& A, const unsigned* __restrict__ claimed, int x0, int y0,
+                                             int z0, int g, int lane, T& s, T& sa, int& nf, int& depth) {
+  const int s0 = A.t.start_cap[g], s1 = A.t.start_cap[g + 1];
+  T ls = 0, lsa = 0;
+  int lf = 0;
+#pragma unroll 4
+  for (int q = s0 + lane; q < s1; q += 32) {
+    const size_t cell = cell_at(x0, y0, z0, A.t.off_cap[q], A.hs);
+    lf += cell_claimed(claimed, cell) ? 1 : 0;
+    const T v = (T)A.delta[cell];
+    ls += v;
+    lsa += v < 0 ? -v : v;
+  }
+  s = warp_sum_t<T>(ls);
+  sa = warp_sum_t<T>(lsa);
+  nf = __reduce_add_sync(0xffffffffu, lf);
+  depth = (s1 - s0 + 31) / 32 + 5;
+}
+
+// Shells g0 .. g0 + K - 1 into the cache: as many whole shells as fit in
+// GW_CHUNK cells (and below GW_CACHE, at most gmax, K <= 31), loaded in one
+// round trip, each lane GW_U consecutive cells; the per-shell sums by a
+// segmented scan (within the lane, then across lanes, then the carry into
+// the lane's first shell): any term passes through at most
+// (GW_U - 1) + 5 + 1 additions.  Returns K (0: shell g0 alone is larger).
+template <typename T>
+__device__ int shell_chunk(const GrowArgs& A, const unsigned* __restrict__ claimed, int x0, int y0, int z0, int g0,
+                           int lane, ShellCache& C) {
+  constexpr unsigned FULL = 0xffffffffu;
+  T* Cs = C.s<T>();
+  T* Csa = C.sa<T>();
+  const int base = A.t.start_cap[g0];
+  const int gk = g0 + lane;                         // lane k: do shells g0 .. g0 + k fit?
+  const bool fit = lane < 31 && gk <= A.t.gmax && gk < GW_CACHE && A.t.start_cap[gk + 1] - base <= GW_CHUNK;
+  const int K = __popc(__ballot_sync(FULL, fit));  // the fits are a prefix of the lanes
+  if (K == 0) return 0;
+  if (lane <= K) C.bnd[lane] = A.t.start_cap[g0 + lane] - base;
+  if (lane < K) {                                   // empty shells (r^2 = 7, 15, ...) keep these
+    Cs[g0 + lane] = 0;
+    Csa[g0 + lane] = 0;
+    C.nf[g0 + lane] = 0;
+    C.depth[g0 + lane] = 1;
+  }
+  __syncwarp();
+  const int nC = C.bnd[K];
+  const int e0 = GW_U * lane;
+  int k = 0;
+  {
+    int hi = K;                                     // last k with bnd[k] <= e0
+    while (hi - k > 1) {
+      const int mid = (k + hi) >> 1;
+      if (C.bnd[mid] <= e0) k = mid; else hi = mid;
+    }
+  }
+  int sh[GW_U];
+#pragma unroll
+  for (int u = 0; u < GW_U; u++) {
+    const int e = e0 + u;
+    while (k + 1 < K && C.bnd[k + 1] <= e) k++;
+    sh[u] = e < nC ? k : K;                         // past the chunk: a segment of its own
+  }
+  T v[GW_U];
+  int f[GW_U];
+#pragma unroll
+  for (int u = 0; u < GW_U; u++) {
+    v[u] = 0;
+    f[u] = 0;
+    if (e0 + u < nC) {
+      const size_t cell = cell_at(x0, y0, z0, A.t.off_cap[base + e0 + u], A.hs);
+      f[u] = cell_claimed(claimed, cell) ? 1 : 0;
+      v[u] = (T)A.delta[cell];
+    }
+  }
+  // runs of one shell within the lane
+  T rs[GW_U], ra[GW_U];
+  int rf[GW_U];
+  rs[0] = v[0]; ra[0] = v[0] < 0 ? -v[0] : v[0]; rf[0] = f[0];
+#pragma unroll
+  for (int u = 1; u < GW_U; u++) {
+    const bool same = sh[u] == sh[u - 1];
+    const T av = v[u] < 0 ? -v[u] : v[u];
+    rs[u] = same ? rs[u - 1] + v[u] : v[u];
+    ra[u] = same ? ra[u - 1] + av : av;
+    rf[u] = same ? rf[u - 1] + f[u] : f[u];
+  }
+  // segmented inclusive scan of the lanes' last runs
+  const int kF = sh[0], kL = sh[GW_U - 1];
+  const int pk = __shfl_up_sync(FULL, kL, 1);
+  int hd = (lane == 0 || kF != kL || pk != kF) ? 1 : 0;
+  T ts = rs[GW_U - 1], ta = ra[GW_U - 1];
+  int tf = rf[GW_U - 1];
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const T ys = __shfl_up_sync(FULL, ts, d), ya = __shfl_up_sync(FULL, ta, d);
+    const int yf = __shfl_up_sync(FULL, tf, d), yh = __shfl_up_sync(FULL, hd, d);
+    if (lane >= d && !hd) {
+      ts = ys + ts;
+      ta = ya + ta;
+      tf = yf + tf;
+      hd = yh;
+    }
+  }
+  // carry into the lane's first shell, then the totals at each shell's last cell
+  const T cs = __shfl_up_sync(FULL, ts, 1), ca = __shfl_up_sync(FULL, ta, 1);
+  const int cf = __shfl_up_sync(FULL, tf, 1);
+  const bool carry = lane > 0 && pk == kF;
+  const int nk = __shfl_down_sync(FULL, kF, 1);
+#pragma unroll
+  for (int u = 0; u < GW_U; u++) {
+    const bool last = (u + 1 < GW_U) ? sh[u + 1] != sh[u] : (lane == 31 || nk != sh[u]);
+    if (last && sh[u] < K) {
+      const bool c = carry && sh[u] == kF;
+      const int g = g0 + sh[u];
+      Cs[g] = c ? cs + rs[u] : rs[u];
+      Csa[g] = c ? ca + ra[u] : ra[u];
+      C.nf[g] = (unsigned short)(c ? cf + rf[u] : rf[u]);
+      C.depth[g] = (unsigned char)(GW_U + 6);
+    }
+  }
+  __syncwarp();
+  return K;
+}
+
+// the sums of shell g for the growth (claimed cells counted) or the shrink;
+// filled: shells 1 .. filled - 1 are in the cache
+template <typename T>
+__device__ __forceinline__ void shell_sums(const GrowArgs& A, const unsigned* __restrict__ claimed, int x0, int y0,
+                                           int z0, int g, int lane, ShellCache& C, int& filled, T& s, T& sa, int& nf,
+                                           int& depth) {
+  if (g >= 1 && g < GW_CACHE) {
+    if (g >= filled) {
+      const int K = shell_chunk<T>(A, claimed, x0, y0, z0, g, lane, C);
+      if (K == 0) {
+        shell_direct<T>(A, claimed, x0, y0, z0, g, lane, s, sa, nf, depth);
+        if (lane == 0) {
+          C.s<T>()[g] = s; C.sa<T>()[g] = sa;
+          C.nf[g] = (unsigned short)min(nf, 65535); C.depth[g] = (unsigned char)min(depth, 255);
+        }
+        __syncwarp();
+        filled = g + 1;
+        return;
+      }
+      filled = g + K;
+    }
+    s = C.s<T>()[g]; sa = C.sa<T>()[g]; nf = C.nf[g]; depth = C.depth[g];
+    return;
+  }
+  shell_direct<T>(A, claimed, x0, y0, z0, g, lane, s, sa, nf, depth);
+}
+
+// Growth and shrink of one peak by a warp with the bound tier T (FP32, or
+// FP64 where FP32 could not decide); 3 when a comparison falls inside the
+// bound (the next tier then redoes the peak).
+template <typename T>
+__device__ int grow_warp_tier(const GrowArgs& A, const unsigned* __restrict__ claimed, int x0, int y0, int z0,
+                              float pden, int lane, ShellCache& C, int& count_out, int& gtmp_out, int& gexit_out) {
+  using TB = Tier<T>;
   const HaloScalars& hs = A.hs;
-  FBound den{pden, 0.f}, den_tmp{pden, 0.f};
+  typename TB::B den = TB::init(pden), den_tmp = TB::init(pden);
   bool rejected = false;                          // den_tmp is the -Mtot case
   int count = 0, count_tmp = 1, grows_tmp = 0, grows = 0;
+  int filled = 1;
   while (true) {
-    int d = rejected ? 0 : fb_ge(den_tmp, hs.Bmin);
+    int d = rejected ? 0 : TB::ge(den_tmp, hs.Bmin);
     if (d < 0) return 3;
     if (!d) break;
     if (count < count_tmp) grows = grows_tmp;
@@ -1179,46 +1421,26 @@ __device__ int grow_warp_f32(const GrowArgs& A, const unsigned* __restrict__ cla
       gexit_out = A.t.gmax;
       return count >= hs.Ncells ? 1 : 2;
     }
-    const int s0 = A.t.start_cap[grows_tmp], s1 = A.t.start_cap[grows_tmp + 1];
-    float s = 0.f, sa = 0.f;
-    bool foreign = false;
-    int steps = 0;
-#pragma unroll 4
-    for (int q = s0 + lane; q < s1; q += 32) {
-      const size_t cell = cell_at(x0, y0, z0, A.t.off_cap[q], hs);
-      if (cell_claimed(claimed, cell)) foreign = true;
-      const float v = A.delta[cell];
-      s += v;
-      sa += fabsf(v);
-      steps++;
-    }
-    const int n = s1 - s0;
+    T s, sa;
+    int nf, depth;
+    shell_sums<T>(A, claimed, x0, y0, z0, grows_tmp, lane, C, filled, s, sa, nf, depth);
+    const int n = A.t.start_cap[grows_tmp + 1] - A.t.start_cap[grows_tmp];
     count_tmp += n;
-    if (__any_sync(0xffffffffu, foreign)) { rejected = true; continue; }
-    s = warp_sum(s);
-    sa = warp_sum(sa);
-    const int depth = (n + 31) / 32 + 5;
-    den_tmp = fb_update(den, count, s, sa, depth, n, count_tmp, 1.f);
+    if (nf > 0) { rejected = true; continue; }
+    den_tmp = TB::update(den, count, s, sa, depth, n, count_tmp, (T)1);
   }
   const int gexit = grows_tmp;
   while (count > 0) {
-    const int d = fb_ge(den, A.Btab[count]);      // shrink while den < B
+    const int d = TB::ge(den, A.Btab[count]);      // shrink while den < B
     if (d < 0) return 3;
     if (d == 1) break;
     count_tmp = count;
-    const int s0 = A.t.start_cap[grows], s1 = A.t.start_cap[grows + 1];
-    float s = 0.f, sa = 0.f;
-#pragma unroll 4
-    for (int q = s0 + lane; q < s1; q += 32) {
-      const float v = A.delta[cell_at(x0, y0, z0, A.t.off_cap[q], hs)];
-      s += v;
-      sa += fabsf(v);
-    }
-    const int n = s1 - s0;
-    s = warp_sum(s);
-    sa = warp_sum(sa);
+    T s, sa;
+    int nf, depth;
+    shell_sums<T>(A, claimed, x0, y0, z0, grows, lane, C, filled, s, sa, nf, depth);
+    const int n = A.t.start_cap[grows + 1] - A.t.start_cap[grows];
     count -= n;
-    if (count > 0) den = fb_update(den, count_tmp, s, sa, (n + 31) / 32 + 5, n, count, -1.f);
+    if (count > 0) den = TB::update(den, count_tmp, s, sa, depth, n, count, (T)-1);
     if (count < count_tmp) grows_tmp = grows;
     grows--;
   }
@@ -1231,27 +1453,72 @@ __device__ int grow_warp_f32(const GrowArgs& A, const unsigned* __restrict__ cla
 constexpr int GROW_T = 256;   // 8 peaks (one per warp) per block
 constexpr int LANE_GMAX = 6;          // shells one thread grows through (81 cells) before a warp takes over
 constexpr int LANE_COMMIT_MAX = 128;  // reserved cells one thread checks and labels
+// Most peaks read shell 1 only (a one-cell halo) and check 7 cells at the
+// commit; a warp whose lanes mix them with larger peaks runs as long as its
+// largest, so the first thread passes stop there and hand the others to a
+// second thread pass, whose warps then hold peaks of similar size.
+constexpr int FIRST_GMAX = 1;         // shells the first growth pass grows through
+constexpr int FIRST_COMMIT_MAX = 7;   // cells the first commit pass checks (r^2 <= 1)
+// The second passes run one thread per peak while many peaks are handed on
+// (throughput); with at most MID_WARP_MAX (growth) or COMMIT_WARP_MAX
+// (commit) the warp passes take them instead, one warp per peak (a round's
+// time is then the longest peak's chain of dependent loads, shorter across a
+// warp).  Thresholds from launch timings of the box_256 workload.
+constexpr int MID_WARP_MAX = 16384;
+constexpr int COMMIT_WARP_MAX = 8192;
 constexpr int GROW_PERSIST = EXH_NUM_SMS * 8;   // blocks of the persistent warp passes
 
 __device__ __forceinline__ unsigned resv_key(int tag, int r) { return ((unsigned)tag << 24) | (0xFFFFFFu - (unsigned)r); }
 
-// warp-aggregated append to a device list
-__device__ __forceinline__ void list_push(int* list, int* n, int v) {
-  const unsigned m = __activemask();
-  const int lane = threadIdx.x & 31;
-  const int leader = __ffs(m) - 1;
-  int base = 0;
-  if (lane == leader) base = atomicAdd(n, __popc(m));
-  base = __shfl_sync(m, base, leader);
-  list[base + __popc(m & ((1u << lane) - 1u))] = v;
+// Appends staged per warp in shared memory: list space is taken 32 entries
+// at a time, one atomic per 32 peaks instead of one per warp and step (the
+// passes of a round hand on a share of nearly every warp's peaks, and the
+// list counters are single words).  Every lane of the warp calls these.
+struct WarpStage {
+  int v[64];
+  int n;
+};
+__device__ __forceinline__ void stage_push(WarpStage& s, int* list, int* cnt, bool flag, int val, int lane) {
+  const unsigned m = __ballot_sync(0xffffffffu, flag);
+  if (!m) return;
+  const int base = s.n;
+  if (flag) s.v[base + __popc(m & ((1u << lane) - 1u))] = val;
+  const int nn = base + __popc(m);
+  __syncwarp();
+  if (nn >= 32) {
+    int g = 0;
+    if (lane == 0) g = atomicAdd(cnt, 32);
+    g = __shfl_sync(0xffffffffu, g, 0);
+    list[g + lane] = s.v[lane];
+    const int rem = nn - 32;
+    const int keep = lane < rem ? s.v[32 + lane] : 0;
+    __syncwarp();
+    if (lane < rem) s.v[lane] = keep;
+    if (lane == 0) s.n = rem;
+  } else if (lane == 0) {
+    s.n = nn;
+  }
+  __syncwarp();
+}
+__device__ __forceinline__ void stage_flush(WarpStage& s, int* list, int* cnt, int lane) {
+  const int nn = s.n;
+  if (nn > 0) {
+    int g = 0;
+    if (lane == 0) g = atomicAdd(cnt, nn);
+    g = __shfl_sync(0xffffffffu, g, 0);
+    if (lane < nn) list[g + lane] = s.v[lane];
+  }
+  __syncwarp();
+  if (lane == 0) s.n = 0;
+  __syncwarp();
 }
 
-// grow_warp_f32 by one thread for the small spheres that most peaks grow:
+// grow_warp_tier<float> by one thread for the small spheres that most peaks grow:
 // the shell sums are sequential (bound depth = cells in the shell).  Returns
-// 3 when a comparison is undecided or the growth would pass shell LANE_GMAX;
-// the warp path then redoes the peak from the start.
+// 3 when a comparison is undecided or the growth would pass shell gmax_lane;
+// a later pass then redoes the peak from the start.
 __device__ int grow_lane_f32(const GrowArgs& A, const unsigned* __restrict__ claimed, int x0, int y0, int z0, float pden,
-                             int& count_out, int& gtmp_out, int& gexit_out) {
+                             int gmax_lane, int& count_out, int& gtmp_out, int& gexit_out) {
   const HaloScalars& hs = A.hs;
   FBound den{pden, 0.f}, den_tmp{pden, 0.f};
   bool rejected = false;
@@ -1270,7 +1537,7 @@ __device__ int grow_lane_f32(const GrowArgs& A, const unsigned* __restrict__ cla
       gexit_out = A.t.gmax;
       return count >= hs.Ncells ? 1 : 2;
     }
-    if (grows_tmp > LANE_GMAX) return 3;
+    if (grows_tmp > gmax_lane) return 3;
     const int s0 = A.t.start_cap[grows_tmp], s1 = A.t.start_cap[grows_tmp + 1];
     float sm = 0.f, sa = 0.f;
     bool foreign = false;
@@ -1330,10 +1597,15 @@ struct RoundArgs {
   int* err;
   int* next;        // peaks left for the next round
   int* nnext;
+  int* mlist;       // peaks handed from the first growth pass to the second
+  int* nm;
   int* wlist;       // peaks handed to the warp growth pass
   int* nw;
+  int* c2list;      // peaks handed from the first commit pass to the second
+  int* nc2;
   int* clist;       // peaks handed to the warp commit pass
   int* nc;
+  int* nexact;      // growths the FP32 bound could not decide (run in FP64)
   unsigned* nwords; // 4-byte words touched per peak (timing only) or null
 };
 
@@ -1390,53 +1662,78 @@ __device__ __forceinline__ unsigned tentative_words(const GrowArgs& A, int ge) {
 // added, and a claimed cell can only stop a growth earlier, so the last shell
 // read (gexit) is an upper bound of the final one, and the cells the peak
 // will flag (r^2 < final grows_tmp <= final gexit) lie inside r^2 < gexit:
-// the peak reserves those cells, its possible writes.  Peaks with larger
-// spheres, or a comparison too close to call in FP32, go to the warp pass.
+// the peak reserves those cells, its possible writes.  FIRST: the round's
+// list, growth through shell FIRST_GMAX, larger peaks to the second pass;
+// second pass: through shell LANE_GMAX, larger peaks (or a comparison too
+// close to call in FP32) to the warp pass.
+template <bool FIRST>
 __global__ void __launch_bounds__(GROW_T)
 k_tentative(GrowArgs A, const int* __restrict__ list, const int* __restrict__ nlist, RoundArgs R) {
-  const int n = *nlist;
+  __shared__ WarpStage stg[GROW_T / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int n = FIRST ? *nlist : *R.nm;
+  const int* lst = FIRST ? list : R.mlist;
+  int* out = FIRST ? R.mlist : R.wlist;
+  int* nout = FIRST ? R.nm : R.nw;
+  if (!FIRST && n <= MID_WARP_MAX) return;   // the warp pass takes them
+  if (lane == 0) stg[warp].n = 0;
+  __syncwarp();
   const int stride = (int)(gridDim.x * blockDim.x);
-  for (int t = (int)(blockIdx.x * (size_t)blockDim.x + threadIdx.x); t < n; t += stride) {
-    const int r = list[t];
-    if (r < 0) continue;                     // first round: a peak below the barrier
-    const int64_t l = *R.np - 1 - r;
-    const unsigned cell0 = A.id[l];
-    if (cell_claimed(R.claimed, cell0)) {    // find_halos.c:233: the peak is already inside a halo
-      R.state[r] = 1;
-      R.cnt[r] = 0;
-      continue;
+  for (int base = (int)(blockIdx.x * (size_t)blockDim.x) + warp * 32; base < n; base += stride) {   // warp-uniform
+    const int t = base + lane;
+    const int r = t < n ? lst[t] : -1;       // first round: -1 also marks a peak below the barrier
+    bool hand_on = false;
+    if (r >= 0) {
+      const int64_t l = *R.np - 1 - r;
+      const unsigned cell0 = A.id[l];
+      if (FIRST && cell_claimed(R.claimed, cell0)) {   // find_halos.c:233: the peak is already inside a halo
+        R.state[r] = 1;
+        R.cnt[r] = 0;
+      } else {
+        int x, y, z;
+        peak_coords(cell0, A.hs, x, y, z);
+        int count, gt, ge;
+        const int st = grow_lane_f32(A, R.claimed, x, y, z, A.key[l], FIRST ? FIRST_GMAX : LANE_GMAX, count, gt, ge);
+        if (st == 3) {
+          hand_on = true;
+        } else {
+          R.cnt[r] = count; R.gtmp[r] = gt; R.gexit[r] = ge; R.gst[r] = st;
+          if (R.nwords) R.nwords[r] += tentative_words(A, ge);
+          const unsigned key = resv_key(*R.tag, r);
+          reserve_cells(A, R.resv, x, y, z, 0, A.t.start_all[ge], 1, key);   // cells it may flag: r^2 < gexit
+        }
+      }
     }
-    int x, y, z;
-    peak_coords(cell0, A.hs, x, y, z);
-    int count, gt, ge;
-    const int st = grow_lane_f32(A, R.claimed, x, y, z, A.key[l], count, gt, ge);
-    if (st == 3) {
-      list_push(R.wlist, R.nw, r);
-      continue;
-    }
-    R.cnt[r] = count; R.gtmp[r] = gt; R.gexit[r] = ge; R.gst[r] = st;
-    if (R.nwords) R.nwords[r] += tentative_words(A, ge);
-    const unsigned key = resv_key(*R.tag, r);
-    reserve_cells(A, R.resv, x, y, z, 0, A.t.start_all[ge], 1, key);   // cells it may flag: r^2 < gexit
+    stage_push(stg[warp], out, nout, hand_on, r, lane);
   }
+  stage_flush(stg[warp], out, nout, lane);
 }
 
 // part 1, warp pass over the peaks the thread pass handed on (persistent)
 __global__ void __launch_bounds__(GROW_T)
 k_tentative_warp(GrowArgs A, RoundArgs R) {
   __shared__ double wb[GROW_T / 32][32];
+  __shared__ ShellCache cache[GROW_T / 32];
   const int lane = threadIdx.x & 31;
   const int nwarps = (int)((gridDim.x * (size_t)blockDim.x) >> 5);
-  const int n = *R.nw;
+  // the first pass's hand-offs when few (the thread pass skipped them), then
+  // the thread pass's
+  const int nmid = *R.nm <= MID_WARP_MAX ? *R.nm : 0;
+  const int n = nmid + *R.nw;
   for (int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5); w < n; w += nwarps) {
-    const int r = R.wlist[w];
+    const int r = w < nmid ? R.mlist[w] : R.wlist[w - nmid];
     const int64_t l = *R.np - 1 - r;
     const unsigned cell0 = A.id[l];
     int x, y, z;
     peak_coords(cell0, A.hs, x, y, z);
     int count, gt, ge;
-    int st = grow_warp_f32(A, R.claimed, x, y, z, A.key[l], lane, count, gt, ge);
-    if (st == 3) st = grow_warp(A, R.claimed, x, y, z, A.key[l], lane, wb[threadIdx.x >> 5], count, gt, ge);
+    ShellCache& C = cache[threadIdx.x >> 5];
+    int st = grow_warp_tier<float>(A, R.claimed, x, y, z, A.key[l], lane, C, count, gt, ge);
+    if (st == 3) st = grow_warp_tier<double>(A, R.claimed, x, y, z, A.key[l], lane, C, count, gt, ge);
+    if (st == 3) {
+      if (lane == 0) atomicAdd(R.nexact, 1);
+      st = grow_warp(A, R.claimed, x, y, z, A.key[l], lane, wb[threadIdx.x >> 5], count, gt, ge);
+    }
     if (lane == 0) { R.cnt[r] = count; R.gtmp[r] = gt; R.gexit[r] = ge; R.gst[r] = st; }
     if (lane == 0 && R.nwords) R.nwords[r] += tentative_words(A, ge);
     const unsigned key = resv_key(*R.tag, r);
@@ -1462,41 +1759,58 @@ __device__ __forceinline__ bool commit_status(const RoundArgs& R, int r) {
 // reserved (may flag) any cell it read (r^2 <= gexit): its tentative result
 // is then the sequential one.  Reservation keys order by round, then rank,
 // so a key above the peak's own is a higher-rank writer of this round.
-// One thread per pending peak with at most LANE_COMMIT_MAX cells read; the
-// others go to the warp pass.
+// FIRST: the round's list, peaks that read at most FIRST_COMMIT_MAX cells,
+// the others to the second pass; second pass: at most LANE_COMMIT_MAX cells,
+// the others to the warp pass.
+template <bool FIRST>
 __global__ void __launch_bounds__(GROW_T)
 k_commit(GrowArgs A, const int* __restrict__ list, const int* __restrict__ nlist, RoundArgs R) {
-  const int n = *nlist;
+  __shared__ WarpStage stg_on[GROW_T / 32], stg_next[GROW_T / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int n = FIRST ? *nlist : *R.nc2;
+  const int* lst = FIRST ? list : R.c2list;
+  int* out = FIRST ? R.c2list : R.clist;
+  int* nout = FIRST ? R.nc2 : R.nc;
+  if (!FIRST && n <= COMMIT_WARP_MAX) return;   // the warp pass takes them
+  if (lane == 0) { stg_on[warp].n = 0; stg_next[warp].n = 0; }
+  __syncwarp();
   const int stride = (int)(gridDim.x * blockDim.x);
-  for (int t = (int)(blockIdx.x * (size_t)blockDim.x + threadIdx.x); t < n; t += stride) {
-    const int r = list[t];
-    if (r < 0 || R.state[r]) continue;     // below the barrier; resolved by the centre test this round
-    const int e = A.t.start_all[R.gexit[r] + 1];
-    if (e > LANE_COMMIT_MAX) {
-      list_push(R.clist, R.nc, r);
-      continue;
+  for (int base = (int)(blockIdx.x * (size_t)blockDim.x) + warp * 32; base < n; base += stride) {   // warp-uniform
+    const int t = base + lane;
+    int r = t < n ? lst[t] : -1;
+    if (r >= 0 && FIRST && R.state[r]) r = -1;     // resolved by the centre test this round
+    bool hand_on = false, retry = false;
+    if (r >= 0) {
+      const int e = A.t.start_all[R.gexit[r] + 1];
+      if (e > (FIRST ? FIRST_COMMIT_MAX : LANE_COMMIT_MAX)) {
+        hand_on = true;
+      } else {
+        const unsigned cell0 = A.id[*R.np - 1 - r];
+        int x, y, z;
+        peak_coords(cell0, A.hs, x, y, z);
+        const unsigned key = resv_key(*R.tag, r);
+        const bool mine = cells_mine(A, R.resv, x, y, z, 0, e, 1, key);
+        if (R.nwords) R.nwords[r] += (unsigned)e;
+        if (!mine) {
+          retry = true;
+        } else if (commit_status(R, r)) {
+          const int we = A.t.start_all[R.gtmp[r]];     // cells with r^2 < grows_tmp
+          for (int q = 0; q < we; q++) {
+            const size_t cq = cell_at(x, y, z, A.t.off_all[q], A.hs);
+            R.flag[cq] = r;
+            claim_cell(R.claimed, cq);
+          }
+          if (R.nwords) R.nwords[r] += (unsigned)we;
+          R.flag[cell0] = -(r + 2);
+          claim_cell(R.claimed, cell0);
+        }
+      }
     }
-    const unsigned cell0 = A.id[*R.np - 1 - r];
-    int x, y, z;
-    peak_coords(cell0, A.hs, x, y, z);
-    const unsigned key = resv_key(*R.tag, r);
-    const bool mine = cells_mine(A, R.resv, x, y, z, 0, e, 1, key);
-    if (R.nwords) R.nwords[r] += (unsigned)e;
-    if (!mine) {
-      list_push(R.next, R.nnext, r);
-      continue;
-    }
-    if (!commit_status(R, r)) continue;
-    const int we = A.t.start_all[R.gtmp[r]];     // cells with r^2 < grows_tmp
-    for (int q = 0; q < we; q++) {
-      const size_t cq = cell_at(x, y, z, A.t.off_all[q], A.hs);
-      R.flag[cq] = r;
-      claim_cell(R.claimed, cq);
-    }
-    if (R.nwords) R.nwords[r] += (unsigned)we;
-    R.flag[cell0] = -(r + 2);
-    claim_cell(R.claimed, cell0);
+    stage_push(stg_on[warp], out, nout, hand_on, r, lane);
+    stage_push(stg_next[warp], R.next, R.nnext, retry, r, lane);
   }
+  stage_flush(stg_on[warp], out, nout, lane);
+  stage_flush(stg_next[warp], R.next, R.nnext, lane);
 }
 
 // part 2, warp pass (persistent) over the peaks handed on by k_commit
@@ -1504,9 +1818,10 @@ __global__ void __launch_bounds__(GROW_T)
 k_commit_warp(GrowArgs A, RoundArgs R) {
   const int lane = threadIdx.x & 31;
   const int nwarps = (int)((gridDim.x * (size_t)blockDim.x) >> 5);
-  const int n = *R.nc;
+  const int nmid = *R.nc2 <= COMMIT_WARP_MAX ? *R.nc2 : 0;
+  const int n = nmid + *R.nc;
   for (int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5); w < n; w += nwarps) {
-    const int r = R.clist[w];
+    const int r = w < nmid ? R.c2list[w] : R.clist[w - nmid];
     const unsigned cell0 = A.id[*R.np - 1 - r];
     int x, y, z;
     peak_coords(cell0, A.hs, x, y, z);
@@ -1540,8 +1855,9 @@ k_commit_warp(GrowArgs A, RoundArgs R) {
 
 // round bookkeeping on the device: counters of the growth loop in B_HOSTIO2
 // ([0] unused, [1] error, [2] [3] the two list lengths, [4] warp growth list,
-// [5] warp commit list, [6..7] byte total, [16] tag, [18..19] peak count)
-constexpr int GROW_TAG = 16, GROW_NP = 18;
+// [5] warp commit list, [6..7] byte total, [10] second growth list, [11]
+// second commit list, [12] FP64 growths, [16] tag, [18..19] peak count)
+constexpr int GROW_TAG = 16, GROW_NP = 18, GROW_NM = 10, GROW_NC2 = 11, GROW_NEXACT = 12;
 constexpr int GROW_ROUNDS_PER_LAUNCH = 250;     // reservation tags 1..250 (8 bits of the key)
 
 // start of a round with current list `cur`: its next list and the warp
@@ -1551,6 +1867,8 @@ __global__ void k_round_begin(int* dcnt, int cur) {
     dcnt[3 - cur] = 0;
     dcnt[4] = 0;
     dcnt[5] = 0;
+    dcnt[GROW_NM] = 0;
+    dcnt[GROW_NC2] = 0;
     dcnt[GROW_TAG] += 1;
   }
 }
@@ -1681,14 +1999,17 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
   int* dcnt = c.buf[B_HOSTIO2].as<int>();
   // pending peaks as lists: the first round's in cell order with gaps
   // (np entries), then compacted lists (hid serves as the second list during
-  // the rounds and is rewritten afterwards); the warp passes' lists and the
-  // first list live in the hand-off buffer, in thirds of its capacity
+  // the rounds and is rewritten afterwards); the hand-off lists of the later
+  // passes and the first list live in the hand-off buffer, in fifths of its
+  // capacity
   const size_t lcap = std::max<size_t>(npr, (size_t)np);
-  EXH_TRY(c.buf[B_HALO3].ensure(sizeof(int) * 3 * lcap));
-  const size_t third = c.buf[B_HALO3].cap / (3 * sizeof(int));
+  EXH_TRY(c.buf[B_HALO3].ensure(sizeof(int) * 5 * lcap));
+  const size_t fifth = c.buf[B_HALO3].cap / (5 * sizeof(int));
   int* wlist = c.buf[B_HALO3].as<int>();
-  int* clist = wlist + third;
-  int* lists[2] = {clist + third, h->hid};
+  int* clist = wlist + fifth;
+  int* mlist = clist + fifth;
+  int* c2list = mlist + fifth;
+  int* lists[2] = {c2list + fifth, h->hid};
   {
     unsigned *pmask, *pcnt, *poff;
     peak_mask_layout(c, ng, &pmask, &pcnt, &poff);
@@ -1716,17 +2037,21 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
     R.cnt = h->cnt; R.gtmp = h->gfin; R.gexit = gexit; R.gst = gst; R.gfin = h->gfin;
     R.err = dcnt + 1; R.next = lists[cur ^ 1]; R.nnext = dcnt + 3 - cur;
     R.wlist = wlist; R.nw = dcnt + 4; R.clist = clist; R.nc = dcnt + 5;
+    R.mlist = mlist; R.nm = dcnt + GROW_NM; R.c2list = c2list; R.nc2 = dcnt + GROW_NC2;
+    R.nexact = dcnt + GROW_NEXACT;
     R.nwords = timing_on() ? h->words : nullptr;
     const int* ncur = dcnt + 2 + cur;
     k_round_begin<<<1, 32, 0, s>>>(dcnt, cur);
-    k_tentative<<<nbl, GROW_T, 0, s>>>(A, lists[cur], ncur, R);
+    k_tentative<true><<<nbl, GROW_T, 0, s>>>(A, lists[cur], ncur, R);
+    k_tentative<false><<<nbl, GROW_T, 0, s>>>(A, lists[cur], ncur, R);
     k_tentative_warp<<<nbl, GROW_T, 0, s>>>(A, R);
-    k_commit<<<nbl, GROW_T, 0, s>>>(A, lists[cur], ncur, R);
+    k_commit<true><<<nbl, GROW_T, 0, s>>>(A, lists[cur], ncur, R);
+    k_commit<false><<<nbl, GROW_T, 0, s>>>(A, lists[cur], ncur, R);
     k_commit_warp<<<nbl, GROW_T, 0, s>>>(A, R);
     EXH_CUDA_TRY(cudaGetLastError());
     return EXH_OK;
   };
-  int hc[6] = {0, 0, 0, 0, 0, 0};
+  int hc[16] = {};
   if (timing_on()) {
     // kernel-class timing: rounds launched one by one, the host checks every
     // few rounds
@@ -1738,7 +2063,7 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
         EXH_CUDA_TRY(cudaMemsetAsync(dcnt + GROW_TAG, 0, sizeof(int), st));
       }
       EXH_TRY(round(cur, st));
-      count_launch(5);
+      count_launch(7);
       cur ^= 1;
       if ((rd + 1) % ROUNDS_PER_CHECK == 0) {
         EXH_CUDA_TRY(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
@@ -1798,8 +2123,11 @@ int grow_halos(Ctx& c, const float* delta, const BoxParams& b, const HaloScalars
       EXH_CUDA_TRY(cudaMemcpyAsync(hc, dcnt, sizeof(hc), cudaMemcpyDeviceToHost, st));
       EXH_CUDA_TRY(cudaMemcpyAsync(&tag, dcnt + GROW_TAG, sizeof(int), cudaMemcpyDeviceToHost, st));
       EXH_CUDA_TRY(cudaStreamSynchronize(st));
-      count_launch(11 * (tag / 2));
-      if (c.verbose > 1) { printf("  growth: %d rounds, %d left\n", tag, hc[2]); fflush(stdout); }
+      count_launch(15 * (tag / 2));
+      if (c.verbose > 1) {
+        printf("  growth: %d rounds, %d left, %d growths in FP64\n", tag, hc[2], hc[GROW_NEXACT]);
+        fflush(stdout);
+      }
       if (hc[1] || hc[2] == 0) break;
       if ((size_t)launch * GROW_ROUNDS_PER_LAUNCH > (size_t)nproc + 2) {
         exh_set_error_msg("halo growth made no progress", __FILE__, __LINE__);
