@@ -489,8 +489,15 @@ k_qs_jump(const Seg* __restrict__ segs, const int* __restrict__ cseg, const int*
 struct SortCtl {
   int nseg, nch, nnext, nsmall, nsingle, err;
   int iters;                   // iterations of the graph's level loop
+  int maxseg;                  // largest segment of the current level
   unsigned long long elems;    // elements partitioned by the level kernels (timing)
 };
+
+// Once every large segment holds at most MID_MAX elements, one block per
+// segment finishes its levels (k_qs_mid) instead of a launch sequence per
+// level: the last levels have few segments and take tens of microseconds
+// each as a level of kernels.
+constexpr int MID_MAX = 32768;
 
 struct SortBufs {
   float* kb[2];
@@ -536,9 +543,9 @@ k_qs_chunks(SortCtl* ctl, const Seg* __restrict__ next, Seg* __restrict__ segs, 
             int* __restrict__ cseg, int* __restrict__ coff, int cap_chunks, cudaGraphConditionalHandle cond,
             int cond_on) {
   __shared__ int ws[32];
-  __shared__ int carry;
+  __shared__ int carry, smax;
   const int nseg = ctl->nnext;
-  if (threadIdx.x == 0) carry = 0;
+  if (threadIdx.x == 0) { carry = 0; smax = 0; }
   __syncthreads();
   for (int base = 0; base < nseg; base += QS_CHUNK_T) {
     const int i = base + threadIdx.x;
@@ -549,6 +556,7 @@ k_qs_chunks(SortCtl* ctl, const Seg* __restrict__ next, Seg* __restrict__ segs, 
       n = (sg.hi - sg.lo + CH - 1) / CH;        // chunks over the elements before the pivot
       segs[i] = sg;
       atomicAdd(&ctl->elems, (unsigned long long)(sg.hi - sg.lo + 1));
+      atomicMax(&smax, sg.hi - sg.lo + 1);
     }
     int tot;
     const int ex = block_exclusive_scan<int>(n, ws, tot) + carry;
@@ -576,11 +584,185 @@ k_qs_chunks(SortCtl* ctl, const Seg* __restrict__ next, Seg* __restrict__ segs, 
     ctl->nseg = nseg;
     ctl->nch = min(carry, cap_chunks);
     ctl->nnext = 0;
+    ctl->maxseg = smax;
     if (cond_on) {
       const int it = ++ctl->iters;
-      cudaGraphSetConditional(cond, (nseg > 0 && ctl->err == 0 && it % SORT_ITERS_PER_LAUNCH != 0) ? 1u : 0u);
+      cudaGraphSetConditional(cond, (nseg > 0 && smax > MID_MAX && ctl->err == 0 && it % SORT_ITERS_PER_LAUNCH != 0)
+                                        ? 1u : 0u);
     }
   }
+}
+
+// The last levels of the large segments (each at most MID_MAX elements), one
+// block per segment: every level partitions all of the block's pending
+// sub-segments (more than SORT_SMALL elements) at once, as k_qs_place does
+// (Lomuto: L elements to the front in order, pivot after them, > elements
+// along their chains), in the ping-pong buffers and with the lam / posl
+// tables in global memory at the segment's positions.  The sub-segments
+// are processed as one concatenated index space in rounds of MID_T x MID_IT
+// elements: one block scan per round gives the L ranks (minus the count
+// before each sub-segment's first element).  Pivots go to their final
+// places; children of at most SORT_SMALL elements go to the block sort's
+// list, single elements to the copy list.  At most n levels.
+constexpr int MID_T = 1024;
+constexpr int MID_IT = 4;
+constexpr int MID_PEND = 32;          // > MID_MAX / (SORT_SMALL + 1) pending sub-segments
+__global__ void __launch_bounds__(MID_T)
+k_qs_mid(const Seg* __restrict__ segs, SortCtl* ctl, SortBufs b, int* __restrict__ lam, int* __restrict__ posl,
+         float* __restrict__ fkey, unsigned* __restrict__ fid, Seg* __restrict__ small, int2* __restrict__ single,
+         int cap_small) {
+  __shared__ int cur[2 * MID_PEND], nxt[4 * MID_PEND], pre[MID_PEND + 1], sbase[2 * MID_PEND];
+  __shared__ int ncur;
+  __shared__ int ws[32];
+  const Seg sg = segs[blockIdx.x];
+  int cb = sg.buf;
+  if (threadIdx.x == 0) { cur[0] = sg.lo; cur[1] = sg.hi; ncur = 1; }
+  __syncthreads();
+  for (int level = 0; level <= sg.hi - sg.lo && ncur > 0; level++) {
+    const int nc = ncur;
+    const float* key = b.kb[cb];
+    const unsigned* id = b.ib[cb];
+    float* okey = b.kb[cb ^ 1];
+    unsigned* oid = b.ib[cb ^ 1];
+    if (threadIdx.x < 32) {                       // prefix of the pending sizes (nc <= MID_PEND)
+      const int lane = threadIdx.x;
+      int v = lane < nc ? cur[2 * lane + 1] - cur[2 * lane] + 1 : 0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+      }
+      pre[lane + 1] = v;
+      if (lane == 0) pre[0] = 0;
+    }
+    __syncthreads();
+    const int total = pre[nc];
+    // pass 1: L flags, L ranks, L elements in place, lam and posl
+    int carry = 0;
+    for (int rb = 0; rb < total; rb += MID_T * MID_IT) {
+      const int i0 = rb + threadIdx.x * MID_IT;
+      int q = 0;
+      {
+        int hi = nc;                              // last q with pre[q] <= i0
+        while (hi - q > 1) {
+          const int mid = (q + hi) >> 1;
+          if (pre[mid] <= i0) q = mid; else hi = mid;
+        }
+      }
+      int sq[MID_IT], pp[MID_IT];
+      bool isL[MID_IT];
+      int c = 0;
+#pragma unroll
+      for (int u = 0; u < MID_IT; u++) {
+        const int i = i0 + u;
+        while (q + 1 < nc && pre[q + 1] <= i) q++;
+        sq[u] = -1;
+        pp[u] = 0;
+        isL[u] = false;
+        if (i < total) {
+          const int p = cur[2 * q] + (i - pre[q]), hi = cur[2 * q + 1];
+          sq[u] = q;
+          pp[u] = p;
+          isL[u] = p < hi && key[p] <= key[hi];
+        }
+        c += isL[u];
+      }
+      int tot;
+      const int r0 = block_exclusive_scan<int>(c, ws, tot) + carry;
+      int r = r0;
+#pragma unroll
+      for (int u = 0; u < MID_IT; u++) {
+        const int q2 = sq[u];
+        if (q2 >= 0) {
+          if (pp[u] == cur[2 * q2]) sbase[2 * q2] = r;
+          if (pp[u] == cur[2 * q2 + 1]) sbase[2 * q2 + 1] = r;
+        }
+        r += isL[u];
+      }
+      __syncthreads();
+      r = r0;
+#pragma unroll
+      for (int u = 0; u < MID_IT; u++) {
+        const int q2 = sq[u];
+        if (q2 >= 0 && pp[u] < cur[2 * q2 + 1]) {
+          const int lo = cur[2 * q2], p = pp[u], rel = r - sbase[2 * q2];
+          if (isL[u]) {
+            okey[lo + rel] = key[p];
+            oid[lo + rel] = id[p];
+            posl[lo + rel] = p - lo;
+          } else {
+            lam[lo + (p - lo - rel)] = rel;
+          }
+        }
+        r += isL[u];
+      }
+      carry += tot;
+      __syncthreads();
+    }
+    // pass 2: the > elements along their chains, pivots to their final places
+    for (int rb = 0; rb < total; rb += MID_T * MID_IT) {
+      const int i0 = rb + threadIdx.x * MID_IT;
+      int q = 0;
+      {
+        int hi = nc;
+        while (hi - q > 1) {
+          const int mid = (q + hi) >> 1;
+          if (pre[mid] <= i0) q = mid; else hi = mid;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < MID_IT; u++) {
+        const int i = i0 + u;
+        while (q + 1 < nc && pre[q + 1] <= i) q++;
+        if (i >= total) continue;
+        const int lo = cur[2 * q], hi = cur[2 * q + 1], p = lo + (i - pre[q]);
+        const int nL = sbase[2 * q + 1] - sbase[2 * q];
+        if (p == hi) {
+          okey[lo + nL] = key[hi];
+          oid[lo + nL] = id[hi];
+          fkey[lo + nL] = key[hi];
+          fid[lo + nL] = id[hi];
+        } else if (!(key[p] <= key[hi])) {
+          const int* ls = lam + lo;
+          const int* ps = posl + lo;
+          const int a = lomuto_g_dest(p - lo, nL, (hi - lo) - nL, [ls](int k) { return ls[k]; },
+                                      [ps](int k) { return ps[k]; });
+          const int dest = (a == nL) ? hi - lo : a;
+          okey[lo + dest] = key[p];
+          oid[lo + dest] = id[p];
+        }
+      }
+    }
+    if (threadIdx.x < nc) {
+      const int q = threadIdx.x, lo = cur[2 * q], hi = cur[2 * q + 1];
+      const int nL = sbase[2 * q + 1] - sbase[2 * q];
+      nxt[4 * q + 0] = lo;
+      nxt[4 * q + 1] = lo + nL - 1;
+      nxt[4 * q + 2] = lo + nL + 1;
+      nxt[4 * q + 3] = hi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int k = 0;
+      for (int q = 0; q < 2 * nc; q++) {
+        const int clo = nxt[2 * q], chi = nxt[2 * q + 1], len = chi - clo + 1;
+        if (len > SORT_SMALL) {
+          if (k < MID_PEND) { cur[2 * k] = clo; cur[2 * k + 1] = chi; k++; }
+          else atomicExch(&ctl->err, 1);
+        } else if (len >= 2) {
+          const int j = atomicAdd(&ctl->nsmall, 1);
+          if (j < cap_small) small[j] = Seg{clo, chi, cb ^ 1, 0}; else atomicExch(&ctl->err, 1);
+        } else if (len == 1) {
+          const int j = atomicAdd(&ctl->nsingle, 1);
+          if (j < cap_small) single[j] = make_int2(clo, cb ^ 1); else atomicExch(&ctl->err, 1);
+        }
+      }
+      ncur = k;
+    }
+    cb ^= 1;
+    __syncthreads();
+  }
+  if (ncur > 0 && threadIdx.x == 0) atomicExch(&ctl->err, 1);
 }
 
 // copy finished single elements into the final arrays
@@ -940,7 +1122,7 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
           EXH_CUDA_TRY(cudaMemcpyAsync(&hc, ctl, sizeof(SortCtl), cudaMemcpyDeviceToHost, st));
           EXH_CUDA_TRY(cudaStreamSynchronize(st));
           if (hc.err) break;
-          if (hc.nseg == 0) {
+          if (hc.nseg == 0 || hc.maxseg <= MID_MAX) {
             kt.bytes = 16.0 * (double)hc.elems;
             break;
           }
@@ -980,9 +1162,20 @@ int sort_peaks(Ctx& c, HaloDev* h, cudaStream_t st) {
         EXH_CUDA_TRY(cudaStreamSynchronize(st));
         count_launch(16 * (hc.iters - done_iters));
         done_iters = hc.iters;
-        if (hc.err || hc.nseg == 0) break;
+        if (hc.err || hc.nseg == 0 || hc.maxseg <= MID_MAX) break;
         if ((size_t)launch * 2 * SORT_ITERS_PER_LAUNCH > (size_t)np + 4) break;
       }
+    }
+    if (!hc.err && hc.nseg > 0 && hc.maxseg <= MID_MAX) {
+      // the remaining large segments, one block each
+      SortBufs mb{{kb[0], kb[1]}, {ib[0], ib[1]}};
+      { KTimer kt(KC_SORT, st, 0.0);
+      k_qs_mid<<<hc.nseg, MID_T, 0, st>>>(d_segs, ctl, mb, lam, j2, fk, fi, d_small, d_single, cap_small); }
+      count_launch(1);
+      EXH_CUDA_TRY(cudaGetLastError());
+      EXH_CUDA_TRY(cudaMemcpyAsync(&hc, ctl, sizeof(SortCtl), cudaMemcpyDeviceToHost, st));
+      EXH_CUDA_TRY(cudaStreamSynchronize(st));
+      hc.nseg = 0;
     }
     if (c.verbose) {
       printf("  sort levels done: %d small segments, %d single\n", hc.nsmall, hc.nsingle);
@@ -1204,6 +1397,7 @@ __device__ __forceinline__ int db_ge(DBound b, double t) {
 template <typename T> struct Tier;
 template <> struct Tier<float> {
   using B = FBound;
+  static constexpr float U = 5.9604645e-08f;           // 2^-24
   __device__ static B init(float v) { return FBound{v, 0.f}; }
   __device__ static B update(B p, int c, float S, float sa, int depth, int n, int cn, float sign) {
     return fb_update(p, c, S, sa, depth, n, cn, sign);
@@ -1212,6 +1406,7 @@ template <> struct Tier<float> {
 };
 template <> struct Tier<double> {
   using B = DBound;
+  static constexpr double U = 1.2e-16;                 // > 2^-53
   __device__ static B init(float v) { return DBound{(double)v, 0.0}; }
   __device__ static B update(B p, int c, double S, double sa, int depth, int n, int cn, double sign) {
     return db_update(p, c, S, sa, depth, n, cn, sign);
@@ -1232,9 +1427,10 @@ template <typename T> __device__ __forceinline__ T warp_sum_t(T v) {
 // tier, double for the FP64 one) in the same storage.
 constexpr int GW_U = 4;                  // consecutive cells per lane in a chunk
 constexpr int GW_CHUNK = 32 * GW_U;      // cells loaded per round trip
-constexpr int GW_CACHE = 128;            // shells a warp keeps
+constexpr int GW_CACHE = 256;            // shells a warp keeps
 struct ShellCache {
-  double sbuf[GW_CACHE], sabuf[GW_CACHE];   // sum and sum of |.| of the shell's densities (T)
+  double sbuf[GW_CACHE], sabuf[GW_CACHE];   // sum and sum of |.| of the shell's densities (T), then their prefixes
+  int cnt[GW_CACHE];                        // cells up to and including the shell (prefix of the shell sizes, + 1)
   unsigned short nf[GW_CACHE];              // claimed cells in the shell
   unsigned char depth[GW_CACHE];            // longest chain of additions that formed the sum
   int bnd[32];                              // chunk: first cell of each shell, relative
@@ -1368,84 +1564,166 @@ __device__ int shell_chunk(const GrowArgs& A, const unsigned* __restrict__ claim
   return K;
 }
 
-// the sums of shell g for the growth (claimed cells counted) or the shrink;
-// filled: shells 1 .. filled - 1 are in the cache
-template <typename T>
-__device__ __forceinline__ void shell_sums(const GrowArgs& A, const unsigned* __restrict__ claimed, int x0, int y0,
-                                           int z0, int g, int lane, ShellCache& C, int& filled, T& s, T& sa, int& nf,
-                                           int& depth) {
-  if (g >= 1 && g < GW_CACHE) {
-    if (g >= filled) {
-      const int K = shell_chunk<T>(A, claimed, x0, y0, z0, g, lane, C);
-      if (K == 0) {
-        shell_direct<T>(A, claimed, x0, y0, z0, g, lane, s, sa, nf, depth);
-        if (lane == 0) {
-          C.s<T>()[g] = s; C.sa<T>()[g] = sa;
-          C.nf[g] = (unsigned short)min(nf, 65535); C.depth[g] = (unsigned char)min(depth, 255);
-        }
-        __syncwarp();
-        filled = g + 1;
-        return;
-      }
-      filled = g + K;
-    }
-    s = C.s<T>()[g]; sa = C.sa<T>()[g]; nf = C.nf[g]; depth = C.depth[g];
-    return;
-  }
-  shell_direct<T>(A, claimed, x0, y0, z0, g, lane, s, sa, nf, depth);
-}
-
 // Growth and shrink of one peak by a warp with the bound tier T (FP32, or
 // FP64 where FP32 could not decide); 3 when a comparison falls inside the
 // bound (the next tier then redoes the peak).
+//
+// The reference's running mean after shells 1..g are accepted is, in exact
+// arithmetic, P_g / C_g with P_g = den_peak + (sum of the densities of
+// shells 1..g) and C_g = 1 + (cells of shells 1..g), whichever way it was
+// reached (grown, or shrunk back from a larger g); its own FP64 recursion
+// stays within (C_g + 2 g + 2) 2^-53 (|den_peak| + SA_g) / C_g of that,
+// SA_g the prefix of the shells' sums of |density|.  A warp takes up to 31
+// consecutive shells at once (lane j: shell g0 + j; a window is the shells
+// of one chunk, so nothing past the stopping shell's chunk is loaded), forms
+// P_g, SA_g and C_g by warp scans (any term of P_g passes through at most D
+// additions: its shell sum's depth, the scan's 5, the FP64 carry from the
+// earlier windows and the rounding to T), and compares P_g / C_g with the
+// barrier with the bound
+// 1.05 (D U_T (|den_peak| + SA_g) / C_g + 2 U_T |den| + the reference's
+// share): the first shell where the sequential loop would stop (the size or
+// table limit, a claimed cell, a mean below the barrier, or a comparison
+// inside the bound) ends the growth.  The shrink then steps down the
+// nonempty shells with the stored prefixes.  The outputs are the sequential
+// loop's (count, the last removed nonempty shell or gexit, gexit).
+// P / C against t with our rounding (D additions at U_T on magnitudes up to
+// pabs + SA, and the division) and the reference's (ref_ops FP64 roundings
+// on magnitudes up to ref_mag)
+template <typename T>
+__device__ __forceinline__ int tier_decide(T P, T SA, int Cg, T pabs, int D, int ref_ops, T ref_mag, float t) {
+  constexpr T U = Tier<T>::U;
+  const T den = P / (T)Cg;
+  const T mag = pabs + SA;
+  const T e = (T)1.05 * (((T)D * U * mag + (T)ref_ops * (T)1.2e-16 * ref_mag) / (T)Cg +
+                         (T)2 * U * (den < 0 ? -den : den)) + (T)1e-30;
+  const T tt = (T)t;
+  const T slack = e + (T)2 * U * ((den < 0 ? -den : den) + (tt < 0 ? -tt : tt));
+  if (den - tt >= slack) return 1;
+  if (tt - den > slack) return 0;
+  return -1;
+}
+
 template <typename T>
 __device__ int grow_warp_tier(const GrowArgs& A, const unsigned* __restrict__ claimed, int x0, int y0, int z0,
                               float pden, int lane, ShellCache& C, int& count_out, int& gtmp_out, int& gexit_out) {
-  using TB = Tier<T>;
+  constexpr unsigned FULL = 0xffffffffu;
   const HaloScalars& hs = A.hs;
-  typename TB::B den = TB::init(pden), den_tmp = TB::init(pden);
-  bool rejected = false;                          // den_tmp is the -Mtot case
-  int count = 0, count_tmp = 1, grows_tmp = 0, grows = 0;
-  int filled = 1;
-  while (true) {
-    int d = rejected ? 0 : TB::ge(den_tmp, hs.Bmin);
+  T* Ps = C.s<T>();
+  T* SAs = C.sa<T>();
+  const T p0 = (T)pden, pabs = p0 < 0 ? -p0 : p0;
+  // the first test of the loop: the peak's own value against the barrier
+  {
+    const int d = tier_decide<T>(p0, (T)0, 1, pabs, 1, 2, pabs, hs.Bmin);
     if (d < 0) return 3;
-    if (!d) break;
-    if (count < count_tmp) grows = grows_tmp;
-    grows_tmp++;
-    den = den_tmp;
-    count = count_tmp;
-    if (count >= hs.Ncells || grows_tmp > A.t.gmax) {
-      count_out = count;
-      gtmp_out = grows_tmp;
-      gexit_out = A.t.gmax;
-      return count >= hs.Ncells ? 1 : 2;
-    }
-    T s, sa;
-    int nf, depth;
-    shell_sums<T>(A, claimed, x0, y0, z0, grows_tmp, lane, C, filled, s, sa, nf, depth);
-    const int n = A.t.start_cap[grows_tmp + 1] - A.t.start_cap[grows_tmp];
-    count_tmp += n;
-    if (nf > 0) { rejected = true; continue; }
-    den_tmp = TB::update(den, count, s, sa, depth, n, count_tmp, (T)1);
+    if (d == 0) { count_out = 0; gtmp_out = 0; gexit_out = 0; return 0; }
   }
-  const int gexit = grows_tmp;
+  __syncwarp();
+  if (lane == 0) { Ps[0] = p0; SAs[0] = (T)0; C.cnt[0] = 1; }
+  // prefixes carried from window to window in FP64: each window's sums
+  // enter them once, so a term's chain of additions does not grow with the
+  // number of windows (depth: its shell sum's, the window scan's 5, the carry
+  // and the rounding of P to T)
+  double carP = (double)p0, carSA = 0.0;
+  int carC = 1, D = 1;
+  int gstar = -1, kind = 0;
+  for (int gw = 1; gstar < 0;) {
+    // the window: the shells of one chunk (at most 128 cells), or one large
+    // shell, or past the table the limit alone
+    int Kw = 1;
+    if (gw <= A.t.gmax) {
+      if (gw >= GW_CACHE) return 3;                    // beyond the cache: the next tier
+      const int K = shell_chunk<T>(A, claimed, x0, y0, z0, gw, lane, C);
+      if (K == 0) {
+        T s1, sa1;
+        int nf1, d1;
+        shell_direct<T>(A, claimed, x0, y0, z0, gw, lane, s1, sa1, nf1, d1);
+        if (lane == 0) {
+          Ps[gw] = s1; SAs[gw] = sa1;
+          C.nf[gw] = (unsigned short)min(nf1, 65535); C.depth[gw] = (unsigned char)min(d1, 255);
+        }
+        __syncwarp();
+      } else {
+        Kw = K;
+      }
+    }
+    const int g = gw + lane;
+    const bool inwin = lane < Kw;
+    const bool exists = inwin && g <= A.t.gmax;
+    T S = 0, sa = 0;
+    int n = 0, nf = 0, dep = 0;
+    if (exists) {
+      S = Ps[g]; sa = SAs[g]; nf = C.nf[g]; dep = C.depth[g];
+      n = A.t.start_cap[g + 1] - A.t.start_cap[g];
+    }
+    T pS = S, pA = sa;
+    int pn = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const T yS = __shfl_up_sync(FULL, pS, o), yA = __shfl_up_sync(FULL, pA, o);
+      const int yn = __shfl_up_sync(FULL, pn, o);
+      if (lane >= o) { pS += yS; pA += yA; pn += yn; }
+    }
+    D = max(D, __reduce_max_sync(FULL, dep) + 8);
+    const T P = (T)(carP + (double)pS), SA = (T)(carSA + (double)pA);
+    const int Cg = carC + pn;
+    // events of shell g, in the sequential loop's order: the limits checked
+    // when shell g - 1 is accepted, a claimed cell in shell g, then the test
+    // of the mean after shell g
+    int ev = 0;
+    if (inwin) {
+      if (!exists) ev = 1;                             // grows_tmp > gmax
+      else if (Cg - n >= hs.Ncells) ev = 1;            // count >= Ncells
+      else if (nf > 0) ev = 2;
+      else {
+        const int d = tier_decide<T>(P, SA, Cg, pabs, D, Cg + 2 * g + 2, pabs + SA, hs.Bmin);
+        ev = d == 0 ? 3 : (d < 0 ? 4 : 0);
+      }
+    }
+    if (exists) { Ps[g] = P; SAs[g] = SA; C.cnt[g] = Cg; }
+    const unsigned evm = __ballot_sync(FULL, ev != 0);
+    if (evm) {
+      const int l = __ffs(evm) - 1;
+      gstar = gw + l;
+      kind = __shfl_sync(FULL, ev, l);
+    } else {
+      carP += (double)__shfl_sync(FULL, pS, Kw - 1);
+      carSA += (double)__shfl_sync(FULL, pA, Kw - 1);
+      carC += __shfl_sync(FULL, pn, Kw - 1);
+    }
+    __syncwarp();
+    gw += Kw;
+  }
+  if (kind == 4) return 3;
+  // accepted shells 1 .. gstar - 1
+  const int count_acc = C.cnt[gstar - 1];
+  if (kind == 1) {
+    count_out = count_acc;
+    gtmp_out = gstar;
+    gexit_out = A.t.gmax;
+    return count_acc >= hs.Ncells ? 1 : 2;
+  }
+  const int gexit = gstar;
+  // grows: the last accepted shell with cells (0: the peak cell)
+  int k = gstar - 1;
+  while (k > 0 && C.cnt[k] == C.cnt[k - 1]) k--;
+  int count = count_acc, gtmp = gexit;
+  // the reference reaches shell k of the shrink by subtracting from the
+  // accepted total: its roundings on the accepted magnitude
+  const int ref_ops = 2 * count_acc + 4 * gstar + 4;
+  const T ref_mag = pabs + SAs[gstar - 1];
   while (count > 0) {
-    const int d = TB::ge(den, A.Btab[count]);      // shrink while den < B
+    const int d = tier_decide<T>(Ps[k], SAs[k], C.cnt[k], pabs, D, ref_ops, ref_mag, A.Btab[count]);   // shrink while den < B
     if (d < 0) return 3;
     if (d == 1) break;
-    count_tmp = count;
-    T s, sa;
-    int nf, depth;
-    shell_sums<T>(A, claimed, x0, y0, z0, grows, lane, C, filled, s, sa, nf, depth);
-    const int n = A.t.start_cap[grows + 1] - A.t.start_cap[grows];
-    count -= n;
-    if (count > 0) den = TB::update(den, count_tmp, s, sa, depth, n, count, (T)-1);
-    if (count < count_tmp) grows_tmp = grows;
-    grows--;
+    gtmp = k;                                          // shell k removed
+    if (k == 0) { count = 0; break; }
+    int j = k - 1;
+    while (j > 0 && C.cnt[j] == C.cnt[j - 1]) j--;    // the next shell down with cells
+    k = j;
+    count = C.cnt[k];
   }
   count_out = count;
-  gtmp_out = grows_tmp;
+  gtmp_out = gtmp;
   gexit_out = gexit;
   return 0;
 }
