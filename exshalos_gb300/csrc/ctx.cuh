@@ -85,6 +85,7 @@ enum BufId {
   B_SCRATCH,      // per-block partials, counters
   B_GAUSS,        // taus field stream: deviates (or phases) in draw order
   B_TAUS,         // taus field stream: jump matrices, per-chunk counts and scans
+  B_HSUM,         // halo sums: the larger halos handed to the warp pass
   B_HOSTIO,       // staging for host pointers
   B_HOSTIO2,
   B_COUNT

@@ -18,6 +18,7 @@
 #include "field.cuh"
 #include "halos.cuh"
 #include "lpt.cuh"
+#include "scan.cuh"
 
 namespace exh {
 
@@ -297,60 +298,110 @@ k_fft_x_poisson(float2* __restrict__ work, RadixPlan pl, const float2* __restric
 
 // ---------------------------------------------------------------- halos
 // Displacement and velocity sums over the member cells of each halo
-// (lpt.c:70-80, 200-210) and the final positions (lpt.c:245-255).  A warp
-// owns 32 consecutive halos: each lane sums its own halo when it has at most
-// 32 cells; larger halos are summed by the whole warp, one after another.
+// (lpt.c:70-80, 200-210) and the final positions (lpt.c:245-255): halos of
+// at most HS_LANE_MAX cells by one thread each, the others by one warp each.
 // The order of every sum is fixed, so the result is deterministic.
+// Halo position (and velocity) from the member sums: cysumf(x Lc + Lc / 2,
+// disp / count, L) per axis, exshalos_h.c:13-19
+__device__ __forceinline__ void halo_write(int64_t h, int cnt, const int xc[3], const double s[3], const double v[3],
+                                           const HaloOut& o) {
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const float disp = (float)s[a];
+    const float xq = (float)((double)((float)xc[a] * o.Lc) + (double)o.Lc / 2.0);
+    float p = xq + disp / (float)cnt;
+    if (p >= o.L[a]) p -= o.L[a];
+    if (p < 0.f) p += o.L[a];
+    o.posh[3 * h + a] = p;
+    if (o.velh) o.velh[3 * h + a] = (float)(v[a] / (double)cnt);
+  }
+}
+
+__device__ __forceinline__ size_t hs_cell(const int* __restrict__ off_all, int q, int xa, int ya, int za, int n0,
+                                          int n1, int n2) {
+  const int pk = off_all[q];
+  const int i = exh_wrap(xa, (pk & 0xff) - 128, n0), j = exh_wrap(ya, ((pk >> 8) & 0xff) - 128, n1),
+            k = exh_wrap(za, ((pk >> 16) & 0xff) - 128, n2);
+  return ((size_t)i * n1 + j) * n2 + k;
+}
+
+__device__ __forceinline__ void hs_centre(const int* __restrict__ hpeak, const int* __restrict__ gfin,
+                                          const unsigned* __restrict__ pid, int64_t np,
+                                          const int* __restrict__ start_all, int64_t h, int n1, int n2, int xc[3],
+                                          int& cnt) {
+  const int r = hpeak[h];
+  const unsigned cell0 = pid[np - 1 - r];
+  xc[2] = (int)(cell0 % n2);
+  const unsigned rr = cell0 / n2;
+  xc[1] = (int)(rr % n1);
+  xc[0] = (int)(rr / n1);
+  cnt = start_all[gfin[r]];
+}
+
+// Member sums of the halos (Compute_Posh, lpt.c:229-255): each member's
+// term in a compensated FP32 sum (FSum), FP64 once per halo.  Most halos are
+// one cell (at box_256, 83 %); a warp whose lanes mixed them with large
+// halos ran as long as its largest, so this pass sums the halos of at most
+// HS_LANE_MAX members, one thread each, and hands the others (one atomic per
+// block) to k_halo_sum_warp.
+constexpr int HS_LANE_MAX = 7;
 __global__ void __launch_bounds__(256)
 k_halo_sum(const int* __restrict__ hpeak, const int* __restrict__ gfin, const unsigned* __restrict__ pid, int64_t np,
            int64_t nh, const int* __restrict__ off_all, const int* __restrict__ start_all, const float* __restrict__ S,
-           const float* __restrict__ V, int n0, int n1, int n2, HaloOut o) {
+           const float* __restrict__ V, int n0, int n1, int n2, HaloOut o, int* __restrict__ big,
+           int* __restrict__ nbig) {
+  __shared__ int ws[32];
+  __shared__ int base;
   const int64_t h = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int lane = threadIdx.x & 31;
   const bool valid = h < nh;
   const size_t ng = (size_t)n0 * n1 * n2;
-  int x0 = 0, y0 = 0, z0 = 0, cnt = 0;
-  if (valid) {
-    const int r = hpeak[h];
-    const unsigned cell0 = pid[np - 1 - r];
-    z0 = (int)(cell0 % n2);
-    const unsigned rr = cell0 / n2;
-    y0 = (int)(rr % n1);
-    x0 = (int)(rr / n1);
-    cnt = start_all[gfin[r]];
-  }
-  // member sums: compensated float per term, FP64 only once per halo (the
-  // FP64 pipe bounded this kernel when every term went through it)
-  double s[3] = {0, 0, 0}, v[3] = {0, 0, 0};
-  auto cell_of = [&](int q, int xa, int ya, int za) {
-    const int pk = off_all[q];
-    const int i = exh_wrap(xa, (pk & 0xff) - 128, n0), j = exh_wrap(ya, ((pk >> 8) & 0xff) - 128, n1),
-              k = exh_wrap(za, ((pk >> 16) & 0xff) - 128, n2);
-    return ((size_t)i * n1 + j) * n2 + k;
-  };
-  const bool small = valid && cnt <= 32;
-  if (small) {
+  int xc[3] = {0, 0, 0}, cnt = 0;
+  if (valid) hs_centre(hpeak, gfin, pid, np, start_all, h, n1, n2, xc, cnt);
+  const bool mine = valid && cnt <= HS_LANE_MAX;
+  if (mine) {
     FSum fs[3], fv[3];
-    for (int q = 0; q < cnt; q++) {
-      const size_t c = cell_of(q, x0, y0, z0);
+#pragma unroll
+    for (int q = 0; q < HS_LANE_MAX; q++) {
+      if (q >= cnt) break;
+      const size_t c = hs_cell(off_all, q, xc[0], xc[1], xc[2], n0, n1, n2);
 #pragma unroll
       for (int a = 0; a < 3; a++) {
         fs[a].add(S[a * ng + c]);
         if (V) fv[a].add(V[a * ng + c]);
       }
     }
+    double s[3], v[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) { s[a] = fs[a].value(); v[a] = fv[a].value(); }
+    halo_write(h, cnt, xc, s, v, o);
   }
-  unsigned big = __ballot_sync(0xffffffffu, valid && !small);
-  while (big) {
-    const int b = __ffs(big) - 1;
-    big &= big - 1;
-    const int bx = __shfl_sync(0xffffffffu, x0, b), by = __shfl_sync(0xffffffffu, y0, b);
-    const int bz = __shfl_sync(0xffffffffu, z0, b), bc = __shfl_sync(0xffffffffu, cnt, b);
+  const int hand = (valid && !mine) ? 1 : 0;
+  int tot;
+  const int ex = block_exclusive_scan<int>(hand, ws, tot);
+  if (threadIdx.x == 0 && tot) base = atomicAdd(nbig, tot);
+  __syncthreads();
+  if (hand) big[base + ex] = (int)h;
+}
+
+// the larger halos, one warp each (persistent): lane-strided compensated
+// sums, the 32 partial values added in FP64 by a butterfly
+__global__ void __launch_bounds__(256)
+k_halo_sum_warp(const int* __restrict__ hpeak, const int* __restrict__ gfin, const unsigned* __restrict__ pid,
+                int64_t np, const int* __restrict__ off_all, const int* __restrict__ start_all,
+                const float* __restrict__ S, const float* __restrict__ V, int n0, int n1, int n2, HaloOut o,
+                const int* __restrict__ big, const int* __restrict__ nbig) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (int)((gridDim.x * (size_t)blockDim.x) >> 5);
+  const int n = *nbig;
+  const size_t ng = (size_t)n0 * n1 * n2;
+  for (int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5); w < n; w += nwarps) {
+    const int64_t h = big[w];
+    int xc[3], cnt;
+    hs_centre(hpeak, gfin, pid, np, start_all, h, n1, n2, xc, cnt);
     FSum fs[3], fv[3];
-    for (int q = lane; q < bc; q += 32) {
-      const size_t c = cell_of(q, bx, by, bz);
+#pragma unroll 4
+    for (int q = lane; q < cnt; q += 32) {
+      const size_t c = hs_cell(off_all, q, xc[0], xc[1], xc[2], n0, n1, n2);
 #pragma unroll
       for (int a = 0; a < 3; a++) {
         fs[a].add(S[a * ng + c]);
@@ -363,25 +414,11 @@ k_halo_sum(const int* __restrict__ hpeak, const int* __restrict__ gfin, const un
 #pragma unroll
     for (int a = 0; a < 3; a++)
 #pragma unroll
-      for (int w = 16; w > 0; w >>= 1) {
-        ts[a] += __shfl_xor_sync(0xffffffffu, ts[a], w);
-        tv[a] += __shfl_xor_sync(0xffffffffu, tv[a], w);
+      for (int ww = 16; ww > 0; ww >>= 1) {
+        ts[a] += __shfl_xor_sync(0xffffffffu, ts[a], ww);
+        tv[a] += __shfl_xor_sync(0xffffffffu, tv[a], ww);
       }
-    if (lane == b)
-      for (int a = 0; a < 3; a++) { s[a] = ts[a]; v[a] = tv[a]; }
-  }
-  if (!valid) return;
-  const int xc[3] = {x0, y0, z0};
-#pragma unroll
-  for (int a = 0; a < 3; a++) {
-    const float disp = (float)s[a];
-    // cysumf(x Lc + Lc/2, disp / count, L), exshalos_h.c:13-19
-    const float xq = (float)((double)((float)xc[a] * o.Lc) + (double)o.Lc / 2.0);
-    float p = xq + disp / (float)cnt;
-    if (p >= o.L[a]) p -= o.L[a];
-    if (p < 0.f) p += o.L[a];
-    o.posh[3 * h + a] = p;
-    if (o.velh) o.velh[3 * h + a] = (float)(v[a] / (double)cnt);
+    if (lane == 0) halo_write(h, cnt, xc, ts, tv, o);
   }
 }
 
@@ -555,12 +592,17 @@ static int lpt_from_phi1(Ctx& c, const BoxParams& b, float k_smooth, bool do2, f
 
 int halo_displacements(Ctx& c, const BoxParams& b, const HaloDev& h, const ShellTable& t, const float* S,
                        const float* V, const HaloOut& o, cudaStream_t st) {
-  (void)c;
   if (h.nh == 0) return EXH_OK;
+  EXH_TRY(c.buf[B_HSUM].ensure(sizeof(int) * ((size_t)h.nh + 64)));
+  int* nbig = c.buf[B_HSUM].as<int>();
+  int* big = nbig + 32;
+  EXH_CUDA_TRY(cudaMemsetAsync(nbig, 0, sizeof(int), st));
   KTimer kt(KC_HALO_DISP, st, 0.0);
   k_halo_sum<<<exh_div_up(h.nh, 256), 256, 0, st>>>(h.hpeak, h.gfin, h.id, h.np, h.nh, t.off_all, t.start_all, S, V,
-                                                    b.nd[0], b.nd[1], b.nd[2], o);
-  count_launch(1);
+                                                    b.nd[0], b.nd[1], b.nd[2], o, big, nbig);
+  k_halo_sum_warp<<<EXH_NUM_SMS * 8, 256, 0, st>>>(h.hpeak, h.gfin, h.id, h.np, t.off_all, t.start_all, S, V,
+                                                  b.nd[0], b.nd[1], b.nd[2], o, big, nbig);
+  count_launch(2);
   EXH_CUDA_TRY(cudaGetLastError());
   return EXH_OK;
 }

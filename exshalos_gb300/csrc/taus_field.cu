@@ -40,7 +40,8 @@ namespace exh {
 
 namespace {
 
-constexpr int TF_CHUNK = 256;     // raw values per thread (even)
+constexpr int TF_CHUNK = 64;      // raw values per thread (even): short chunks, many warps for the
+                                  // dependent double-float chains of the deviates
 constexpr int TF_T = 256;
 
 // columns of J^(TF_CHUNK l) for the lane offsets l = 0..31 of a warp's
