@@ -52,10 +52,11 @@ def test_clock_without_windows_uses_every_sample():
     assert _sampler(lines, []).stop()["samples"] == 3
 
 
-def test_committed_traffic_covers_the_roofline_classes():
+def test_committed_traffic_covers_the_dominant_class():
+    # the bench line's roofline names the strided FFT passes (the class with the most time); its traffic
+    # comes from the committed ncu summary of one strided pass
     t = bench.committed_traffic()
-    for cls in ("fft_strided", "fft_rows", "sort", "grow"):
-        assert cls in t and t[cls] > 1e6, cls
+    assert "fft_strided" in t and 1e6 < t["fft_strided"] < 2e8
 
 
 def test_step_bytes_of_a_256_cube_realisation():
