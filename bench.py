@@ -44,7 +44,7 @@ LATENCY_NOTES = {
     "sort": "latency-bound: exact Lomuto order, dependent L2 loads along the > chains of each level "
             "(eight steps per load through per-level jump tables)",
     "grow": "latency-bound: per-peak shell gathers and reservation rounds",
-    "mass": "FP64 spline evaluations",
+    "mass": "per halo: one taus draw by jump-ahead, count-only tables, inverse-spline knot search and Horner step (FP64)",
     "halo_disp": "per-halo gathers over member cells",
 }
 N_RADII, R_LADDER = 50, 30.0
@@ -392,6 +392,71 @@ def field_stream_summary(k, P, reps=5):
     return res
 
 
+def fft_comparator_summary(sizes=(256, 512), reps=5):
+    """The library's 3-D real FFT beside cuFFT (through torch.fft, which
+    calls it), as a timing and accuracy comparator only: the same seeded
+    float32 field, forward r2c and the r2c + c2r round trip, CUDA events
+    (median of reps after two warm-ups), and both forward transforms
+    against a cuFFT FP64 transform of the same field (relative rms over the
+    half-complex modes).  The library's path uses its own kernels; nothing
+    here feeds it."""
+    import torch
+    from exshalos_gb300 import _capi
+    L_ = _capi.load()
+    ctx = _capi.context()
+    out = {}
+    for nd in sizes:
+        g = torch.Generator(device="cuda").manual_seed(11)
+        x = torch.randn(nd, nd, nd, device="cuda", dtype=torch.float32, generator=g)
+        y = torch.empty(nd, nd, nd, device="cuda", dtype=torch.float32)
+        c = torch.empty(nd, nd, nd // 2 + 1, device="cuda", dtype=torch.complex64)
+
+        def ours_fwd():
+            _capi.check(L_.exh_fft_r2c_3d(ctx, nd, nd, nd, _capi.ptr(x), _capi.ptr(c), None))
+
+        def ours_rt():
+            ours_fwd()
+            _capi.check(L_.exh_fft_c2r_3d(ctx, nd, nd, nd, _capi.ptr(c), _capi.ptr(y), None))
+
+        def cufft_fwd():
+            return torch.fft.rfftn(x)
+
+        def cufft_rt():
+            return torch.fft.irfftn(torch.fft.rfftn(x), s=(nd, nd, nd), norm="forward")
+
+        def timed(f):
+            ts = []
+            for r in range(reps + 2):
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                f()
+                e1.record()
+                torch.cuda.synchronize()
+                if r >= 2:
+                    ts.append(e0.elapsed_time(e1))
+            return round(float(np.median(ts)), 4)
+
+        res = {"ours_r2c_ms": timed(ours_fwd), "cufft_r2c_ms": timed(cufft_fwd),
+               "ours_roundtrip_ms": timed(ours_rt), "cufft_roundtrip_ms": timed(cufft_rt)}
+        ref = torch.fft.rfftn(x.double())
+        den = float(torch.sqrt(torch.mean(torch.abs(ref) ** 2)))
+        ours_fwd()
+        res["ours_r2c_rel_rms_vs_fp64"] = float(torch.sqrt(torch.mean(torch.abs(c.to(torch.complex128) - ref) ** 2))) / den
+        res["cufft_r2c_rel_rms_vs_fp64"] = float(torch.sqrt(torch.mean(torch.abs(cufft_fwd().to(torch.complex128) - ref) ** 2))) / den
+        del ref
+        ours_rt()
+        xs = float(torch.sqrt(torch.mean(x.double() ** 2)))
+        res["ours_roundtrip_rel_rms"] = float(torch.sqrt(torch.mean((y.double() / nd ** 3 - x.double()) ** 2))) / xs
+        res["cufft_roundtrip_rel_rms"] = float(torch.sqrt(torch.mean((cufft_rt().double() / nd ** 3 - x.double()) ** 2))) / xs
+        out[f"fft_{nd}"] = res
+        del x, y, c
+        torch.cuda.empty_cache()
+    out["how"] = ("seeded N(0,1) float32 field; library exh_fft_r2c_3d / exh_fft_c2r_3d (unnormalised, FFTW layout) "
+                  "beside torch.fft.rfftn / irfftn(norm='forward') = cuFFT; forward transforms against cuFFT FP64")
+    return out
+
+
 def batched_summary(k, P, lanes, ws=1, rank=0):
     """Batched workload: 256 realisations with Philox seeds 0..255 and box
     sizes drawn uniformly from {64, 96, 128, 192, 256} (fixed draw), cell
@@ -703,6 +768,7 @@ def run_ours(args, ws, rank, local):
     if rank == 0 and not args.no_accuracy:
         accuracy = accuracy_summary(k, P, done_seeds[0])
     fields = field_stream_summary(k, P) if rank == 0 else None
+    fft_cmp = fft_comparator_summary() if (rank == 0 and not args.no_batched) else None
     batched = None if args.no_batched else batched_summary(k, P, args.lanes, ws=ws, rank=rank)
     differentiable = None if args.no_batched else diff_summary(k, P)
     galaxies = None if args.no_batched else galaxies_summary(k, P, reps=5, cpu=not args.no_cpu_baseline)
@@ -748,6 +814,7 @@ def run_ours(args, ws, rank, local):
         "cpu_baseline": cpu,
         "accuracy": accuracy,
         "field_streams": fields,
+        "fft_comparator": fft_cmp,
         "batched": batched,
         "differentiable": differentiable,
         "galaxies": galaxies,
