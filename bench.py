@@ -663,11 +663,12 @@ def run_ours(args, ws, rank, local):
     # the same seed policy as the reference arm: a realisation whose halo
     # masses leave the mass-function splines is skipped (run_seeds)
     seed0 = 1000 * rank + 1
-    run_seeds(step, args.warmup, seed0 + 500, _capi.HaloRangeError)
-    # the timed seeds are screened in an untimed pass (which also warms the
-    # caches): the timed region then holds exactly `steps` completed
-    # realisations, as the reference arm counts them
+    # the timed seeds are screened in an untimed pass: the timed region then
+    # holds exactly `steps` completed realisations, as the reference arm
+    # counts them.  The warm-up seeds run after it, so that no context enters
+    # the timed region holding the field draws of a timed seed
     _, done_seeds, skipped_seeds = run_seeds(step, args.steps, seed0, _capi.HaloRangeError)
+    run_seeds(step, args.warmup, seed0 + 500, _capi.HaloRangeError)
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()

@@ -6,6 +6,7 @@
 #include <string>
 
 #include "ctx.cuh"
+#include "lpt.cuh"
 #include "spectrum.cuh"
 #include "pipeline.cuh"
 
@@ -77,6 +78,7 @@ int exh_ctx_create(int device, exh_ctx** out) {
 int exh_ctx_destroy(exh_ctx* ctx) {
   if (!ctx) return EXH_OK;
   cudaSetDevice(ctx->c.device);
+  taus_offer_release(ctx->c);        // no other context starts a copy from its buffers after this
   cudaDeviceSynchronize();
   for (size_t i = 0; i < ctx->c.lane_ctx.size(); i++) {
     exh_ctx_destroy(ctx->c.lane_ctx[i]);

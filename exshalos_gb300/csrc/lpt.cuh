@@ -35,7 +35,12 @@ int make_field_modes(Ctx& c, const BoxParams& b, const float* A_dev, int stream,
                      cudaStream_t st, FieldModes* out);
 // the draws of the reference's taus stream for box b and its seed into
 // context memory (*out): deviates, or with `fixed` phases, in draw order
+// (or a copy of another context's draws of the same box and seed, when that
+// context offers them)
 int taus_field_draws(Ctx& c, const BoxParams& b, int fixed, cudaStream_t st, const float** out);
+// withdraw c's offered draws and wait for the copies taken from them (before
+// c's buffers are freed)
+void taus_offer_release(Ctx& c);
 // after the stream of the last taus_field_draws has been synchronised: did
 // its stream hold every draw (EXH_E_RANGE if not)
 int taus_verify(Ctx& c);

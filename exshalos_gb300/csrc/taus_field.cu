@@ -26,7 +26,9 @@
 // a double-float evaluation wherever that decides it, and from the FP64
 // formula for the rest (taus_chunk.h).
 #include <cmath>
+#include <mutex>
 #include <string>
+#include <vector>
 
 #include "ctx.cuh"
 #include "field.cuh"
@@ -224,7 +226,124 @@ __global__ void __launch_bounds__(TF_T) k_taus_phases(const TausJump* __restrict
   }
 }
 
+// The draws of one (box, seed, fixed) are the same in every context, and a
+// mock realisation draws them in two (the halo finder's and the smoothing
+// ladder's, which run side by side).  Each context therefore offers the draws
+// of its last seed to the other contexts of the process on the same device:
+// an entry holds its device pointers (B_GAUSS and the accepted-pair count in
+// B_TAUS), an event recorded on the producing stream once they are written,
+// and one event per copy taken from them.  A context that needs the draws of
+// an offered key waits on that event and copies them (one device-to-device
+// copy instead of the three passes); a context rewrites or frees its own
+// buffers only after withdrawing its entry and ordering its stream after
+// every copy taken (a host wait where the buffers are reallocated).
+struct TausOffer {
+  const Ctx* owner = nullptr;
+  int device = 0;
+  std::string key;
+  const float* draws = nullptr;
+  size_t bytes = 0;
+  const unsigned* have_dev = nullptr;   // accepted pairs (nullptr for phases)
+  long long need = 0;
+  cudaEvent_t ready = nullptr;
+  std::vector<cudaEvent_t> reads;
+};
+
+std::mutex g_offer_mu;
+std::vector<TausOffer> g_offers;
+
+// withdraw c's offer; `st` (or, with host_wait, the host) waits for every
+// copy taken from it
+int offer_withdraw(const Ctx& c, cudaStream_t st, bool host_wait) {
+  std::lock_guard<std::mutex> lk(g_offer_mu);
+  for (size_t i = 0; i < g_offers.size(); i++) {
+    TausOffer& o = g_offers[i];
+    if (o.owner != &c) continue;
+    cudaError_t e = cudaSuccess;
+    for (cudaEvent_t ev : o.reads) {
+      const cudaError_t ei = host_wait ? cudaEventSynchronize(ev) : cudaStreamWaitEvent(st, ev, 0);
+      if (e == cudaSuccess) e = ei;
+      cudaEventDestroy(ev);
+    }
+    cudaEventDestroy(o.ready);
+    g_offers.erase(g_offers.begin() + (long)i);
+    EXH_CUDA_TRY(e);
+    return EXH_OK;
+  }
+  return EXH_OK;
+}
+
+// offer c's draws of `key`, written on `st`
+int offer_publish(const Ctx& c, const std::string& key, const float* draws, size_t bytes, const unsigned* have_dev,
+                  long long need, cudaStream_t st) {
+  cudaEvent_t ev = nullptr;
+  EXH_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  const cudaError_t e = cudaEventRecord(ev, st);
+  if (e != cudaSuccess) {
+    cudaEventDestroy(ev);
+    EXH_CUDA_TRY(e);
+  }
+  TausOffer o;
+  o.owner = &c;
+  o.device = c.device;
+  o.key = key;
+  o.draws = draws;
+  o.bytes = bytes;
+  o.have_dev = have_dev;
+  o.need = need;
+  o.ready = ev;
+  std::lock_guard<std::mutex> lk(g_offer_mu);
+  g_offers.push_back(std::move(o));
+  return EXH_OK;
+}
+
+// copy another context's offered draws of `key` into dev on `st`; *taken is
+// false when no context of this device offers them
+int offer_take(Ctx& c, const std::string& key, float* dev, size_t bytes, cudaStream_t st, bool* taken) {
+  *taken = false;
+  std::lock_guard<std::mutex> lk(g_offer_mu);
+  for (TausOffer& o : g_offers) {
+    if (o.owner == &c || o.device != c.device || o.key != key || o.bytes != bytes) continue;
+    // copies that have completed need no further wait
+    size_t w = 0;
+    for (size_t r = 0; r < o.reads.size(); r++) {
+      if (cudaEventQuery(o.reads[r]) == cudaSuccess) {
+        cudaEventDestroy(o.reads[r]);
+      } else {
+        o.reads[w++] = o.reads[r];
+      }
+    }
+    o.reads.resize(w);
+    cudaGetLastError();
+    if (o.have_dev && !c.taus_have_host)
+      EXH_CUDA_TRY(cudaHostAlloc((void**)&c.taus_have_host, sizeof(unsigned), 0));
+    cudaEvent_t rd = nullptr;
+    EXH_CUDA_TRY(cudaEventCreateWithFlags(&rd, cudaEventDisableTiming));
+    cudaError_t e = cudaStreamWaitEvent(st, o.ready, 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dev, o.draws, bytes, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess && o.have_dev)
+      e = cudaMemcpyAsync(c.taus_have_host, o.have_dev, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaEventRecord(rd, st);
+    if (e != cudaSuccess) {
+      // the copy may have been enqueued: the owner must still wait for it
+      cudaEventDestroy(rd);
+      cudaStreamSynchronize(st);
+      EXH_CUDA_TRY(e);
+    }
+    o.reads.push_back(rd);
+    if (o.have_dev) {
+      c.taus_need = o.need;
+      c.taus_pending = true;
+    }
+    *taken = true;
+    return EXH_OK;
+  }
+  return EXH_OK;
+}
+
 }  // namespace
+
+void taus_offer_release(Ctx& c) { offer_withdraw(c, nullptr, true); }
 
 int taus_field_draws(Ctx& c, const BoxParams& b, int fixed, cudaStream_t st, const float** out) {
   const int n0 = b.nd[0], n1 = b.nd[1], n2 = b.nd[2];
@@ -232,19 +351,33 @@ int taus_field_draws(Ctx& c, const BoxParams& b, int fixed, cudaStream_t st, con
   std::string key;
   const int kv[5] = {n0, n1, n2, b.seed, fixed};
   key.append(reinterpret_cast<const char*>(kv), sizeof(kv));
-  EXH_TRY(c.buf[B_GAUSS].ensure(sizeof(float) * (size_t)G));
-  float* dev = c.buf[B_GAUSS].as<float>();
-  *out = dev;
-  if (key == c.taus_key) return EXH_OK;        // the draws of this seed and box are there already
+  const size_t gbytes = sizeof(float) * (size_t)G;
+  if (key == c.taus_key && c.buf[B_GAUSS].cap >= gbytes) {
+    *out = c.buf[B_GAUSS].as<float>();         // the draws of this seed and box are there already
+    return EXH_OK;
+  }
   c.taus_key.clear();
-  // device copy of the jump matrices (host table of static storage)
   const size_t jbytes = (sizeof(TausJump) + sizeof(LaneJump) + sizeof(LogTables) + 255) / 256 * 256;
   const double p = M_PI / 4.0;                 // polar-method acceptance
   const long long pairs = fixed ? 0 : (long long)std::ceil(G / p + 12.0 * std::sqrt(G * (1.0 - p)) / p + 64.0);
   const long long nraw = fixed ? G : 2 * pairs;
   const int nch = (int)((nraw + TF_CHUNK - 1) / TF_CHUNK);
   const size_t nsc = (size_t)nch / SCAN_TILE + 2;
-  EXH_TRY(c.buf[B_TAUS].ensure(jbytes + sizeof(unsigned) * (6 * (size_t)nch + 2 * nsc + 4)));
+  const size_t tbytes = jbytes + sizeof(unsigned) * (6 * (size_t)nch + 2 * nsc + 4);
+  // another context may still be copying this context's previous draws:
+  // order this stream after those copies (the host, where a buffer is
+  // about to be freed and reallocated)
+  EXH_TRY(offer_withdraw(c, st, gbytes > c.buf[B_GAUSS].cap || tbytes > c.buf[B_TAUS].cap));
+  EXH_TRY(c.buf[B_GAUSS].ensure(gbytes));
+  float* dev = c.buf[B_GAUSS].as<float>();
+  *out = dev;
+  bool taken = false;
+  EXH_TRY(offer_take(c, key, dev, gbytes, st, &taken));
+  if (taken) {
+    c.taus_key = key;
+    return EXH_OK;
+  }
+  EXH_TRY(c.buf[B_TAUS].ensure(tbytes));
   TausJump* dJ = c.buf[B_TAUS].as<TausJump>();
   LaneJump* dL = reinterpret_cast<LaneJump*>(dJ + 1);
   LogTables* dT = reinterpret_cast<LogTables*>(dL + 1);
@@ -263,6 +396,7 @@ int taus_field_draws(Ctx& c, const BoxParams& b, int fixed, cudaStream_t st, con
     k_taus_phases<<<nb, TF_T, 0, st>>>(dJ, dL, s0, G, dev);
     count_launch(1);
     EXH_CUDA_TRY(cudaGetLastError());
+    EXH_TRY(offer_publish(c, key, dev, gbytes, nullptr, 0, st));
     c.taus_key = key;
     return EXH_OK;
   }
@@ -294,6 +428,7 @@ int taus_field_draws(Ctx& c, const BoxParams& b, int fixed, cudaStream_t st, con
   EXH_CUDA_TRY(cudaMemcpyAsync(c.taus_have_host, tot + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
   c.taus_need = G;
   c.taus_pending = true;
+  EXH_TRY(offer_publish(c, key, dev, gbytes, tot + 1, G, st));
   c.taus_key = key;
   return EXH_OK;
 }

@@ -97,3 +97,66 @@ def test_taus_ladder_matches_fp64(orc, pk):
     want = orc.ladder(p, orc.field_modes(p, k, P, stream=0), r["R"], r["B"])
     assert 0.0 < np.mean(want != 255) < 1.0
     assert np.mean(r["cross"] != want) < 1e-3
+
+
+def test_taus_draws_shared_between_contexts(pk):
+    """A context that needs the taus draws another context of the process
+    has just made for the same box and seed copies them instead of running
+    the stream again (fewer launches); the fields stay bit-identical to a
+    fresh context's, also when the offering context moves on to the next
+    seed right after, and after it is destroyed."""
+    import ctypes as C
+
+    import torch
+    from exshalos_gb300 import _capi
+    k, P = pk
+    k, P = k.astype(np.float32), P.astype(np.float32)
+    L = _capi.load()
+    nd, Lc, seed = 64, 4.0, 77
+    ng = nd ** 3
+
+    def make_ctx():
+        h = C.c_void_p()
+        _capi.check(L.exh_ctx_create(0, C.byref(h)))
+        return h
+
+    def field(ctx, s, stream, fixed=0, out=None):
+        prm = _capi.default_params(ndx=nd, ndy=nd, ndz=nd, Lc=Lc, seed=s, fixed=fixed,
+                                   field_stream=_capi.field_stream_code("taus"))
+        g = torch.empty(ng, dtype=torch.float32, device="cuda") if out is None else out
+        l0 = _capi.launch_count()
+        _capi.check(L.exh_density_grid_compute(ctx, _capi.ptr(k), _capi.ptr(P), k.size, prm, _capi.ptr(g),
+                                               _capi.EXH_MEM_DEVICE, C.c_void_p(stream.cuda_stream)))
+        return g, _capi.launch_count() - l0
+
+    a, b, fresh = make_ctx(), make_ctx(), make_ctx()
+    sa, sb, sf = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
+    try:
+        want = {}
+        for fixed in (0, 1):
+            # references first, each drawn by its own context: only the last
+            # draws of a context are offered, and a final unrelated seed
+            # withdraws those before a and b start
+            wf, nf = field(fresh, seed, sf, fixed)
+            wf2, _ = field(fresh, seed + 1, sf, fixed)
+            field(fresh, seed + 100, sf, fixed)
+            torch.cuda.synchronize()
+            want[fixed] = wf2
+            ga, na = field(a, seed, sa, fixed)
+            gb, nb = field(b, seed, sb, fixed)
+            ga2, _ = field(a, seed + 1, sa, fixed)      # a rewrites its draws while b's copy may be in flight
+            torch.cuda.synchronize()
+            assert nb <= na - 1, (nf, na, nb)            # b did not launch the stream's passes again
+            assert torch.equal(ga, wf) and torch.equal(gb, wf) and torch.equal(ga2, wf2)
+        # the offering context goes away: b draws seed + 1 (Gaussian) itself,
+        # with more launches than its copy of the fixed-phase draws took
+        _capi.check(L.exh_ctx_destroy(a))
+        a = None
+        gb3, nb3 = field(b, seed + 1, sb)
+        torch.cuda.synchronize()
+        assert nb3 > nb, (nb3, nb)
+        assert torch.equal(gb3, want[0])
+    finally:
+        for h in (a, b, fresh):
+            if h is not None:
+                L.exh_ctx_destroy(h)
