@@ -65,20 +65,25 @@ struct FsShape {
   static constexpr int R = FS_THREADS / NMAX;                                     // rows per tile
 };
 
-// strided pass over data [outer][n][inner]: tile of W adjacent columns
+// Strided pass over data [outer][n][inner]: a tile of W columns.  Column q
+// of the flattened (outer, inner) index is (q / inner, q % inner), so a tile
+// may end one outer row and start the next (two contiguous runs per row):
+// with inner = n/2 + 1 every tile is full, where tiles within one outer row
+// would leave one column in the last tile of each row.
 template <int N1, int N2, class Src, class Dst>
 __global__ void __launch_bounds__(FS_THREADS, 4)
-k_fft4_strided(Src src, Dst dst, const float2* __restrict__ tw, float sgn, int inner) {
+k_fft4_strided(Src src, Dst dst, const float2* __restrict__ tw, float sgn, int inner, int ncol) {
   using S = FsShape<N1, N2>;
   constexpr int W = S::W;
   __shared__ float2 sm[S::n * W];
-  const int o = blockIdx.y, i0 = blockIdx.x * W;
-  const int nb = min(W, inner - i0);
   const int c = threadIdx.x % W, jj = threadIdx.x / W;
+  const int q = blockIdx.x * W + c;
+  const bool ok = q < ncol;
+  const int o = q / inner, i = q - o * inner;
   if (jj < N2) {
     float2 v[N1];
 #pragma unroll
-    for (int j1 = 0; j1 < N1; j1++) v[j1] = (c < nb) ? src(o, jj + N2 * j1, i0 + c) : make_float2(0.f, 0.f);
+    for (int j1 = 0; j1 < N1; j1++) v[j1] = ok ? src(o, jj + N2 * j1, i) : make_float2(0.f, 0.f);
     RDft<N1>::run(v, sgn, [tw](int m) { return __ldg(&tw[m * N2]); });
 #pragma unroll
     for (int k1 = 0; k1 < N1; k1++) {
@@ -93,9 +98,9 @@ k_fft4_strided(Src src, Dst dst, const float2* __restrict__ tw, float sgn, int i
 #pragma unroll
     for (int j2 = 0; j2 < N2; j2++) u[j2] = sm[(jj * N2 + j2) * W + c];
     RDft<N2>::run(u, sgn, [tw](int m) { return __ldg(&tw[m * N1]); });
-    if (c < nb) {
+    if (ok) {
 #pragma unroll
-      for (int k2 = 0; k2 < N2; k2++) dst(o, jj + N1 * k2, i0 + c, u[k2]);
+      for (int k2 = 0; k2 < N2; k2++) dst(o, jj + N1 * k2, i, u[k2]);
     }
   }
 }
@@ -159,19 +164,21 @@ __device__ __forceinline__ void f512_run(Load ld, float2* sm, const float2* __re
   f512_core(v, sm, tw, sgn, c, q);
 }
 
+// columns over the flattened (outer, inner) index, as k_fft4_strided
 template <class Src, class Dst>
 __global__ void __launch_bounds__(F512_T, 3)
-k_fft8_strided512(Src src, Dst dst, const float2* __restrict__ tw, float sgn, int inner) {
+k_fft8_strided512(Src src, Dst dst, const float2* __restrict__ tw, float sgn, int inner, int ncol) {
   __shared__ float2 sm[(512 + 64) * F512_W];
-  const int o = blockIdx.y, i0 = blockIdx.x * F512_W;
-  const int nb = min(F512_W, inner - i0);
   const int c = threadIdx.x % F512_W, q = threadIdx.x / F512_W;
+  const int col = blockIdx.x * F512_W + c;
+  const bool ok = col < ncol;
+  const int o = col / inner, i = col - o * inner;
   float2 v[8];
-  f512_run([&](int j) { return (c < nb) ? src(o, j, i0 + c) : make_float2(0.f, 0.f); }, sm, tw, sgn, c, q, v);
-  if (c < nb) {
+  f512_run([&](int j) { return ok ? src(o, j, i) : make_float2(0.f, 0.f); }, sm, tw, sgn, c, q, v);
+  if (ok) {
     const int k1 = q >> 3, k2a = q & 7;
 #pragma unroll
-    for (int k2b = 0; k2b < 8; k2b++) dst(o, k1 + 8 * k2a + 64 * k2b, i0 + c, v[k2b]);
+    for (int k2b = 0; k2b < 8; k2b++) dst(o, k1 + 8 * k2a + 64 * k2b, i, v[k2b]);
   }
 }
 
@@ -319,17 +326,17 @@ inline int fs_split(int n) {
 template <class Src, class Dst>
 inline bool launch_fs_strided(Src src, Dst dst, int n, const float2* tw, float sgn, int outer, int inner,
                               cudaStream_t st, cudaError_t* err) {
+  const int ncol = outer * inner;             // at most 512 x 257 x 512 columns
   if (n == 512) {
-    dim3 grid(exh_div_up(inner, F512_W), outer);
-    k_fft8_strided512<Src, Dst><<<grid, F512_T, 0, st>>>(src, dst, tw, sgn, inner);
+    k_fft8_strided512<Src, Dst><<<exh_div_up(ncol, F512_W), F512_T, 0, st>>>(src, dst, tw, sgn, inner, ncol);
     *err = cudaGetLastError();
     return true;
   }
   switch (fs_split(n)) {
 #define X(a, b)                                                                     \
   case a * 1000 + b: {                                                              \
-    dim3 grid(exh_div_up(inner, FsShape<a, b>::W), outer);                           \
-    k_fft4_strided<a, b, Src, Dst><<<grid, FS_THREADS, 0, st>>>(src, dst, tw, sgn, inner); \
+    k_fft4_strided<a, b, Src, Dst><<<exh_div_up(ncol, FsShape<a, b>::W), FS_THREADS, 0, st>>>(src, dst, tw, sgn, \
+                                                                                          inner, ncol); \
     *err = cudaGetLastError();                                                      \
     return true;                                                                    \
   }
