@@ -216,42 +216,71 @@ __host__ __device__ __forceinline__ size_t binw_smem(int NW, int Nk, int nd, int
   return 16 + 16 * (size_t)W + sizeof(float) * (4 * (size_t)NW * Nk + (size_t)(nd / 2 + 2));
 }
 
-__device__ void bin_tile_mirror(const float2* res, int PW, int W, int nb, int i0, int nd, int nc,
-                                const BinParams& bp, void* scratch, double* hP, double* hK, unsigned* hN) {
+// The epilogue in three steps, for blocks that bin several tiles in turn:
+// binw_begin once per block (warp histograms zeroed, the per-entry factors),
+// binw_tile per tile (after a barrier: the tile in res; ends before the
+// block's next barrier), binw_end once (after a barrier: the warp
+// histograms combined into hP, hK).
+struct BinwSmem {
+  float4* colt;      // per column of the tile: ky, kz, column factor, skip flags
+  float* ws;         // 4 NW Nk: the warps' (P sum, P carry, K sum, K carry)
+  float* rowt;       // per entry q: Normk over the entry's window factor
+  size_t stride;     // NW Nk
+};
+
+__device__ __forceinline__ BinwSmem binw_layout(void* scratch, int W, int Nk) {
+  BinwSmem s;
+  s.colt = reinterpret_cast<float4*>((reinterpret_cast<uintptr_t>(scratch) + 15) & ~(uintptr_t)15);
+  s.ws = reinterpret_cast<float*>(s.colt + W);
+  s.stride = (size_t)(blockDim.x >> 5) * Nk;
+  s.rowt = s.ws + 4 * s.stride;
+  return s;
+}
+
+__device__ void binw_begin(const BinwSmem& s, int nd, const BinParams& bp) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int Nk = bp.Nk, E = nd / 2 + 1;
+  const int wq = bp.window == 2 ? 2 : (bp.window == 1 ? 1 : 0);     // W = (wx wy wz)^wq
+  float* Ps = s.ws + (size_t)warp * Nk;
+  for (int b = lane; b < Nk; b += 32) {
+    Ps[b] = 0.f;
+    Ps[s.stride + b] = 0.f;
+    Ps[2 * s.stride + b] = 0.f;
+    Ps[3 * s.stride + b] = 0.f;
+  }
+  for (int q = threadIdx.x; q < E; q += blockDim.x) {
+    float rf = bp.Normk;
+    if (wq) {
+      float sn = sinc_f((float)q * bp.kn * bp.Lb * 0.5f);            // sinc is even: both rows of the entry
+      if (wq == 2) sn = __fmul_rn(sn, sn);
+      rf = __fdiv_rn(bp.Normk, sn);
+    }
+    s.rowt[q] = rf;
+  }
+}
+
+__device__ void binw_tile(const BinwSmem& s, const float2* res, int PW, int nb, int i0, int nd, int nc,
+                          const BinParams& bp, unsigned* hN) {
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, NW = blockDim.x >> 5;
   const int Nk = bp.Nk, h = nd / 2, E = h + 1, G = (E + 31) >> 5;
-  const int wq = bp.window == 2 ? 2 : (bp.window == 1 ? 1 : 0);     // W = (wx wy wz)^wq
-  float4* colt = reinterpret_cast<float4*>((reinterpret_cast<uintptr_t>(scratch) + 15) & ~(uintptr_t)15);
-  float* ws = reinterpret_cast<float*>(colt + W);
-  const size_t stride = (size_t)NW * Nk;
-  float* Ps = ws + (size_t)warp * Nk;
-  float* Pc = Ps + stride;
-  float* Ks = Pc + stride;
-  float* Kc = Ks + stride;
-  float* rowt = ws + 4 * stride;
-  for (int b = lane; b < Nk; b += 32) { Ps[b] = 0.f; Pc[b] = 0.f; Ks[b] = 0.f; Kc[b] = 0.f; }
+  const int wq = bp.window == 2 ? 2 : (bp.window == 1 ? 1 : 0);
+  float* Ps = s.ws + (size_t)warp * Nk;
+  float* Pc = Ps + s.stride;
+  float* Ks = Pc + s.stride;
+  float* Kc = Ks + s.stride;
   for (int t = threadIdx.x; t < nb; t += blockDim.x) {
     const int col = i0 + t, j = col / nc, k = col % nc;
     const float ky = (float)((2 * j < nd) ? j : j - nd) * bp.kn;
     const float kz = (float)((2 * k < nd) ? k : k - nd) * bp.kn;
     float cf = 1.f;
     if (wq) {
-      float s = __fmul_rn(sinc_f(ky * bp.Lb * 0.5f), sinc_f(kz * bp.Lb * 0.5f));
-      if (wq == 2) s = __fmul_rn(s, s);
-      cf = __frcp_rn(s);
+      float sn = __fmul_rn(sinc_f(ky * bp.Lb * 0.5f), sinc_f(kz * bp.Lb * 0.5f));
+      if (wq == 2) sn = __fmul_rn(sn, sn);
+      cf = __frcp_rn(sn);
     }
     const int flag = ((k == 0 || k == h) ? 1 : 0) | ((j == 0 || j == h) ? 2 : 0);
-    colt[t] = make_float4(ky, kz, cf, __int_as_float(flag));
-  }
-  for (int q = threadIdx.x; q < E; q += blockDim.x) {
-    float rf = bp.Normk;
-    if (wq) {
-      float s = sinc_f((float)q * bp.kn * bp.Lb * 0.5f);             // sinc is even: both rows of the entry
-      if (wq == 2) s = __fmul_rn(s, s);
-      rf = __fdiv_rn(bp.Normk, s);
-    }
-    rowt[q] = rf;
+    s.colt[t] = make_float4(ky, kz, cf, __int_as_float(flag));
   }
   __syncthreads();
   const float inv_dk = __frcp_rn(bp.dk);
@@ -262,7 +291,7 @@ __device__ void bin_tile_mirror(const float2* res, int PW, int W, int nb, int i0
     int key = -1, two = 0;
     float pw = 0.f, kk = 0.f;
     if (q < E) {
-      const float4 cq = colt[b];
+      const float4 cq = s.colt[b];
       const int fl = __float_as_int(cq.w);
       const bool fk = fl & 1, fj = fl & 2;
       const int r2 = nd - q;                            // the mirror row, when it is a row other than q
@@ -279,7 +308,7 @@ __device__ void bin_tile_mirror(const float2* res, int PW, int W, int nb, int i0
         if (fr <= BIN_EDGE || fr >= 1.f - BIN_EDGE) fb = floorf(__fdiv_rn(d, bp.dk));
         if (fb >= 0.f && fb < (float)Nk) {
           key = (int)fb;
-          const float sc = __fmul_rn(rowt[q], cq.z);
+          const float sc = __fmul_rn(s.rowt[q], cq.z);
           float p = 0.f;
           if (keep1) {
             const float2 v = res[q * PW + b];
@@ -320,13 +349,16 @@ __device__ void bin_tile_mirror(const float2* res, int PW, int W, int nb, int i0
       atomicAdd(&hN[key], (unsigned)(end - lane) + (unsigned)__popc(tmask & run));
     }
   }
-  __syncthreads();
+}
+
+__device__ void binw_end(const BinwSmem& s, int Nk, double* hP, double* hK) {
+  const int NW = blockDim.x >> 5;
   for (int b = threadIdx.x; b < Nk; b += blockDim.x) {
     float ps = 0.f, pc = 0.f, ks = 0.f, kc = 0.f;
     for (int w = 0; w < NW; w++) {
       const size_t o = (size_t)w * Nk + b;
-      pair_add(ps, pc, ws[o], ws[stride + o]);
-      pair_add(ks, kc, ws[2 * stride + o], ws[3 * stride + o]);
+      pair_add(ps, pc, s.ws[o], s.ws[s.stride + o]);
+      pair_add(ks, kc, s.ws[2 * s.stride + o], s.ws[3 * s.stride + o]);
     }
     hP[b] = (double)ps + (double)pc;
     hK[b] = (double)ks + (double)kc;
@@ -367,7 +399,11 @@ k_fft_x_bin(const float2* __restrict__ work, RadixPlan pl, const float2* __restr
 
 // The same x pass as a four-step register FFT (fft4.cuh) for the lengths it
 // covers: step 1 and the transpose as k_fft4_strided, then the results go
-// back to shared memory in natural order for bin_tile.
+// back to shared memory in natural order for the binning.  One tile per
+// block: at these lengths the epilogue's set-up and combine are small beside
+// the tile, and blocks that bin several tiles in turn (k_fft8_x_bin512) run
+// slower here (fewer resident warps, no overlap of one block's loads with
+// another's binning).
 template <int N1, int N2>
 __global__ void __launch_bounds__(FS_THREADS, 4)
 k_fft4_x_bin(const float2* __restrict__ work, const float2* __restrict__ tw, int nd, int nc, BinParams bp,
@@ -409,9 +445,17 @@ k_fft4_x_bin(const float2* __restrict__ work, const float2* __restrict__ tw, int
 #pragma unroll
     for (int k2 = 0; k2 < N2; k2++) sm[(jj + N1 * k2) * (W + 1) + c] = u[k2];
   }
-  __syncthreads();
-  if (bp.Nk <= BINW_MAX_NK) bin_tile_mirror(sm, W + 1, W, nb, i0, nd, nc, bp, hN + bp.Nk, hP, hK, hN);
-  else bin_tile(sm, W + 1, n, nb, i0, nd, nc, bp, hP, hK, hN);
+  if (bp.Nk <= BINW_MAX_NK) {
+    const BinwSmem bs = binw_layout(hN + bp.Nk, W, bp.Nk);
+    binw_begin(bs, nd, bp);
+    __syncthreads();
+    binw_tile(bs, sm, W + 1, nb, i0, nd, nc, bp, hN);
+    __syncthreads();
+    binw_end(bs, bp.Nk, hP, hK);
+  } else {
+    __syncthreads();
+    bin_tile(sm, W + 1, n, nb, i0, nd, nc, bp, hP, hK, hN);
+  }
   __syncthreads();
   for (int b = threadIdx.x; b < bp.Nk; b += blockDim.x) {
     partP[(size_t)blockIdx.x * bp.Nk + b] = hP[b];
@@ -421,39 +465,66 @@ k_fft4_x_bin(const float2* __restrict__ work, const float2* __restrict__ tw, int
 }
 
 // Length 512: the three radix-8 stages of k_fft8_strided512, the results
-// back in shared memory in natural order for bin_tile.
+// back in shared memory in natural order for the binning.  Each block bins
+// the tiles blockIdx.x * per .. + per - 1 in turn into one set of
+// histograms: with 8-column tiles and up to 256 bins the per-tile histogram
+// set-up, combine and partial sums cost as much as the tile itself (16448
+// tiles wrote 73 MB of partials at 512^3), so they are paid once per block.
 __global__ void __launch_bounds__(F512_T, 2)
 k_fft8_x_bin512(const float2* __restrict__ work, const float2* __restrict__ tw, int nd, int nc, BinParams bp,
-                double* __restrict__ partP, double* __restrict__ partK, unsigned int* __restrict__ partN) {
+                int per, double* __restrict__ partP, double* __restrict__ partK, unsigned int* __restrict__ partN) {
   constexpr int W = F512_W, n = 512;
   extern __shared__ float2 dsm[];
   float2* sm = dsm;                                   // (n + 64) W float2
   double* hP = reinterpret_cast<double*>(sm + (n + 64) * W);
   double* hK = hP + bp.Nk;
   unsigned int* hN = reinterpret_cast<unsigned int*>(hK + bp.Nk);
-  const int inner = nd * nc;
-  const int i0 = blockIdx.x * W;
-  const int nb = min(W, inner - i0);
+  const int inner = nd * nc, ntile = (inner + W - 1) / W;
   const int c = threadIdx.x % W, q = threadIdx.x / W;
+  const bool mirror = bp.Nk <= BINW_MAX_NK;
   for (int b = threadIdx.x; b < bp.Nk; b += blockDim.x) { hP[b] = 0.0; hK[b] = 0.0; hN[b] = 0u; }
-  float2 v[8];
-  f512_run([&](int j) { return (c < nb) ? work[(size_t)j * inner + i0 + c] : make_float2(0.f, 0.f); }, sm, tw,
-           -1.f, c, q, v);
-  __syncthreads();
-  {
-    const int k1 = q >> 3, k2a = q & 7;
-#pragma unroll
-    for (int k2b = 0; k2b < 8; k2b++) sm[(k1 + 8 * k2a + 64 * k2b) * (W + 1) + c] = v[k2b];
+  BinwSmem bs{};
+  if (mirror) {
+    bs = binw_layout(hN + bp.Nk, W, bp.Nk);
+    binw_begin(bs, nd, bp);
   }
-  __syncthreads();
-  if (bp.Nk <= BINW_MAX_NK) bin_tile_mirror(sm, W + 1, W, nb, i0, nd, nc, bp, hN + bp.Nk, hP, hK, hN);
-  else bin_tile(sm, W + 1, n, nb, i0, nd, nc, bp, hP, hK, hN);
+  const int t1 = min(ntile, (int)(blockIdx.x + 1) * per);
+  for (int t = blockIdx.x * per; t < t1; t++) {
+    const int i0 = t * W, nb = min(W, inner - i0);
+    float2 v[8];
+    f512_run([&](int j) { return (c < nb) ? work[(size_t)j * inner + i0 + c] : make_float2(0.f, 0.f); }, sm, tw,
+             -1.f, c, q, v);
+    __syncthreads();
+    {
+      const int k1 = q >> 3, k2a = q & 7;
+#pragma unroll
+      for (int k2b = 0; k2b < 8; k2b++) sm[(k1 + 8 * k2a + 64 * k2b) * (W + 1) + c] = v[k2b];
+    }
+    __syncthreads();
+    if (mirror) binw_tile(bs, sm, W + 1, nb, i0, nd, nc, bp, hN);
+    else bin_tile(sm, W + 1, n, nb, i0, nd, nc, bp, hP, hK, hN);
+    __syncthreads();                                  // the tile and its columns are free again
+  }
+  if (mirror) binw_end(bs, bp.Nk, hP, hK);
   __syncthreads();
   for (int b = threadIdx.x; b < bp.Nk; b += blockDim.x) {
     partP[(size_t)blockIdx.x * bp.Nk + b] = hP[b];
     partK[(size_t)blockIdx.x * bp.Nk + b] = hK[b];
     partN[(size_t)blockIdx.x * bp.Nk + b] = hN[b];
   }
+}
+
+// Tiles per block for a binning x pass of ntile tiles: as many blocks as fit
+// on the GPU at once (one wave), each with an equal share of the tiles.
+template <class K>
+static cudaError_t bin_blocks(K kernel, int threads, size_t smem, int ntile, int* per, int* grid) {
+  int fit = 0;
+  const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kernel, threads, smem);
+  if (e != cudaSuccess) return e;
+  const int resident = (fit > 0 ? fit : 1) * EXH_NUM_SMS;
+  *per = (ntile + resident - 1) / resident;
+  *grid = (ntile + *per - 1) / *per;
+  return cudaSuccess;
 }
 
 // launches k_fft4_x_bin (k_fft8_x_bin512 for 512) for the lengths with a
@@ -464,13 +535,16 @@ static cudaError_t launch_fs_x_bin(const float2* work, const float2* tw, int nd,
   *nblk = 0;
   const int inner = nd * nc;
   if (nd == 512) {
-    const int nb = (int)exh_div_up(inner, F512_W);
-    if (nb > nblk_cap) return cudaSuccess;
+    const int ntile = (int)exh_div_up(inner, F512_W);
     size_t sm = sizeof(float2) * (512 + 64) * F512_W + (size_t)bp.Nk * (2 * sizeof(double) + sizeof(unsigned)) + 16;
     if (bp.Nk <= BINW_MAX_NK) sm += binw_smem(F512_T / 32, bp.Nk, 512, F512_W);
     cudaError_t e = set_smem(k_fft8_x_bin512, sm);
     if (e != cudaSuccess) return e;
-    k_fft8_x_bin512<<<nb, F512_T, sm, st>>>(work, tw, nd, nc, bp, partP, partK, partN);
+    int per = 0, nb = 0;
+    e = bin_blocks(k_fft8_x_bin512, F512_T, sm, ntile, &per, &nb);
+    if (e != cudaSuccess) return e;
+    if (nb > nblk_cap) return cudaSuccess;
+    k_fft8_x_bin512<<<nb, F512_T, sm, st>>>(work, tw, nd, nc, bp, per, partP, partK, partN);
     *nblk = nb;
     return cudaGetLastError();
   }
@@ -478,14 +552,14 @@ static cudaError_t launch_fs_x_bin(const float2* work, const float2* tw, int nd,
 #define X(A_, B_)                                                                                        \
   case A_ * 1000 + B_: {                                                                                 \
     using S = FsShape<A_, B_>;                                                                           \
-    const int nb = (int)exh_div_up(inner, S::W);                                                         \
-    if (nb > nblk_cap) return cudaSuccess;                                                               \
+    const int ntile = (int)exh_div_up(inner, S::W);                                                      \
     size_t sm = sizeof(float2) * S::n * (S::W + 1) + (size_t)bp.Nk * (2 * sizeof(double) + sizeof(unsigned)) + 16; \
     if (bp.Nk <= BINW_MAX_NK) sm += binw_smem(FS_THREADS / 32, bp.Nk, S::n, S::W);                      \
     cudaError_t e = set_smem(k_fft4_x_bin<A_, B_>, sm);                                                  \
     if (e != cudaSuccess) return e;                                                                      \
-    k_fft4_x_bin<A_, B_><<<nb, FS_THREADS, sm, st>>>(work, tw, nd, nc, bp, partP, partK, partN);          \
-    *nblk = nb;                                                                                          \
+    if (ntile > nblk_cap) return cudaSuccess;                                                            \
+    k_fft4_x_bin<A_, B_><<<ntile, FS_THREADS, sm, st>>>(work, tw, nd, nc, bp, partP, partK, partN);       \
+    *nblk = ntile;                                                                                       \
     return cudaGetLastError();                                                                           \
   }
     EXH_FS_STRIDED_CASES(X)

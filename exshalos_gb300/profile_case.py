@@ -4,10 +4,16 @@
     python -m exshalos_gb300.profile_case pk     [--timing]   # CIC of the halos, then the 128-bin P(k)
     python -m exshalos_gb300.profile_case ladder [--timing]   # the 50-radius smoothing ladder
     python -m exshalos_gb300.profile_case fft                 # one 256^3 r2c + c2r round trip
+    python -m exshalos_gb300.profile_case grid512             # CIC of 512^3 particles, 256-bin P(k)
 
 Each runs one realisation of nd = 256, Lc = 2 Mpc/h (L = 512), 2LPT, barrier
 a = 1, beta = 0.12, seed 1 (about 1.5 GB on the device; every field and work
-array exceeds L2), after one untimed warm-up call of the same stage.  With
+array exceeds L2), after one untimed warm-up call of the same stage.
+grid512 runs the CIC and P(k) stage of the nd = 512 box (L = 1024 Mpc/h):
+512^3 particles in Lagrangian order at their cell centres moved by
+Gaussian displacements of 2 Mpc/h rms per axis (torch generator seeded 3),
+as the box's 2LPT particles arrive (about 4 GB on the device), the 512^3
+CIC grid, then P(k) in 256 bins.  With
 --timing the library's per-kernel-class timing is on: the quicksort levels
 and the growth rounds are then launched one by one from the host instead of
 as CUDA graphs, so a profiler can filter their kernels by name.
@@ -21,7 +27,7 @@ import numpy as np
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
-    ap.add_argument("stage", choices=("halos", "pk", "ladder", "fft"))
+    ap.add_argument("stage", choices=("halos", "pk", "ladder", "fft", "grid512"))
     ap.add_argument("--timing", action="store_true", help="per-kernel-class timing on (host-driven loops)")
     a = ap.parse_args(argv)
     import torch
@@ -67,9 +73,37 @@ def main(argv=None):
         _capi.check(lib.exh_fft_r2c_3d(ctx, nd, nd, nd, _capi.ptr(x), _capi.ptr(c), None))
         _capi.check(lib.exh_fft_c2r_3d(ctx, nd, nd, nd, _capi.ptr(c), _capi.ptr(x), None))
 
+    def grid512():
+        n5, Lc5, nk5 = 512, 2.0, 256
+        L5 = n5 * Lc5
+        g5 = torch.Generator(device="cuda").manual_seed(3)
+        q5 = (torch.arange(n5, device="cuda", dtype=torch.float32) + 0.5) * Lc5
+        pos5 = torch.empty((n5, n5, n5, 3), dtype=torch.float32, device="cuda")
+        pos5[..., 0] = q5.view(n5, 1, 1)
+        pos5[..., 1] = q5.view(1, n5, 1)
+        pos5[..., 2] = q5.view(1, 1, n5)
+        for s5 in range(0, n5, 64):                  # displacements slab by slab (small temporaries)
+            sl = pos5[s5:s5 + 64]
+            sl += torch.randn(sl.shape, generator=g5, device="cuda") * 2.0
+            sl.remainder_(L5)
+        pos5 = pos5.view(-1)
+        grid5 = torch.empty(n5 ** 3, dtype=torch.float32, device="cuda")
+        kmin5, kmax5 = np.float32(2 * np.pi / L5), np.float32(np.pi / L5 * n5)
+        ko5, po5, co5 = np.zeros(nk5, np.float32), np.zeros(nk5, np.float32), np.zeros(nk5, np.int64)
+
+        def run5():
+            _capi.check(lib.exh_grid_compute(ctx, _capi.ptr(pos5), n5 ** 3, n5, float(L5), 2, 1, _capi.ptr(grid5),
+                                             _capi.EXH_MEM_DEVICE, None))
+            _capi.check(lib.exh_power_compute(ctx, _capi.ptr(grid5), n5, float(L5), 2, nk5, float(kmin5),
+                                              float(kmax5), _capi.ptr(ko5), _capi.ptr(po5), _capi.ptr(co5),
+                                              _capi.EXH_MEM_DEVICE, None))
+        return run5
+
     if a.stage == "pk":
         halos()
         run = pk
+    elif a.stage == "grid512":
+        run = grid512()
     else:
         run = {"halos": halos, "ladder": ladder, "fft": fft}[a.stage]
     run()                     # warm-up: tables, plans and buffers settle

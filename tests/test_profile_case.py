@@ -17,7 +17,7 @@ def _run(*args):
 def test_help_lists_the_stages():
     r = _run("--help")
     assert r.returncode == 0
-    for stage in ("halos", "pk", "ladder", "fft"):
+    for stage in ("halos", "pk", "ladder", "fft", "grid512"):
         assert stage in r.stdout
 
 
